@@ -1,0 +1,446 @@
+"""Benchmark of the oibvh collision pipeline on one GB300 (or N replicas).
+
+Default workload ("deforming"): two noise-displaced icospheres at
+subdivision 8 (1,310,720 triangles, 655,362 vertices each), B placed by a
+seeded rigid transform with ~1% of its surface inside A. One step = one
+frame = one collision query: per-vertex Gaussian jitter (sigma 1e-3) on both
+meshes, refit both trees, BVTT broad phase (entry level 4, expand 3, the
+reference demo's settings), triangle narrow phase, pair count on the host.
+
+  value  queries/s with the frame's positions already in HBM
+  e2e    queries/s through the public C ABI with HOST buffers: the pinned
+         host positions are copied in, and the colliding pairs copied out,
+         inside every timed step
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload deforming|plain]
+
+--impl reference times the reference's CPU path (the oracle port; the
+reference's compiled sources cannot be built on the GPU host) on all host
+cores, one independent frame per thread.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "collision queries/s"
+UNIT = "queries/s"
+ENTRY_LEVEL, EXPAND_LEVELS = 4, 3  # src/main.cpp:284
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["deforming", "plain"], default="deforming")
+    ap.add_argument("--cpu-seconds", type=float, default=8.0, help="budget of the CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def make_workload(name):
+    from oibvh_gb300 import workloads as W
+
+    return W.deforming() if name == "deforming" else W.plain()
+
+
+def workload_config(w, args, extra=None):
+    m = w.meshes
+    cfg = {
+        "workload": w.name,
+        "meshes": len(m),
+        "triangles_per_mesh": [x.n_triangles for x in m],
+        "vertices_per_mesh": [x.n_vertices for x in m],
+        "entry_level": ENTRY_LEVEL,
+        "expand_levels": EXPAND_LEVELS,
+        "l2": "flushed between steps (256 MiB write, outside the timed events)",
+        "parallelism": f"replicas{args.gpus}",
+    }
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def jitter_frames(w, n_frames, seed=5):
+    """Host float32 positions per frame per mesh: rest + N(0, sigma^2), via torch's CPU generator."""
+    import torch
+
+    g = torch.Generator().manual_seed(seed)
+    frames = []
+    for f in range(n_frames):
+        per = []
+        for m in w.meshes:
+            base = torch.from_numpy(m.xyz)
+            if w.jitter_sigma:
+                x = base + torch.randn(base.shape, generator=g, dtype=torch.float32) * w.jitter_sigma
+            else:
+                x = base.clone()
+            per.append(x.contiguous())
+        frames.append(per)
+    return frames
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                smax.append(float(r[1]))
+            except (ValueError, IndexError):
+                continue
+            for k, n in enumerate(names):
+                if len(r) > 4 + k and r[4 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------- our arm
+def run_ours(args, rank, world, local):
+    import torch
+
+    from oibvh_gb300 import DeviceType, OibvhTree, Scene, _native
+
+    torch.cuda.set_device(local)
+    dev = local
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    w = make_workload(args.workload)
+    n_frames = args.warmup + args.steps
+    host_frames = jitter_frames(w, n_frames, seed=5 + rank)
+    pinned = [[x.pin_memory() for x in fr] for fr in host_frames]
+    dev_frames = [[x.to(f"cuda:{dev}") for x in fr] for fr in host_frames]
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+
+    trees = [OibvhTree(m, device=dev) for m in w.meshes]
+    for t in trees:
+        t.build(stream=sh)
+    sc = Scene(dev)
+    for t in trees:
+        sc.addOibvhTree(t)
+    L = _native.lib()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+
+    def step_device(f):
+        for t, x in zip(trees, dev_frames[f]):
+            t.refit_device(x.data_ptr(), stream=sh)
+        sc.detectCollision(DeviceType(dev), ENTRY_LEVEL, EXPAND_LEVELS, stream=sh)
+
+    hit_buf = torch.empty((1 << 22, 4), dtype=torch.int32).pin_memory()
+    hit_bytes = [0]
+
+    def step_e2e(f):
+        for t, x in zip(trees, pinned[f]):
+            # pinned host positions -> device copy inside the refit call
+            N_ = _native
+            N_.check(L.oibvh_tree_refit(t.handle, ctypes_f32(x), ctypes_stream(sh)), "oibvh_tree_refit")
+        sc.detectCollision(DeviceType(dev), ENTRY_LEVEL, EXPAND_LEVELS, stream=sh)
+        n = sc.getIntTriPairCount()
+        import ctypes as C
+
+        got = C.c_uint64()
+        cap = min(n, hit_buf.shape[0])
+        N_.check(L.oibvh_scene_get_int_tri_pairs(sc.handle, C.cast(C.c_void_p(hit_buf.data_ptr()), N_._u32p), cap,
+                                                  C.byref(got)), "oibvh_scene_get_int_tri_pairs")
+        hit_bytes[0] += 16 * cap
+
+    def timed(step_fn):
+        for f in range(args.warmup):
+            step_fn(f)
+        barrier()
+        flush.fill_(1)
+        barrier()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        launches0 = L.oibvh_get_launch_count()
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.fill_(k & 255)  # evict L2 between steps, outside the events
+            starts[k].record(stream)
+            step_fn(args.warmup + k)
+            ends[k].record(stream)
+        barrier()
+        wall = time.perf_counter() - wall0
+        launches = L.oibvh_get_launch_count() - launches0
+        ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+        return ms, wall, launches
+
+    sampler = ClockSampler(dev) if rank == 0 else None
+    if sampler:
+        sampler.start()
+    ms_dev, wall_dev, launches = timed(step_device)
+    stats = sc.stats()
+    hits = sc.getIntTriPairCount()
+    cands = sc.candidate_count()
+    hit_bytes[0] = 0
+    ms_e2e, wall_e2e, _ = timed(step_e2e)
+    clocks = sampler.stop() if sampler else None
+
+    # dominant kernel (refit) timed alone on the same stream, per launch
+    rf_s = [torch.cuda.Event(enable_timing=True) for _ in range(20)]
+    rf_e = [torch.cuda.Event(enable_timing=True) for _ in range(20)]
+    for k in range(20):
+        flush.fill_(k & 255)
+        rf_s[k].record(stream)
+        trees[k % 2].refit_device(dev_frames[0][k % 2].data_ptr(), stream=sh)
+        rf_e[k].record(stream)
+    torch.cuda.synchronize()
+    refit_ms = statistics.mean(s.elapsed_time(e) for s, e in zip(rf_s, rf_e))
+
+    # max over ranks
+    t_dev = torch.tensor([ms_dev, ms_e2e], dtype=torch.float64, device=f"cuda:{dev}")
+    if dist is not None:
+        dist.all_reduce(t_dev, op=dist.ReduceOp.MAX)
+    ms_dev, ms_e2e = float(t_dev[0]), float(t_dev[1])
+    if dist is not None:
+        dist.destroy_process_group()
+    if rank != 0:
+        return None
+
+    K = args.steps
+    queries = K * world
+    value = queries / (ms_dev / 1e3)
+    e2e = queries / (ms_e2e / 1e3)
+    tri_total = sum(m.n_triangles for m in w.meshes)
+    V = sum(m.n_vertices for m in w.meshes)
+    # refit algorithmic bytes per launch (one tree): 12 B per vertex read,
+    # 12 B per face read, 24 B per node written (compulsory, reference layout)
+    m0 = w.meshes[0]
+    size0 = 2 * m0.n_triangles + bin((1 << (m0.n_triangles - 1).bit_length()) - m0.n_triangles).count("1") - 1
+    refit_bytes = 12 * m0.n_vertices + 12 * m0.n_triangles + 24 * size0
+    peaks = load_peaks()
+    achieved = refit_bytes / (refit_ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC,
+        "value": round(value, 3),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": K,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_dev / K, 5),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded noise icospheres, per-frame Gaussian jitter)",
+        "config": workload_config(w, args),
+        "tri_pairs_per_s": round(cands * queries / (ms_dev / 1e3), 1),
+        "triangles_per_s": round(tri_total * queries / (ms_dev / 1e3), 1),
+        "hits_last_frame": hits,
+        "candidates_last_frame": cands,
+        "bvtt_nodes_last_frame": stats["nodes_tested"],
+        "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": 12 * V,
+                "d2h_bytes_per_step": int(hit_bytes[0] / max(1, K)), "ms_per_step": round(ms_e2e / K, 5)},
+        "roofline": {"kernel": "k_refit (one tree: leaf boxes + every level)", "bound": "hbm",
+                     "achieved": round(achieved, 1), "peak": peaks[0], "unit": "GB/s",
+                     "frac": round(achieved / peaks[0], 4), "peak_source": peaks[1],
+                     "algorithmic_bytes_per_launch": refit_bytes, "launch_ms": round(refit_ms, 5),
+                     "traffic": None},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "wall_s": round(wall_dev, 3),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample(w, args.cpu_seconds)
+    return line
+
+
+def ctypes_f32(t):
+    import ctypes
+
+    return ctypes.cast(ctypes.c_void_p(t.data_ptr()), ctypes.POINTER(ctypes.c_float))
+
+
+def ctypes_stream(h):
+    import ctypes
+
+    return ctypes.c_void_p(h)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (of measured)"
+    except Exception:
+        return 6800.0, "fallback 6.8 TB/s (of fallback)"
+
+
+# --------------------------------------------------------------------------- CPU
+def cpu_baseline_sample(w, seconds, threads=1):
+    """The oracle port (C restatement of the reference CPU path) on this host:
+    one frame = refit both SimpleBVHs to the frame's positions + detect."""
+    from oracle.oracle import Port
+
+    frames = jitter_frames(w, 64, seed=99)
+
+    def worker(out, idx0, stride, deadline):
+        p = Port()
+        for m in w.meshes:
+            p.add_mesh(m.xyz, m.tri)
+        n = 0
+        f = idx0
+        while time.perf_counter() < deadline or n == 0:
+            fr = frames[f % len(frames)]
+            for i, x in enumerate(fr):
+                p.set_positions(i, x.numpy())
+            p.detect()
+            n += 1
+            f += stride
+        out.append(n)
+
+    out = []
+    # build (not timed) happens inside the workers; give it a head start
+    t0 = time.perf_counter()
+    deadline = t0 + seconds
+    ths = [threading.Thread(target=worker, args=(out, k, threads, deadline)) for k in range(threads)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    el = time.perf_counter() - t0
+    n = sum(out)
+    return {"value": round(n / el, 3), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} frames of the workload (refit both + detect) in {el:.1f} s, build included"}
+
+
+def run_reference(args, rank, world):
+    """The reference arm: the reference CPU path (oracle port) on all host cores."""
+    if rank != 0:
+        return None
+    w = make_workload(args.workload)
+    threads = os.cpu_count() or 1
+    from oracle.oracle import Port
+
+    frames = jitter_frames(w, max(8, threads), seed=5)
+    scenes = [None] * threads
+
+    def setup(k):
+        p = Port()
+        for m in w.meshes:
+            p.add_mesh(m.xyz, m.tri)
+        scenes[k] = p
+
+    ths = [threading.Thread(target=setup, args=(k,)) for k in range(threads)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+
+    def one_step(step):
+        def work(k):
+            fr = frames[(step * threads + k) % len(frames)]
+            for i, x in enumerate(fr):
+                scenes[k].set_positions(i, x.numpy())
+            scenes[k].detect()
+
+        ts = [threading.Thread(target=work, args=(k,)) for k in range(threads)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+
+    for s in range(args.warmup):
+        one_step(s)
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        one_step(args.warmup + s)
+    el = time.perf_counter() - t0
+    q = args.steps * threads
+    value = q / el
+    return {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1e3 * el / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded noise icospheres, per-frame Gaussian jitter)",
+        "config": workload_config(w, args, {"parallelism": f"{threads} host threads, one frame each per step"}),
+        "impl": "reference",
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{q} frames (refit both + detect), {threads} per step"},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's C++ sources are not on the GPU host; the C restatement of its CPU path runs instead",
+    }
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        line = run_ours(args, rank, world, local)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,178 @@
+/*
+ * oibvh_gb300 — C ABI of the GB300 (sm_103a) oibvh collision pipeline.
+ *
+ * The reference (hhhcbw/oibvh) exposes this path only as C++ classes:
+ * OibvhTree (include/cuda/oibvhTree.cuh:50-93) and Scene
+ * (include/cuda/scene.cuh:44-61). Each entry point below replaces one of
+ * their members; the comment names the member it stands for (file:line in
+ * the reference). Plain pointers and sizes only: positions are float xyz
+ * triples (the Vertex::m_position field of include/utils/mesh.h:23-53),
+ * faces are uint32 index triples (Mesh::m_indices, include/utils/mesh.h:183).
+ *
+ * Conventions (the reference ignores every CUDA error, include/cuda/utils.cuh:
+ * 6-34; here nothing is ignored):
+ *   - every call returns an OIBVH_* status; 0 is success; oibvh_last_error()
+ *     gives a one-line reason for the last failure on the calling thread;
+ *   - a handle is used by one host thread at a time;
+ *   - `stream` is a cudaStream_t (NULL = the legacy default stream); calls
+ *     documented as blocking synchronise that stream before returning,
+ *     the others only enqueue work on it;
+ *   - there is no CPU fallback: a device type of CPU is refused
+ *     (the reference's detectCollisionOnCPU is an empty TODO,
+ *     src/cuda/scene.cu:187-190).
+ *
+ * Limits: 1 <= triangles per mesh <= 2^23; at most 2^16 mesh pairs are
+ * traversed per pass (more are processed in several passes).
+ */
+#ifndef OIBVH_GB300_H
+#define OIBVH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum oibvh_status {
+    OIBVH_OK = 0,
+    OIBVH_ERR_ARG = 1,         /* invalid argument (null, size, index out of range) */
+    OIBVH_ERR_OOM = 2,         /* device or pinned host allocation failed */
+    OIBVH_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+    OIBVH_ERR_OVERFLOW = 4,    /* a work queue stayed too small after regrowing */
+    OIBVH_ERR_STATE = 5,       /* call out of order (e.g. detect before build) */
+    OIBVH_ERR_UNSUPPORTED = 6, /* e.g. the CPU device type */
+};
+
+/* DeviceType (include/cuda/scene.cuh:12-24): CPU = -1, GPU0..GPU8 = 0..8. */
+#define OIBVH_DEVICE_CPU (-1)
+#define OIBVH_DEVICE_GPU0 0
+
+typedef struct oibvh_tree_s* oibvh_tree_t;
+typedef struct oibvh_scene_s* oibvh_scene_t;
+
+/* Text of a status code, and the last failure reason on this thread. */
+const char* oibvh_status_string(int status);
+const char* oibvh_last_error(void);
+/* Library version: major * 10000 + minor * 100 + patch. */
+int oibvh_version(void);
+/* Kernels this library has launched so far in this process (all devices). */
+uint64_t oibvh_get_launch_count(void);
+
+/* ------------------------------------------------------------------ tree */
+
+/* OibvhTree::OibvhTree(std::shared_ptr<Mesh>) + setup()
+ * (src/cuda/oibvhTree.cu:9-15,157-191): copies the mesh's positions and
+ * faces to `device`. Face indices are checked against n_vertices. */
+int oibvh_tree_create(const float* xyz, uint32_t n_vertices, const uint32_t* tri, uint32_t n_triangles, int device,
+                      oibvh_tree_t* out);
+
+/* OibvhTree::OibvhTree(std::shared_ptr<OibvhTree>, std::shared_ptr<Mesh>)
+ * (src/cuda/oibvhTree.cu:17-33): a tree over a copy of `other`'s mesh with
+ * new positions. It keeps `other`'s Morton order (the reference never
+ * rebuilds a copied tree, src/main.cpp:132-135); call oibvh_tree_refit next.
+ * `other` must be built. */
+int oibvh_tree_create_copy(oibvh_tree_t other, const float* xyz, uint32_t n_vertices, oibvh_tree_t* out);
+
+/* OibvhTree::build() (src/cuda/oibvhTree.cu:237-388): mesh bounds, Morton
+ * codes, stable radix sort, then every tree level. Blocking. */
+int oibvh_tree_build(oibvh_tree_t t, void* stream);
+
+/* OibvhTree::refit() (src/cuda/oibvhTree.cu:193-235): new leaf boxes from the
+ * mesh's current positions, then every level. `xyz` is a host array of
+ * 3 * n_vertices floats copied to the device first, or NULL to refit to the
+ * positions already held. Stream-ordered (not blocking). */
+int oibvh_tree_refit(oibvh_tree_t t, const float* xyz, void* stream);
+
+/* Same as oibvh_tree_refit with positions already in device memory. The
+ * tree keeps using `d_xyz` (no copy) until the next refit: the caller keeps
+ * it alive and unchanged until every detect that uses this tree is done. */
+int oibvh_tree_refit_device(oibvh_tree_t t, const float* d_xyz, void* stream);
+
+/* OibvhTree::getDepth() (src/cuda/oibvhTree.cu:46-49) = floor(log2(size)). */
+uint32_t oibvh_tree_get_depth(oibvh_tree_t t);
+/* OibvhTree::getPrimCount() (src/cuda/oibvhTree.cu:51-54). */
+uint32_t oibvh_tree_get_prim_count(oibvh_tree_t t);
+/* m_aabbTree.size() (src/cuda/oibvhTree.cu:375): oibvh_get_size(T). */
+uint32_t oibvh_tree_get_size(oibvh_tree_t t);
+
+/* m_aabbTree (src/cuda/oibvhTree.cu:232,375-376): the level-ordered real
+ * nodes, root first, 6 floats each (min xyz, max xyz). Blocking. */
+int oibvh_tree_get_aabbs(oibvh_tree_t t, float* out6, uint64_t cap_nodes);
+
+/* m_faces after build (src/cuda/oibvhTree.cu:377): the faces in Morton
+ * order, and perm[i] = original index of sorted face i (either output may be
+ * NULL). Blocking. */
+int oibvh_tree_get_sorted_faces(oibvh_tree_t t, uint32_t* out3, uint32_t* perm, uint64_t cap);
+
+int oibvh_tree_destroy(oibvh_tree_t t);
+
+/* ----------------------------------------------------------------- scene */
+
+/* Scene::Scene() (src/cuda/scene.cu:12-34) on a device. */
+int oibvh_scene_create(int device, oibvh_scene_t* out);
+
+/* Scene::addOibvhTree (src/cuda/scene.cu:95-129). The scene refers to the
+ * tree (no copy); *id is its index, reported as bvhIndex in the pairs. */
+int oibvh_scene_add_tree(oibvh_scene_t s, oibvh_tree_t t, uint32_t* id);
+
+/* Which tree pairs are tested. pairs = NULL (the default) means every i < j,
+ * the reference's behaviour (src/cuda/scene.cu:195-196); otherwise n_pairs
+ * (a, b) id pairs, a != b. */
+int oibvh_scene_set_pairs(oibvh_scene_t s, const uint32_t* pairs, uint32_t n_pairs);
+
+/* Scene::detectCollision(deviceType, entryLevel, expandLevels)
+ * (src/cuda/scene.cu:157-185,225-446): BVTT broad phase from the cross
+ * product of the nodes at entry_level (clamped to each tree's leaf level),
+ * expanding expand_levels (1..16) levels per step, then the triangle test.
+ * Blocking: returns once the pair count is known. */
+int oibvh_scene_detect(oibvh_scene_t s, int device_type, uint32_t entry_level, uint32_t expand_levels, void* stream);
+
+/* The two halves of detect (src/cuda/scene.cu:270-311 and :382-423):
+ * broad leaves the candidate leaf pairs on the device (blocking, it reads
+ * their count); narrow tests them (blocking). */
+int oibvh_scene_broad(oibvh_scene_t s, int device_type, uint32_t entry_level, uint32_t expand_levels, void* stream);
+int oibvh_scene_narrow(oibvh_scene_t s, void* stream);
+
+/* Scene::getIntTriPairCount() (src/cuda/scene.cu:50-53). */
+uint32_t oibvh_scene_get_int_tri_pair_count(oibvh_scene_t s);
+/* Candidate (overlapping leaf box) pairs of the last broad phase
+ * (printed by the reference at src/cuda/scene.cu:316-322). */
+uint64_t oibvh_scene_get_candidate_count(oibvh_scene_t s);
+
+/* m_intTriPairs (include/cuda/scene.cuh:133; private in the reference):
+ * records {bvhA, bvhB, triA, triB}, 4 uint32 each, tri indices are the
+ * ORIGINAL face indices of each mesh, in no particular order. Writes
+ * min(cap, count) records, *n = count. Blocking. */
+int oibvh_scene_get_int_tri_pairs(oibvh_scene_t s, uint32_t* out4, uint64_t cap, uint64_t* n);
+
+/* Candidate leaf pairs of the last broad phase as {bvhA, bvhB, sortedA,
+ * sortedB} records (Morton-order leaf indices, the reference GPU path's
+ * tri_pair_node_t). Blocking. */
+int oibvh_scene_get_candidates(oibvh_scene_t s, uint32_t* out4, uint64_t cap, uint64_t* n);
+
+/* Starting capacities (entries) of the BVTT front, candidate and hit queues.
+ * They grow on demand (an overflow is detected on the device and the pass
+ * reruns), so this only trades memory against reruns. 0 keeps a value. */
+int oibvh_scene_set_queue_capacity(oibvh_scene_t s, uint32_t front, uint32_t candidates, uint32_t hits);
+
+/* Per-detect diagnostics: passes, BVTT steps, queue regrowths, nodes tested. */
+typedef struct oibvh_detect_stats {
+    uint32_t passes;         /* pair batches */
+    uint32_t steps;          /* BVTT steps of the last pass */
+    uint32_t retries;        /* queue regrowths */
+    uint32_t pad0;
+    uint64_t nodes_tested;   /* BVTT nodes tested, all passes */
+    uint64_t candidates;
+    uint64_t hits;
+    uint64_t front_peak;     /* largest front */
+} oibvh_detect_stats;
+int oibvh_scene_get_stats(oibvh_scene_t s, oibvh_detect_stats* out);
+
+int oibvh_scene_destroy(oibvh_scene_t s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OIBVH_GB300_H */

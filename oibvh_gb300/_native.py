@@ -1,0 +1,131 @@
+"""ctypes binding of the C ABI in include/oibvh_gb300.h.
+
+The CUDA library is built in-tree (oibvh_gb300/_lib/liboibvh_gb300.so, see
+build.py). There is no fallback: if the library is missing or fails to load,
+``lib()`` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_f32p = ctypes.POINTER(ctypes.c_float)
+_vp = ctypes.c_void_p
+_u32 = ctypes.c_uint32
+_u64 = ctypes.c_uint64
+
+OK = 0
+ERR_ARG = 1
+ERR_OOM = 2
+ERR_CUDA = 3
+ERR_OVERFLOW = 4
+ERR_STATE = 5
+ERR_UNSUPPORTED = 6
+
+DEVICE_CPU = -1
+
+
+class DetectStats(ctypes.Structure):
+    _fields_ = [
+        ("passes", ctypes.c_uint32),
+        ("steps", ctypes.c_uint32),
+        ("retries", ctypes.c_uint32),
+        ("pad0", ctypes.c_uint32),
+        ("nodes_tested", ctypes.c_uint64),
+        ("candidates", ctypes.c_uint64),
+        ("hits", ctypes.c_uint64),
+        ("front_peak", ctypes.c_uint64),
+    ]
+
+
+# (name, restype, argtypes) for every symbol of include/oibvh_gb300.h
+SIGNATURES = [
+    ("oibvh_status_string", ctypes.c_char_p, [ctypes.c_int]),
+    ("oibvh_last_error", ctypes.c_char_p, []),
+    ("oibvh_version", ctypes.c_int, []),
+    ("oibvh_get_launch_count", _u64, []),
+    ("oibvh_tree_create", ctypes.c_int, [_f32p, _u32, _u32p, _u32, ctypes.c_int, ctypes.POINTER(_vp)]),
+    ("oibvh_tree_create_copy", ctypes.c_int, [_vp, _f32p, _u32, ctypes.POINTER(_vp)]),
+    ("oibvh_tree_build", ctypes.c_int, [_vp, _vp]),
+    ("oibvh_tree_refit", ctypes.c_int, [_vp, _f32p, _vp]),
+    ("oibvh_tree_refit_device", ctypes.c_int, [_vp, _vp, _vp]),
+    ("oibvh_tree_get_depth", _u32, [_vp]),
+    ("oibvh_tree_get_prim_count", _u32, [_vp]),
+    ("oibvh_tree_get_size", _u32, [_vp]),
+    ("oibvh_tree_get_aabbs", ctypes.c_int, [_vp, _f32p, _u64]),
+    ("oibvh_tree_get_sorted_faces", ctypes.c_int, [_vp, _u32p, _u32p, _u64]),
+    ("oibvh_tree_destroy", ctypes.c_int, [_vp]),
+    ("oibvh_scene_create", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_vp)]),
+    ("oibvh_scene_add_tree", ctypes.c_int, [_vp, _vp, _u32p]),
+    ("oibvh_scene_set_pairs", ctypes.c_int, [_vp, _u32p, _u32]),
+    ("oibvh_scene_detect", ctypes.c_int, [_vp, ctypes.c_int, _u32, _u32, _vp]),
+    ("oibvh_scene_broad", ctypes.c_int, [_vp, ctypes.c_int, _u32, _u32, _vp]),
+    ("oibvh_scene_narrow", ctypes.c_int, [_vp, _vp]),
+    ("oibvh_scene_get_int_tri_pair_count", _u32, [_vp]),
+    ("oibvh_scene_get_candidate_count", _u64, [_vp]),
+    ("oibvh_scene_get_int_tri_pairs", ctypes.c_int, [_vp, _u32p, _u64, ctypes.POINTER(_u64)]),
+    ("oibvh_scene_get_candidates", ctypes.c_int, [_vp, _u32p, _u64, ctypes.POINTER(_u64)]),
+    ("oibvh_scene_set_queue_capacity", ctypes.c_int, [_vp, _u32, _u32, _u32]),
+    ("oibvh_scene_get_stats", ctypes.c_int, [_vp, ctypes.POINTER(DetectStats)]),
+    ("oibvh_scene_destroy", ctypes.c_int, [_vp]),
+]
+
+_lib = None
+_lock = threading.Lock()
+
+
+class OibvhError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, status: int, func: str, detail: str):
+        self.status = status
+        self.func = func
+        super().__init__(f"{func} failed: {status_string(status)} ({status}): {detail}")
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(path: str | None = None, auto_build: bool = False):
+    """Load the library (build it first when auto_build and it is stale)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or lib_path()
+        if auto_build and not _build.up_to_date():
+            _build.build()
+        if not os.path.exists(p):
+            raise RuntimeError(
+                f"oibvh_gb300 CUDA library not found at {p}; build it with `python -m oibvh_gb300.build` "
+                "(there is no CPU fallback)"
+            )
+        L = ctypes.CDLL(p)
+        for name, res, args in SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+        return _lib
+
+
+def lib():
+    return load(auto_build=os.environ.get("OIBVH_AUTO_BUILD", "1") == "1")
+
+
+def status_string(status: int) -> str:
+    try:
+        return lib().oibvh_status_string(status).decode()
+    except Exception:  # library not loadable: still give a name
+        return {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "queue overflow",
+                5: "invalid state", 6: "unsupported"}.get(status, "unknown status")
+
+
+def check(status: int, func: str) -> None:
+    if status != OK:
+        raise OibvhError(status, func, lib().oibvh_last_error().decode(errors="replace"))

@@ -1,0 +1,244 @@
+"""Python mirror of the reference's tree / scene interface, over the C ABI.
+
+    OibvhTree(mesh)            -> OibvhTree::OibvhTree   (src/cuda/oibvhTree.cu:9-15)
+    OibvhTree.copy_of(o, mesh) -> OibvhTree(other, mesh) (src/cuda/oibvhTree.cu:17-33)
+    tree.build()               -> OibvhTree::build       (src/cuda/oibvhTree.cu:237-388)
+    tree.refit(xyz)            -> OibvhTree::refit       (src/cuda/oibvhTree.cu:193-235)
+    tree.getDepth(), getPrimCount()                      (src/cuda/oibvhTree.cu:46-54)
+    Scene().addOibvhTree(tree)                           (src/cuda/scene.cu:95-129)
+    scene.detectCollision(DeviceType.GPU0, 4, 3)         (src/cuda/scene.cu:157-185)
+    scene.getIntTriPairCount()                           (src/cuda/scene.cu:50-53)
+
+Every call goes through liboibvh_gb300.so; errors raise OibvhError with the
+library's status code (the reference ignores them).
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+
+import numpy as np
+
+from . import _native as N
+from .meshes import Mesh
+
+__all__ = ["DeviceType", "OibvhTree", "Scene", "OibvhError"]
+
+OibvhError = N.OibvhError
+
+
+class DeviceType(enum.IntEnum):
+    """include/cuda/scene.cuh:12-24"""
+
+    CPU = -1
+    GPU0 = 0
+    GPU1 = 1
+    GPU2 = 2
+    GPU3 = 3
+    GPU4 = 4
+    GPU5 = 5
+    GPU6 = 6
+    GPU7 = 7
+    GPU8 = 8
+
+
+def _stream_handle(stream) -> ctypes.c_void_p:
+    if stream is None:
+        return ctypes.c_void_p(None)
+    if isinstance(stream, int):
+        return ctypes.c_void_p(stream)
+    h = getattr(stream, "cuda_stream", None)  # torch.cuda.Stream
+    if h is not None:
+        return ctypes.c_void_p(int(h))
+    raise TypeError("stream must be None, an int handle or a torch.cuda.Stream")
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class OibvhTree:
+    """An oibvh over one triangle mesh, resident on one GPU."""
+
+    def __init__(self, mesh: Mesh | None = None, *, xyz=None, tri=None, device: int = 0, _handle=None):
+        self._h = ctypes.c_void_p(None)
+        self._nv = 0
+        if _handle is not None:
+            self._h = _handle
+            return
+        if mesh is not None:
+            xyz, tri = mesh.xyz, mesh.tri
+        x = _f32(xyz).reshape(-1, 3)
+        t = np.ascontiguousarray(tri, dtype=np.uint32).reshape(-1, 3)
+        h = ctypes.c_void_p()
+        N.check(
+            N.lib().oibvh_tree_create(
+                x.ctypes.data_as(N._f32p), x.shape[0], t.ctypes.data_as(N._u32p), t.shape[0], int(device),
+                ctypes.byref(h)),
+            "oibvh_tree_create",
+        )
+        self._h = h
+        self._nv = int(x.shape[0])
+
+    @classmethod
+    def copy_of(cls, other: "OibvhTree", mesh: Mesh | None = None, *, xyz=None) -> "OibvhTree":
+        x = _f32(mesh.xyz if mesh is not None else xyz).reshape(-1, 3)
+        h = ctypes.c_void_p()
+        N.check(N.lib().oibvh_tree_create_copy(other._h, x.ctypes.data_as(N._f32p), x.shape[0], ctypes.byref(h)),
+                "oibvh_tree_create_copy")
+        t = cls(_handle=h)
+        t._nv = int(x.shape[0])
+        return t
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                N.lib().oibvh_tree_destroy(h)
+            except Exception:
+                pass
+            self._h = ctypes.c_void_p(None)
+
+    close = __del__
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def build(self, stream=None) -> None:
+        N.check(N.lib().oibvh_tree_build(self._h, _stream_handle(stream)), "oibvh_tree_build")
+
+    def refit(self, xyz=None, stream=None) -> None:
+        """Refit to host positions `xyz` (float32[V,3]), or to the positions
+        already held when None. Stream-ordered."""
+        if xyz is None:
+            N.check(N.lib().oibvh_tree_refit(self._h, None, _stream_handle(stream)), "oibvh_tree_refit")
+            return
+        x = _f32(xyz)
+        if x.size != 3 * self.vertex_count:
+            raise ValueError("refit positions must be float32[V,3]")
+        N.check(N.lib().oibvh_tree_refit(self._h, x.ctypes.data_as(N._f32p), _stream_handle(stream)),
+                "oibvh_tree_refit")
+        self._keep = x  # pageable source: copied before the call returns, kept for safety
+
+    def refit_device(self, d_xyz_ptr: int, stream=None) -> None:
+        """Refit to positions in device memory (a raw pointer, e.g. tensor.data_ptr())."""
+        N.check(N.lib().oibvh_tree_refit_device(self._h, ctypes.c_void_p(int(d_xyz_ptr)), _stream_handle(stream)),
+                "oibvh_tree_refit_device")
+
+    # reference accessors
+    def getDepth(self) -> int:
+        return int(N.lib().oibvh_tree_get_depth(self._h))
+
+    def getPrimCount(self) -> int:
+        return int(N.lib().oibvh_tree_get_prim_count(self._h))
+
+    @property
+    def size(self) -> int:
+        return int(N.lib().oibvh_tree_get_size(self._h))
+
+    @property
+    def vertex_count(self) -> int:
+        return self._nv
+
+    def aabb_tree(self) -> np.ndarray:
+        """m_aabbTree: float32[size, 6] (min xyz, max xyz), level-ordered."""
+        out = np.empty((self.size, 6), dtype=np.float32)
+        N.check(N.lib().oibvh_tree_get_aabbs(self._h, out.ctypes.data_as(N._f32p), out.shape[0]),
+                "oibvh_tree_get_aabbs")
+        return out
+
+    def sorted_faces(self) -> tuple[np.ndarray, np.ndarray]:
+        n = self.getPrimCount()
+        f = np.empty((n, 3), dtype=np.uint32)
+        p = np.empty(n, dtype=np.uint32)
+        N.check(N.lib().oibvh_tree_get_sorted_faces(self._h, f.ctypes.data_as(N._u32p), p.ctypes.data_as(N._u32p), n),
+                "oibvh_tree_get_sorted_faces")
+        return f, p
+
+
+class Scene:
+    """A set of trees tested pairwise on one GPU."""
+
+    def __init__(self, device: int = 0):
+        h = ctypes.c_void_p()
+        N.check(N.lib().oibvh_scene_create(int(device), ctypes.byref(h)), "oibvh_scene_create")
+        self._h = h
+        self._trees = []
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                N.lib().oibvh_scene_destroy(h)
+            except Exception:
+                pass
+            self._h = ctypes.c_void_p(None)
+
+    close = __del__
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def addOibvhTree(self, tree: OibvhTree) -> int:
+        i = ctypes.c_uint32()
+        N.check(N.lib().oibvh_scene_add_tree(self._h, tree.handle, ctypes.byref(i)), "oibvh_scene_add_tree")
+        self._trees.append(tree)
+        return int(i.value)
+
+    def set_pairs(self, pairs=None) -> None:
+        if pairs is None:
+            N.check(N.lib().oibvh_scene_set_pairs(self._h, None, 0), "oibvh_scene_set_pairs")
+            return
+        p = np.ascontiguousarray(pairs, dtype=np.uint32).reshape(-1, 2)
+        N.check(N.lib().oibvh_scene_set_pairs(self._h, p.ctypes.data_as(N._u32p), p.shape[0]),
+                "oibvh_scene_set_pairs")
+
+    def detectCollision(self, deviceType: int = DeviceType.GPU0, entryLevel: int = 0, expandLevels: int = 1,
+                        stream=None) -> None:
+        N.check(N.lib().oibvh_scene_detect(self._h, int(deviceType), int(entryLevel), int(expandLevels),
+                                           _stream_handle(stream)), "oibvh_scene_detect")
+
+    def broad(self, deviceType: int = DeviceType.GPU0, entryLevel: int = 0, expandLevels: int = 1,
+              stream=None) -> None:
+        N.check(N.lib().oibvh_scene_broad(self._h, int(deviceType), int(entryLevel), int(expandLevels),
+                                          _stream_handle(stream)), "oibvh_scene_broad")
+
+    def narrow(self, stream=None) -> None:
+        N.check(N.lib().oibvh_scene_narrow(self._h, _stream_handle(stream)), "oibvh_scene_narrow")
+
+    def getIntTriPairCount(self) -> int:
+        return int(N.lib().oibvh_scene_get_int_tri_pair_count(self._h))
+
+    def candidate_count(self) -> int:
+        return int(N.lib().oibvh_scene_get_candidate_count(self._h))
+
+    def int_tri_pairs(self, sort: bool = True) -> np.ndarray:
+        """uint32[n, 4] records {bvhA, bvhB, triA, triB} with original face indices."""
+        n = ctypes.c_uint64()
+        cnt = self.getIntTriPairCount()
+        out = np.empty((max(cnt, 1), 4), dtype=np.uint32)
+        N.check(N.lib().oibvh_scene_get_int_tri_pairs(self._h, out.ctypes.data_as(N._u32p), cnt, ctypes.byref(n)),
+                "oibvh_scene_get_int_tri_pairs")
+        out = out[: int(n.value)]
+        if sort and out.shape[0]:
+            out = out[np.lexsort((out[:, 3], out[:, 2], out[:, 1], out[:, 0]))]
+        return out
+
+    def candidates(self) -> np.ndarray:
+        n = ctypes.c_uint64()
+        cnt = self.candidate_count()
+        out = np.empty((max(cnt, 1), 4), dtype=np.uint32)
+        N.check(N.lib().oibvh_scene_get_candidates(self._h, out.ctypes.data_as(N._u32p), cnt, ctypes.byref(n)),
+                "oibvh_scene_get_candidates")
+        return out[: int(n.value)]
+
+    def set_queue_capacity(self, front: int = 0, candidates: int = 0, hits: int = 0) -> None:
+        N.check(N.lib().oibvh_scene_set_queue_capacity(self._h, int(front), int(candidates), int(hits)),
+                "oibvh_scene_set_queue_capacity")
+
+    def stats(self) -> dict:
+        st = N.DetectStats()
+        N.check(N.lib().oibvh_scene_get_stats(self._h, ctypes.byref(st)), "oibvh_scene_get_stats")
+        return {k: int(getattr(st, k)) for k, _ in N.DetectStats._fields_ if k != "pad0"}

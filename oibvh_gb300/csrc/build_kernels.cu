@@ -1,0 +1,334 @@
+// Build-time kernels: mesh bounds, leaf boxes + Morton codes, the stable
+// LSD radix sort of the codes, and the gather of Morton-ordered faces.
+//
+// Reference: src/cuda/oibvh.cu:6-70 (strech_by_3, morton3D,
+// calculate_aabb_and_morton_kernel) and src/cuda/oibvhTree.cu:253-299
+// (mesh bounds from Mesh::m_aabb, two thrust::stable_sort_by_key calls).
+// Here one stable sort of (code, face index) replaces the two payload sorts
+// and the permutation is kept, so faces are gathered once into a 16-byte
+// record (v0, v1, v2, original index).
+#include "oibvh_common.cuh"
+#include "oibvh_launch.h"
+
+namespace oibvh {
+
+// ---------------------------------------------------------------------------
+// Mesh bounds (src/utils/mesh.cpp:91-98): exact min/max over every vertex,
+// accumulated as order-preserving unsigned keys with atomicMin/atomicMax.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t float_to_ordered(float f)
+{
+    const uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float ordered_to_float(uint32_t k)
+{
+    const uint32_t b = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    return __uint_as_float(b);
+}
+
+__global__ void k_bounds_init(uint32_t* keys)
+{
+    if (threadIdx.x < 3) {
+        keys[threadIdx.x] = 0xffffffffu;  // min accumulators
+        keys[3 + threadIdx.x] = 0u;       // max accumulators
+    }
+}
+
+__global__ void __launch_bounds__(256) k_mesh_bounds(const float* __restrict__ xyz, uint32_t nV, uint32_t* keys)
+{
+    uint32_t mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu};
+    uint32_t mx[3] = {0u, 0u, 0u};
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const uint32_t o = float_to_ordered(__ldg(xyz + 3 * (size_t)v + k));
+            mn[k] = min(mn[k], o);
+            mx[k] = max(mx[k], o);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        for (int s = 16; s > 0; s >>= 1) {
+            mn[k] = min(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], s));
+            mx[k] = max(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], s));
+        }
+    }
+    __shared__ uint32_t smn[3][8], smx[3][8];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
+        for (int k = 0; k < 3; ++k) {
+            smn[k][w] = mn[k];
+            smx[k][w] = mx[k];
+        }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int k = threadIdx.x;
+        uint32_t a = 0xffffffffu, b = 0u;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+            a = min(a, smn[k][i]);
+            b = max(b, smx[k][i]);
+        }
+        atomicMin(keys + k, a);
+        atomicMax(keys + 3 + k, b);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Leaf boxes + Morton codes (src/cuda/oibvh.cu:6-22,42-70). The float ops are
+// the reference's, each rounded on its own (the *0.5f and *1024.0f scalings
+// are exact, the one division is IEEE round-to-nearest).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t stretch3(uint32_t x)
+{
+    x &= 0x3ffu;
+    x = (x | (x << 16)) & 0x30000ffu;
+    x = (x | (x << 8)) & 0x300f00fu;
+    x = (x | (x << 4)) & 0x30c30c3u;
+    x = (x | (x << 2)) & 0x9249249u;
+    return x;
+}
+
+__device__ __forceinline__ uint32_t quant1024(float u)
+{
+    float v = __fmul_rn(u, 1024.0f);
+    v = (v < 0.0f) ? 0.0f : v;        // thrust::max(v, 0.0f)
+    v = (1023.0f < v) ? 1023.0f : v;  // thrust::min(v, 1023.0f)
+    return __float2uint_rz(v);        // NaN -> 0
+}
+
+__global__ void __launch_bounds__(256) k_leaf_morton(const uint32_t* __restrict__ tri, const float* __restrict__ xyz,
+                                                     uint32_t nT, const uint32_t* __restrict__ bound_keys,
+                                                     uint32_t* __restrict__ codes, uint32_t* __restrict__ idx)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nT) return;
+    float bmin[3], bmax[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        bmin[k] = ordered_to_float(bound_keys[k]);
+        bmax[k] = ordered_to_float(bound_keys[3 + k]);
+    }
+    const uint32_t f0 = __ldg(tri + 3 * (size_t)i), f1 = __ldg(tri + 3 * (size_t)i + 1),
+                   f2 = __ldg(tri + 3 * (size_t)i + 2);
+    uint32_t q[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float a = __ldg(xyz + 3 * (size_t)f0 + k), b = __ldg(xyz + 3 * (size_t)f1 + k),
+                    c = __ldg(xyz + 3 * (size_t)f2 + k);
+        const float mn = gmin(gmin(a, b), c), mx = gmax(gmax(a, b), c);
+        const float centroid = __fmul_rn(__fadd_rn(mn, mx), 0.5f);
+        const float off = __fsub_rn(centroid, bmin[k]);
+        const float len = __fsub_rn(bmax[k], bmin[k]);
+        q[k] = quant1024(__fdiv_rn(off, len));
+    }
+    codes[i] = (stretch3(q[0]) << 2) | (stretch3(q[1]) << 1) | stretch3(q[2]);
+    idx[i] = i;
+}
+
+// ---------------------------------------------------------------------------
+// Stable LSD radix sort, 8-bit digits. A tile is 2048 consecutive items
+// (8 warps x 8 rounds x 32 lanes); ranks inside a tile come from
+// __match_any_sync peer groups in item order, so equal digits keep their
+// input order and the sort is stable, as thrust::stable_sort_by_key is.
+// ---------------------------------------------------------------------------
+constexpr int kRsThreads = 256;
+constexpr int kRsRounds = 8;
+constexpr int kRsTile = kRsThreads * kRsRounds;
+
+__global__ void __launch_bounds__(kRsThreads) k_rs_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift,
+                                                        uint32_t* __restrict__ hist, uint32_t n_tiles)
+{
+    __shared__ uint32_t cnt[256];
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * kRsTile;
+#pragma unroll
+    for (int r = 0; r < kRsRounds; ++r) {
+        const uint32_t i = base + r * kRsThreads + threadIdx.x;
+        if (i < n) atomicAdd(&cnt[(__ldg(keys + i) >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[(size_t)threadIdx.x * n_tiles + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// Block-wide exclusive scan of one value per thread (256 threads).
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total, uint32_t* sh /*[8]*/)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int s = 1; s < 32; s <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, s);
+        if (lane >= s) x += y;
+    }
+    if (lane == 31) sh[w] = x;
+    __syncthreads();
+    uint32_t wpre = 0, tot = 0;
+#pragma unroll
+    for (int i = 0; i < kRsThreads / 32; ++i) {
+        const uint32_t t = sh[i];
+        if (i < w) wpre += t;
+        tot += t;
+    }
+    __syncthreads();
+    *total = tot;
+    return wpre + x - v;
+}
+
+// One CTA per digit: exclusive scan of hist[d][0..n_tiles) in place, digit total out.
+__global__ void __launch_bounds__(kRsThreads) k_rs_scan_digit(uint32_t* __restrict__ hist, uint32_t n_tiles,
+                                                              uint32_t* __restrict__ totals)
+{
+    __shared__ uint32_t sh[8];
+    uint32_t* row = hist + (size_t)blockIdx.x * n_tiles;
+    uint32_t carry = 0;
+    for (uint32_t s = 0; s < n_tiles; s += kRsThreads) {
+        const uint32_t i = s + threadIdx.x;
+        const uint32_t v = (i < n_tiles) ? row[i] : 0u;
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_scan(v, &tot, sh);
+        if (i < n_tiles) row[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) totals[blockIdx.x] = carry;
+}
+
+__global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                                           uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                           uint32_t n, int shift, const uint32_t* __restrict__ hist,
+                                                           uint32_t n_tiles, const uint32_t* __restrict__ totals)
+{
+    __shared__ uint32_t warp_cnt[kRsThreads / 32][256];
+    __shared__ uint32_t base[256];
+    __shared__ uint32_t sh[8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < (kRsThreads / 32) * 256; i += kRsThreads) (&warp_cnt[0][0])[i] = 0;
+    {
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_scan(totals[threadIdx.x], &tot, sh);
+        base[threadIdx.x] = ex + hist[(size_t)threadIdx.x * n_tiles + blockIdx.x];
+    }
+    __syncthreads();
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t key[kRsRounds], val[kRsRounds], rank[kRsRounds];
+    const uint32_t tile0 = blockIdx.x * kRsTile + w * (kRsRounds * 32);
+#pragma unroll
+    for (int r = 0; r < kRsRounds; ++r) {
+        const uint32_t i = tile0 + r * 32 + lane;
+        const bool valid = i < n;
+        key[r] = valid ? kin[i] : 0u;
+        val[r] = valid ? vin[i] : 0u;
+        const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+        rank[r] = 0;
+        if (valid) {
+            const uint32_t d = (key[r] >> shift) & 255u;
+            const uint32_t peers = __match_any_sync(vmask, d);
+            const uint32_t b = warp_cnt[w][d];
+            rank[r] = b + __popc(peers & lt);
+            __syncwarp(vmask);
+            if (lane == __ffs(peers) - 1) warp_cnt[w][d] = b + __popc(peers);
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    {
+        const int d = threadIdx.x;
+        uint32_t s = 0;
+#pragma unroll
+        for (int i = 0; i < kRsThreads / 32; ++i) {
+            const uint32_t t = warp_cnt[i][d];
+            warp_cnt[i][d] = s;
+            s += t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kRsRounds; ++r) {
+        const uint32_t i = tile0 + r * 32 + lane;
+        if (i < n) {
+            const uint32_t d = (key[r] >> shift) & 255u;
+            const uint32_t dst = base[d] + warp_cnt[w][d] + rank[r];
+            kout[dst] = key[r];
+            vout[dst] = val[r];
+        }
+    }
+}
+
+// Morton-ordered face records: (v0, v1, v2, original face index).
+__global__ void __launch_bounds__(256) k_gather_faces(const uint32_t* __restrict__ tri, const uint32_t* __restrict__ perm,
+                                                      uint32_t nT, uint4* __restrict__ out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nT) return;
+    const uint32_t o = perm[i];
+    out[i] = make_uint4(__ldg(tri + 3 * (size_t)o), __ldg(tri + 3 * (size_t)o + 1), __ldg(tri + 3 * (size_t)o + 2), o);
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers
+// ---------------------------------------------------------------------------
+size_t radix_sort_scratch_bytes(uint32_t n)
+{
+    const uint32_t n_tiles = (n + kRsTile - 1) / kRsTile;
+    return (size_t)256 * n_tiles * sizeof(uint32_t) + 256 * sizeof(uint32_t) + 2 * (size_t)n * sizeof(uint32_t);
+}
+
+cudaError_t launch_mesh_bounds(const float* xyz, uint32_t nV, uint32_t* bound_keys, int num_sms, cudaStream_t s)
+{
+    note_launches(1);
+    k_bounds_init<<<1, 32, 0, s>>>(bound_keys);
+    uint32_t blocks = (nV + 255) / 256;
+    const uint32_t cap = (uint32_t)num_sms * 8u;
+    if (blocks > cap) blocks = cap;
+    if (blocks == 0) blocks = 1;
+    note_launches(1);
+    k_mesh_bounds<<<blocks, 256, 0, s>>>(xyz, nV, bound_keys);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_leaf_morton(const uint32_t* tri, const float* xyz, uint32_t nT, const uint32_t* bound_keys,
+                               uint32_t* codes, uint32_t* idx, cudaStream_t s)
+{
+    note_launches(1);
+    k_leaf_morton<<<(nT + 255) / 256, 256, 0, s>>>(tri, xyz, nT, bound_keys, codes, idx);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_radix_sort(uint32_t* keys, uint32_t* vals, uint32_t n, int key_bits, void* scratch,
+                              cudaStream_t s)
+{
+    if (n <= 1) return cudaSuccess;
+    const uint32_t n_tiles = (n + kRsTile - 1) / kRsTile;
+    uint32_t* hist = (uint32_t*)scratch;
+    uint32_t* totals = hist + (size_t)256 * n_tiles;
+    uint32_t* k2 = totals + 256;
+    uint32_t* v2 = k2 + n;
+    uint32_t *ki = keys, *vi = vals, *ko = k2, *vo = v2;
+    int passes = 0;
+    for (int shift = 0; shift < key_bits; shift += 8) {
+        note_launches(1);
+        k_rs_hist<<<n_tiles, kRsThreads, 0, s>>>(ki, n, shift, hist, n_tiles);
+        note_launches(1);
+        k_rs_scan_digit<<<256, kRsThreads, 0, s>>>(hist, n_tiles, totals);
+        note_launches(1);
+        k_rs_scatter<<<n_tiles, kRsThreads, 0, s>>>(ki, vi, ko, vo, n, shift, hist, n_tiles, totals);
+        uint32_t* t = ki; ki = ko; ko = t;
+        t = vi; vi = vo; vo = t;
+        ++passes;
+    }
+    if (passes & 1) {
+        cudaMemcpyAsync(keys, ki, (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(vals, vi, (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_faces(const uint32_t* tri, const uint32_t* perm, uint32_t nT, uint4* out, cudaStream_t s)
+{
+    note_launches(1);
+    k_gather_faces<<<(nT + 255) / 256, 256, 0, s>>>(tri, perm, nT, out);
+    return cudaGetLastError();
+}
+
+} // namespace oibvh

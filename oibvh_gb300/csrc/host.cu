@@ -1,0 +1,862 @@
+// Host orchestration and the C ABI (include/oibvh_gb300.h).
+//
+// oibvh_tree_s mirrors OibvhTree (include/cuda/oibvhTree.cuh:50-93,
+// src/cuda/oibvhTree.cu) and oibvh_scene_s mirrors Scene
+// (include/cuda/scene.cuh:44-61, src/cuda/scene.cu). Differences by design:
+//   * the tree stays resident in device memory; nothing is copied back to
+//     the host after build or refit unless asked (oibvh_tree_get_aabbs);
+//   * the BVTT loop is enqueued whole: each level reads its front size on
+//     the device, so detect reads counters back once per pass, not once per
+//     level (the reference reads after every level, src/cuda/scene.cu:302);
+//   * queues are sized by demand: an overflow is detected, the queue grows,
+//     and the pass reruns (the reference writes past fixed 10M-entry buffers
+//     unchecked, src/cuda/scene.cu:15-21, src/cuda/collide.cu:160-161);
+//   * every CUDA status is checked and returned.
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/oibvh_gb300.h"
+#include "oibvh_common.cuh"
+#include "oibvh_launch.h"
+
+using namespace oibvh;
+
+namespace oibvh {
+static std::atomic<uint64_t> g_launches{0};
+void note_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+}  // namespace oibvh
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    const int code = (e == cudaErrorMemoryAllocation) ? OIBVH_ERR_OOM : OIBVH_ERR_CUDA;
+    g_last_error = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return code;
+}
+
+#define CUDA_TRY(expr)                                   \
+    do {                                                 \
+        cudaError_t _e = (expr);                         \
+        if (_e != cudaSuccess) return cuda_fail(_e, #expr); \
+    } while (0)
+
+#define OK_TRY(expr)              \
+    do {                          \
+        int _s = (expr);          \
+        if (_s != OIBVH_OK) return _s; \
+    } while (0)
+
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = true;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
+    }
+    ~DeviceGuard()
+    {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+int sm_count(int dev)
+{
+    static int cache[64] = {};
+    if (dev >= 0 && dev < 64 && cache[dev]) return cache[dev];
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+    if (dev >= 0 && dev < 64) cache[dev] = n;
+    return n;
+}
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    // grow to at least `want` elements; contents are not kept
+    int ensure(size_t want, const char* what)
+    {
+        if (want <= n && p) return OIBVH_OK;
+        release();
+        if (want == 0) want = 1;
+        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            cudaGetLastError();
+            return cuda_fail(e, what);
+        }
+        n = want;
+        return OIBVH_OK;
+    }
+    // grow keeping the first `keep` elements (stream-ordered copy)
+    int grow_keep(size_t want, size_t keep, cudaStream_t s, const char* what)
+    {
+        if (want <= n && p) return OIBVH_OK;
+        T* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, want * sizeof(T));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return cuda_fail(e, what);
+        }
+        if (p && keep) {
+            e = cudaMemcpyAsync(q, p, std::min(keep, n) * sizeof(T), cudaMemcpyDeviceToDevice, s);
+            if (e != cudaSuccess) {
+                cudaFree(q);
+                return cuda_fail(e, what);
+            }
+            e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) {
+                cudaFree(q);
+                return cuda_fail(e, what);
+            }
+        }
+        release();
+        p = q;
+        n = want;
+        return OIBVH_OK;
+    }
+};
+
+template <class T>
+struct PinnedBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf&) = delete;
+    PinnedBuf& operator=(const PinnedBuf&) = delete;
+    ~PinnedBuf()
+    {
+        if (p) cudaFreeHost(p);
+    }
+    int ensure(size_t want, const char* what)
+    {
+        if (want <= n && p) return OIBVH_OK;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        if (want == 0) want = 1;
+        cudaError_t e = cudaMallocHost(&p, want * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            cudaGetLastError();
+            return cuda_fail(e, what);
+        }
+        n = want;
+        return OIBVH_OK;
+    }
+};
+
+}  // namespace
+
+// ============================================================================
+// Tree
+// ============================================================================
+struct oibvh_tree_s {
+    int device = 0;
+    uint32_t nV = 0, nT = 0;
+    TreeShape shape{};
+    DevBuf<float> xyz;          // owned positions (3 * nV)
+    const float* cur_xyz = nullptr;  // positions of the last build/refit
+    DevBuf<uint32_t> tri;       // faces as given (3 * nT)
+    DevBuf<uint4> face;         // Morton-ordered faces (v0, v1, v2, original index)
+    DevBuf<float4> box;         // 2 * size
+    DevBuf<uint32_t> counters;  // refit climbing counters
+    bool built = false;
+
+    RefitJob job() const
+    {
+        RefitJob j{};
+        j.box = box.p;
+        j.face = face.p;
+        j.xyz = cur_xyz;
+        j.shape = shape;
+        j.block_begin = 0;
+        j.n_blocks = refit_blocks_for(nT);
+        j.counters = counters.p;
+        return j;
+    }
+};
+
+static int tree_alloc(oibvh_tree_t t)
+{
+    OK_TRY(t->xyz.ensure(3 * (size_t)t->nV, "cudaMalloc(positions)"));
+    OK_TRY(t->tri.ensure(3 * (size_t)t->nT, "cudaMalloc(faces)"));
+    OK_TRY(t->face.ensure(t->nT, "cudaMalloc(sorted faces)"));
+    OK_TRY(t->box.ensure(2 * (size_t)t->shape.size, "cudaMalloc(tree)"));
+    OK_TRY(t->counters.ensure(refit_counters_per_tree(), "cudaMalloc(counters)"));
+    return OIBVH_OK;
+}
+
+static int tree_create_impl(const float* xyz, uint32_t nV, const uint32_t* tri, uint32_t nT, int device,
+                            oibvh_tree_t* out)
+{
+    if (!out) return fail(OIBVH_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (!xyz || !tri) return fail(OIBVH_ERR_ARG, "xyz or tri is NULL");
+    if (nT == 0) return fail(OIBVH_ERR_ARG, "a mesh needs at least one triangle");
+    if (nT > (1u << kMaxLeafLevel)) return fail(OIBVH_ERR_ARG, "more than 2^23 triangles");
+    if (nV == 0) return fail(OIBVH_ERR_ARG, "no vertices");
+    for (size_t i = 0; i < 3 * (size_t)nT; ++i)
+        if (tri[i] >= nV)
+            return fail(OIBVH_ERR_ARG, "face " + std::to_string(i / 3) + " refers to vertex " +
+                                           std::to_string(tri[i]) + " >= " + std::to_string(nV));
+    int ndev = 0;
+    CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(OIBVH_ERR_ARG, "no such device");
+    DeviceGuard g(device);
+    if (!g.ok) return fail(OIBVH_ERR_CUDA, "cudaSetDevice failed");
+    oibvh_tree_t t = new oibvh_tree_s();
+    t->device = device;
+    t->nV = nV;
+    t->nT = nT;
+    t->shape = TreeShape::of(nT);
+    int st = tree_alloc(t);
+    if (st == OIBVH_OK) {
+        cudaError_t e = cudaMemcpy(t->xyz.p, xyz, 3 * (size_t)nV * sizeof(float), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(t->tri.p, tri, 3 * (size_t)nT * sizeof(uint32_t), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpy(mesh)");
+    }
+    if (st != OIBVH_OK) {
+        delete t;
+        return st;
+    }
+    t->cur_xyz = t->xyz.p;
+    *out = t;
+    return OIBVH_OK;
+}
+
+static int tree_build_impl(oibvh_tree_t t, cudaStream_t s)
+{
+    if (!t) return fail(OIBVH_ERR_ARG, "tree is NULL");
+    DeviceGuard g(t->device);
+    const uint32_t nT = t->nT;
+    // scratch: bounds keys, codes, indices, sort buffers
+    DevBuf<uint8_t> scratch;
+    const size_t sort_bytes = radix_sort_scratch_bytes(nT);
+    const size_t codes_off = 256, idx_off = codes_off + ((size_t)nT * 4 + 255) / 256 * 256;
+    const size_t sort_off = idx_off + ((size_t)nT * 4 + 255) / 256 * 256;
+    OK_TRY(scratch.ensure(sort_off + sort_bytes, "cudaMalloc(build scratch)"));
+    uint32_t* keys6 = (uint32_t*)scratch.p;
+    uint32_t* codes = (uint32_t*)(scratch.p + codes_off);
+    uint32_t* idx = (uint32_t*)(scratch.p + idx_off);
+    t->cur_xyz = t->xyz.p;
+    CUDA_TRY(launch_mesh_bounds(t->xyz.p, t->nV, keys6, sm_count(t->device), s));
+    CUDA_TRY(launch_leaf_morton(t->tri.p, t->xyz.p, nT, keys6, codes, idx, s));
+    CUDA_TRY(launch_radix_sort(codes, idx, nT, 30, scratch.p + sort_off, s));
+    CUDA_TRY(launch_gather_faces(t->tri.p, idx, nT, t->face.p, s));
+    CUDA_TRY(launch_refit_one(t->job(), s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    t->built = true;
+    return OIBVH_OK;
+}
+
+// ============================================================================
+// Scene
+// ============================================================================
+struct oibvh_scene_s {
+    int device = 0;
+    std::vector<oibvh_tree_t> trees;
+    bool all_pairs = true;
+    std::vector<uint32_t> pairs;  // flattened (a, b)
+
+    DevBuf<TreeView> views;
+    DevBuf<PairView> pairv;
+    DevBuf<uint64_t> front0, front1, cand;
+    DevBuf<uint4> hits;
+    DevBuf<uint32_t> counts;
+    PinnedBuf<TreeView> h_views;
+    PinnedBuf<PairView> h_pairs;
+    PinnedBuf<uint32_t> h_counts;
+
+    uint32_t front_cap = 1u << 20;
+    uint32_t cand_cap = 1u << 20;
+    uint32_t hit_cap = 1u << 18;
+
+    uint64_t hit_count = 0;
+    uint64_t cand_count = 0;
+    bool cands_valid = false;    // candidates of a single pass are on the device
+    std::vector<PairView> last_pairs;
+    oibvh_detect_stats stats{};
+};
+
+namespace {
+
+struct PassPlan {
+    std::vector<PairView> pv;
+    uint64_t front0 = 0;
+    uint32_t iters = 1;
+};
+
+void list_pairs(const oibvh_scene_s* s, std::vector<uint32_t>& out)
+{
+    out.clear();
+    if (s->all_pairs) {
+        const uint32_t n = (uint32_t)s->trees.size();
+        for (uint32_t i = 0; i < n; ++i)
+            for (uint32_t j = i + 1; j < n; ++j) {
+                out.push_back(i);
+                out.push_back(j);
+            }
+    } else {
+        out = s->pairs;
+    }
+}
+
+int plan_pass(const oibvh_scene_s* s, const uint32_t* pr, uint32_t n, uint32_t entry, uint32_t expand, PassPlan& plan)
+{
+    plan.pv.resize(n);
+    plan.front0 = 0;
+    plan.iters = 1;
+    for (uint32_t p = 0; p < n; ++p) {
+        const TreeShape& A = s->trees[pr[2 * p]]->shape;
+        const TreeShape& B = s->trees[pr[2 * p + 1]]->shape;
+        PairView v{};
+        v.a = pr[2 * p];
+        v.b = pr[2 * p + 1];
+        v.entry_a = std::min(entry, A.L);
+        v.entry_b = std::min(entry, B.L);
+        v.front_cnt_a = A.level_count(v.entry_a);
+        v.front_cnt_b = B.level_count(v.entry_b);
+        if (plan.front0 > 0x7fffffffull) return fail(OIBVH_ERR_ARG, "initial BVTT front exceeds 2^31 nodes");
+        v.front_off = (uint32_t)plan.front0;
+        plan.front0 += (uint64_t)v.front_cnt_a * v.front_cnt_b;
+        const uint32_t depth = std::max(A.L - v.entry_a, B.L - v.entry_b);
+        const uint32_t it = (depth + expand - 1) / expand + 1;
+        plan.iters = std::max(plan.iters, it);
+        plan.pv[p] = v;
+    }
+    if (plan.front0 > 0x7fffffffull) return fail(OIBVH_ERR_ARG, "initial BVTT front exceeds 2^31 nodes");
+    return OIBVH_OK;
+}
+
+uint32_t grow_cap(uint64_t need, uint32_t cur)
+{
+    uint64_t c = std::max<uint64_t>(need + need / 4 + 1024, (uint64_t)cur * 2);
+    if (c > 0x7fffffffull) c = 0x7fffffffull;
+    return (uint32_t)c;
+}
+
+int upload_views(oibvh_scene_s* s, cudaStream_t st)
+{
+    const size_t n = s->trees.size();
+    OK_TRY(s->h_views.ensure(n, "cudaMallocHost(views)"));
+    OK_TRY(s->views.ensure(n, "cudaMalloc(views)"));
+    CUDA_TRY(cudaStreamSynchronize(st));  // the pinned staging buffer may still feed an earlier copy
+    for (size_t i = 0; i < n; ++i) {
+        const oibvh_tree_t t = s->trees[i];
+        TreeView v{};
+        v.box = t->box.p;
+        v.face = t->face.p;
+        v.xyz = t->cur_xyz;
+        v.shape = t->shape;
+        v.nV = t->nV;
+        s->h_views.p[i] = v;
+    }
+    CUDA_TRY(cudaMemcpyAsync(s->views.p, s->h_views.p, n * sizeof(TreeView), cudaMemcpyHostToDevice, st));
+    return OIBVH_OK;
+}
+
+// Broad phase (+ narrow phase when `narrow`) over every pair, pass by pass.
+int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expand, bool narrow, cudaStream_t st)
+{
+    if (device_type < 0)
+        return fail(OIBVH_ERR_UNSUPPORTED,
+                    "device type CPU: the reference's detectCollisionOnCPU is empty; this library has no CPU path");
+    if (device_type != s->device) return fail(OIBVH_ERR_ARG, "device type does not match the scene's device");
+    if (expand < 1 || expand > 16) return fail(OIBVH_ERR_ARG, "expand_levels must be in 1..16");
+    for (auto t : s->trees)
+        if (!t->built) return fail(OIBVH_ERR_STATE, "every tree must be built before detect");
+    DeviceGuard g(s->device);
+    s->stats = oibvh_detect_stats{};
+    s->hit_count = 0;
+    s->cand_count = 0;
+    s->cands_valid = false;
+    std::vector<uint32_t> pr;
+    list_pairs(s, pr);
+    const uint32_t n_pairs = (uint32_t)(pr.size() / 2);
+    for (uint32_t i = 0; i < n_pairs; ++i)
+        if (pr[2 * i] >= s->trees.size() || pr[2 * i + 1] >= s->trees.size() || pr[2 * i] == pr[2 * i + 1])
+            return fail(OIBVH_ERR_ARG, "pair list refers to a missing tree or pairs a tree with itself");
+    if (n_pairs == 0) return OIBVH_OK;
+    OK_TRY(upload_views(s, st));
+    OK_TRY(s->hits.ensure(s->hit_cap, "cudaMalloc(hits)"));
+
+    const int grid = sm_count(s->device) * 8;
+    for (uint32_t p0 = 0; p0 < n_pairs; p0 += kMaxPairsPerPass) {
+        const uint32_t np = std::min(kMaxPairsPerPass, n_pairs - p0);
+        PassPlan plan;
+        OK_TRY(plan_pass(s, pr.data() + 2 * (size_t)p0, np, entry, expand, plan));
+        const uint32_t n_counts = kCountFront0 + plan.iters + 1;
+        OK_TRY(s->counts.ensure(n_counts, "cudaMalloc(counts)"));
+        OK_TRY(s->h_counts.ensure(n_counts, "cudaMallocHost(counts)"));
+        OK_TRY(s->h_pairs.ensure(np, "cudaMallocHost(pairs)"));
+        OK_TRY(s->pairv.ensure(np, "cudaMalloc(pairs)"));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        std::memcpy(s->h_pairs.p, plan.pv.data(), np * sizeof(PairView));
+        CUDA_TRY(cudaMemcpyAsync(s->pairv.p, s->h_pairs.p, np * sizeof(PairView), cudaMemcpyHostToDevice, st));
+        const uint64_t hits_before = s->hit_count;
+        for (int attempt = 0;; ++attempt) {
+            if (attempt > 12) return fail(OIBVH_ERR_OVERFLOW, "BVTT queues kept overflowing after regrowing");
+            if (plan.front0 > s->front_cap) s->front_cap = grow_cap(plan.front0, s->front_cap);
+            OK_TRY(s->front0.ensure(s->front_cap, "cudaMalloc(front)"));
+            OK_TRY(s->front1.ensure(s->front_cap, "cudaMalloc(front)"));
+            OK_TRY(s->cand.ensure(s->cand_cap, "cudaMalloc(candidates)"));
+            CUDA_TRY(cudaMemsetAsync(s->counts.p, 0, n_counts * sizeof(uint32_t), st));
+            s->h_counts.p[0] = (uint32_t)hits_before;
+            CUDA_TRY(cudaMemcpyAsync(s->counts.p, s->h_counts.p, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+            DetectArgs a{};
+            a.trees = s->views.p;
+            a.pairs = s->pairv.p;
+            a.n_pairs = np;
+            a.expand_levels = expand;
+            a.front[0] = s->front0.p;
+            a.front[1] = s->front1.p;
+            a.front_cap = s->front_cap;
+            a.cand = s->cand.p;
+            a.cand_cap = s->cand_cap;
+            a.hits = s->hits.p;
+            a.hit_cap = s->hit_cap;
+            a.counts = s->counts.p;
+            a.iters = plan.iters;
+            a.grid = grid;
+            CUDA_TRY(launch_init_front(a, (uint32_t)plan.front0, st));
+            for (uint32_t it = 0; it < plan.iters; ++it) CUDA_TRY(launch_bvtt_step(a, it, st));
+            if (narrow) CUDA_TRY(launch_narrow(a, st));
+            CUDA_TRY(cudaMemcpyAsync(s->h_counts.p, s->counts.p, n_counts * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                     st));
+            CUDA_TRY(cudaStreamSynchronize(st));
+            const uint32_t* c = s->h_counts.p;
+            const uint32_t flags = c[kCountFlags];
+            if (c[kCountFront0 + plan.iters] != 0)
+                return fail(OIBVH_ERR_STATE, "internal: BVTT front not empty after the last level");
+            if (flags) {
+                s->stats.retries++;
+                if (flags & kFlagFrontOverflow) {
+                    uint64_t peak = 0;
+                    for (uint32_t k = 0; k <= plan.iters; ++k) peak = std::max<uint64_t>(peak, c[kCountFront0 + k]);
+                    s->front_cap = grow_cap(peak, s->front_cap);
+                }
+                if (flags & kFlagCandOverflow) s->cand_cap = grow_cap(c[kCountCands], s->cand_cap);
+                if (flags & kFlagHitOverflow) {
+                    const uint32_t want = grow_cap(c[kCountHits], s->hit_cap);
+                    OK_TRY(s->hits.grow_keep(want, hits_before, st, "cudaMalloc(hits)"));
+                    s->hit_cap = want;
+                }
+                continue;
+            }
+            uint64_t nodes = 0, peak = 0;
+            for (uint32_t k = 0; k < plan.iters; ++k) {
+                nodes += c[kCountFront0 + k];
+                peak = std::max<uint64_t>(peak, c[kCountFront0 + k]);
+            }
+            s->stats.nodes_tested += nodes;
+            s->stats.front_peak = std::max(s->stats.front_peak, peak);
+            s->stats.steps = plan.iters;
+            s->cand_count += c[kCountCands];
+            if (narrow) s->hit_count = c[kCountHits];
+            break;
+        }
+        s->stats.passes++;
+        if (!narrow) {
+            if (n_pairs > kMaxPairsPerPass)
+                return fail(OIBVH_ERR_UNSUPPORTED, "the split broad phase handles at most 65536 pairs");
+            s->last_pairs = plan.pv;
+            s->cands_valid = true;
+        }
+    }
+    s->stats.candidates = s->cand_count;
+    s->stats.hits = s->hit_count;
+    return OIBVH_OK;
+}
+
+int narrow_impl(oibvh_scene_s* s, cudaStream_t st)
+{
+    if (!s->cands_valid) return fail(OIBVH_ERR_STATE, "narrow phase needs a broad phase first");
+    DeviceGuard g(s->device);
+    const uint32_t np = (uint32_t)s->last_pairs.size();
+    for (int attempt = 0;; ++attempt) {
+        if (attempt > 12) return fail(OIBVH_ERR_OVERFLOW, "hit queue kept overflowing");
+        // counts[2] still holds the candidate count of the broad phase
+        uint32_t z[2] = {0, 0};
+        std::memcpy(s->h_counts.p, z, sizeof(z));
+        CUDA_TRY(cudaMemcpyAsync(s->counts.p, s->h_counts.p, 2 * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+        DetectArgs a{};
+        a.trees = s->views.p;
+        a.pairs = s->pairv.p;
+        a.n_pairs = np;
+        a.cand = s->cand.p;
+        a.cand_cap = s->cand_cap;
+        a.hits = s->hits.p;
+        a.hit_cap = s->hit_cap;
+        a.counts = s->counts.p;
+        a.grid = sm_count(s->device) * 8;
+        CUDA_TRY(launch_narrow(a, st));
+        CUDA_TRY(cudaMemcpyAsync(s->h_counts.p, s->counts.p, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        if (s->h_counts.p[kCountFlags] & kFlagHitOverflow) {
+            const uint32_t want = grow_cap(s->h_counts.p[kCountHits], s->hit_cap);
+            OK_TRY(s->hits.ensure(want, "cudaMalloc(hits)"));
+            s->hit_cap = want;
+            continue;
+        }
+        s->hit_count = s->h_counts.p[kCountHits];
+        s->stats.hits = s->hit_count;
+        return OIBVH_OK;
+    }
+}
+
+}  // namespace
+
+// ============================================================================
+// C ABI
+// ============================================================================
+#define API extern "C" __attribute__((visibility("default")))
+
+#define GUARD_BEGIN try {
+#define GUARD_END                                                   \
+    }                                                               \
+    catch (const std::bad_alloc&)                                   \
+    {                                                               \
+        return fail(OIBVH_ERR_OOM, "host allocation failed");       \
+    }                                                               \
+    catch (...)                                                     \
+    {                                                               \
+        return fail(OIBVH_ERR_CUDA, "unexpected C++ exception");    \
+    }
+
+API const char* oibvh_status_string(int status)
+{
+    switch (status) {
+    case OIBVH_OK: return "ok";
+    case OIBVH_ERR_ARG: return "invalid argument";
+    case OIBVH_ERR_OOM: return "out of memory";
+    case OIBVH_ERR_CUDA: return "CUDA error";
+    case OIBVH_ERR_OVERFLOW: return "queue overflow";
+    case OIBVH_ERR_STATE: return "invalid state";
+    case OIBVH_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+    }
+}
+
+API const char* oibvh_last_error(void) { return g_last_error.c_str(); }
+
+API int oibvh_version(void) { return 100; }
+
+API uint64_t oibvh_get_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+API int oibvh_tree_create(const float* xyz, uint32_t n_vertices, const uint32_t* tri, uint32_t n_triangles, int device,
+                          oibvh_tree_t* out)
+{
+    GUARD_BEGIN
+    return tree_create_impl(xyz, n_vertices, tri, n_triangles, device, out);
+    GUARD_END
+}
+
+API int oibvh_tree_create_copy(oibvh_tree_t other, const float* xyz, uint32_t n_vertices, oibvh_tree_t* out)
+{
+    GUARD_BEGIN
+    if (!out) return fail(OIBVH_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (!other || !xyz) return fail(OIBVH_ERR_ARG, "other or xyz is NULL");
+    if (!other->built) return fail(OIBVH_ERR_STATE, "the source tree is not built");
+    if (n_vertices != other->nV) return fail(OIBVH_ERR_ARG, "vertex count differs from the source mesh");
+    DeviceGuard g(other->device);
+    oibvh_tree_t t = new oibvh_tree_s();
+    t->device = other->device;
+    t->nV = other->nV;
+    t->nT = other->nT;
+    t->shape = other->shape;
+    int st = tree_alloc(t);
+    if (st == OIBVH_OK) {
+        cudaError_t e = cudaMemcpy(t->xyz.p, xyz, 3 * (size_t)t->nV * sizeof(float), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(t->tri.p, other->tri.p, 3 * (size_t)t->nT * sizeof(uint32_t), cudaMemcpyDeviceToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(t->face.p, other->face.p, (size_t)t->nT * sizeof(uint4), cudaMemcpyDeviceToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(t->box.p, other->box.p, 2 * (size_t)t->shape.size * sizeof(float4), cudaMemcpyDeviceToDevice);
+        if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpy(copy tree)");
+    }
+    if (st != OIBVH_OK) {
+        delete t;
+        return st;
+    }
+    t->cur_xyz = t->xyz.p;
+    t->built = true;  // the copied boxes describe `other`'s positions until refit
+    *out = t;
+    return OIBVH_OK;
+    GUARD_END
+}
+
+API int oibvh_tree_build(oibvh_tree_t t, void* stream)
+{
+    GUARD_BEGIN
+    return tree_build_impl(t, (cudaStream_t)stream);
+    GUARD_END
+}
+
+API int oibvh_tree_refit(oibvh_tree_t t, const float* xyz, void* stream)
+{
+    GUARD_BEGIN
+    if (!t) return fail(OIBVH_ERR_ARG, "tree is NULL");
+    if (!t->built) return fail(OIBVH_ERR_STATE, "refit before build");
+    DeviceGuard g(t->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (xyz)
+        CUDA_TRY(cudaMemcpyAsync(t->xyz.p, xyz, 3 * (size_t)t->nV * sizeof(float), cudaMemcpyHostToDevice, s));
+    t->cur_xyz = t->xyz.p;
+    CUDA_TRY(launch_refit_one(t->job(), s));
+    return OIBVH_OK;
+    GUARD_END
+}
+
+API int oibvh_tree_refit_device(oibvh_tree_t t, const float* d_xyz, void* stream)
+{
+    GUARD_BEGIN
+    if (!t || !d_xyz) return fail(OIBVH_ERR_ARG, "tree or d_xyz is NULL");
+    if (!t->built) return fail(OIBVH_ERR_STATE, "refit before build");
+    DeviceGuard g(t->device);
+    cudaPointerAttributes attr{};
+    CUDA_TRY(cudaPointerGetAttributes(&attr, d_xyz));
+    if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
+        return fail(OIBVH_ERR_ARG, "d_xyz is not device memory");
+    t->cur_xyz = d_xyz;
+    CUDA_TRY(launch_refit_one(t->job(), (cudaStream_t)stream));
+    return OIBVH_OK;
+    GUARD_END
+}
+
+API uint32_t oibvh_tree_get_depth(oibvh_tree_t t) { return t ? ilog2(t->shape.size) : 0; }
+API uint32_t oibvh_tree_get_prim_count(oibvh_tree_t t) { return t ? t->nT : 0; }
+API uint32_t oibvh_tree_get_size(oibvh_tree_t t) { return t ? t->shape.size : 0; }
+
+API int oibvh_tree_get_aabbs(oibvh_tree_t t, float* out6, uint64_t cap_nodes)
+{
+    GUARD_BEGIN
+    if (!t || !out6) return fail(OIBVH_ERR_ARG, "tree or out6 is NULL");
+    if (!t->built) return fail(OIBVH_ERR_STATE, "tree not built");
+    DeviceGuard g(t->device);
+    const size_t n = std::min<uint64_t>(cap_nodes, t->shape.size);
+    std::vector<float4> tmp(2 * n);
+    CUDA_TRY(cudaDeviceSynchronize());
+    CUDA_TRY(cudaMemcpy(tmp.data(), t->box.p, 2 * n * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; ++i) {
+        out6[6 * i + 0] = tmp[2 * i].x;
+        out6[6 * i + 1] = tmp[2 * i].y;
+        out6[6 * i + 2] = tmp[2 * i].z;
+        out6[6 * i + 3] = tmp[2 * i + 1].x;
+        out6[6 * i + 4] = tmp[2 * i + 1].y;
+        out6[6 * i + 5] = tmp[2 * i + 1].z;
+    }
+    return OIBVH_OK;
+    GUARD_END
+}
+
+API int oibvh_tree_get_sorted_faces(oibvh_tree_t t, uint32_t* out3, uint32_t* perm, uint64_t cap)
+{
+    GUARD_BEGIN
+    if (!t) return fail(OIBVH_ERR_ARG, "tree is NULL");
+    if (!t->built) return fail(OIBVH_ERR_STATE, "tree not built");
+    DeviceGuard g(t->device);
+    const size_t n = std::min<uint64_t>(cap, t->nT);
+    std::vector<uint4> tmp(n);
+    CUDA_TRY(cudaDeviceSynchronize());
+    CUDA_TRY(cudaMemcpy(tmp.data(), t->face.p, n * sizeof(uint4), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; ++i) {
+        if (out3) {
+            out3[3 * i] = tmp[i].x;
+            out3[3 * i + 1] = tmp[i].y;
+            out3[3 * i + 2] = tmp[i].z;
+        }
+        if (perm) perm[i] = tmp[i].w;
+    }
+    return OIBVH_OK;
+    GUARD_END
+}
+
+API int oibvh_tree_destroy(oibvh_tree_t t)
+{
+    if (!t) return OIBVH_OK;
+    {
+        DeviceGuard g(t->device);
+        delete t;
+    }
+    return OIBVH_OK;
+}
+
+API int oibvh_scene_create(int device, oibvh_scene_t* out)
+{
+    GUARD_BEGIN
+    if (!out) return fail(OIBVH_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(OIBVH_ERR_ARG, "no such device");
+    oibvh_scene_t s = new oibvh_scene_s();
+    s->device = device;
+    *out = s;
+    return OIBVH_OK;
+    GUARD_END
+}
+
+API int oibvh_scene_add_tree(oibvh_scene_t s, oibvh_tree_t t, uint32_t* id)
+{
+    GUARD_BEGIN
+    if (!s || !t) return fail(OIBVH_ERR_ARG, "scene or tree is NULL");
+    if (t->device != s->device) return fail(OIBVH_ERR_ARG, "tree lives on another device");
+    if (!t->built) return fail(OIBVH_ERR_STATE, "addOibvhTree needs a built tree (src/cuda/scene.cu:97)");
+    s->trees.push_back(t);
+    if (id) *id = (uint32_t)(s->trees.size() - 1);
+    return OIBVH_OK;
+    GUARD_END
+}
+
+API int oibvh_scene_set_pairs(oibvh_scene_t s, const uint32_t* pairs, uint32_t n_pairs)
+{
+    GUARD_BEGIN
+    if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
+    if (!pairs) {
+        s->all_pairs = true;
+        s->pairs.clear();
+        return OIBVH_OK;
+    }
+    for (uint32_t i = 0; i < n_pairs; ++i)
+        if (pairs[2 * i] >= s->trees.size() || pairs[2 * i + 1] >= s->trees.size() || pairs[2 * i] == pairs[2 * i + 1])
+            return fail(OIBVH_ERR_ARG, "pair " + std::to_string(i) + " is not two distinct trees of this scene");
+    s->all_pairs = false;
+    s->pairs.assign(pairs, pairs + 2 * (size_t)n_pairs);
+    return OIBVH_OK;
+    GUARD_END
+}
+
+API int oibvh_scene_detect(oibvh_scene_t s, int device_type, uint32_t entry_level, uint32_t expand_levels,
+                           void* stream)
+{
+    GUARD_BEGIN
+    if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
+    return detect_impl(s, device_type, entry_level, expand_levels, true, (cudaStream_t)stream);
+    GUARD_END
+}
+
+API int oibvh_scene_broad(oibvh_scene_t s, int device_type, uint32_t entry_level, uint32_t expand_levels, void* stream)
+{
+    GUARD_BEGIN
+    if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
+    return detect_impl(s, device_type, entry_level, expand_levels, false, (cudaStream_t)stream);
+    GUARD_END
+}
+
+API int oibvh_scene_narrow(oibvh_scene_t s, void* stream)
+{
+    GUARD_BEGIN
+    if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
+    return narrow_impl(s, (cudaStream_t)stream);
+    GUARD_END
+}
+
+API uint32_t oibvh_scene_get_int_tri_pair_count(oibvh_scene_t s) { return s ? (uint32_t)s->hit_count : 0; }
+API uint64_t oibvh_scene_get_candidate_count(oibvh_scene_t s) { return s ? s->cand_count : 0; }
+
+API int oibvh_scene_get_int_tri_pairs(oibvh_scene_t s, uint32_t* out4, uint64_t cap, uint64_t* n)
+{
+    GUARD_BEGIN
+    if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
+    if (n) *n = s->hit_count;
+    const uint64_t k = std::min(cap, s->hit_count);
+    if (k == 0) return OIBVH_OK;
+    if (!out4) return fail(OIBVH_ERR_ARG, "out4 is NULL");
+    DeviceGuard g(s->device);
+    CUDA_TRY(cudaMemcpy(out4, s->hits.p, k * sizeof(uint4), cudaMemcpyDeviceToHost));
+    return OIBVH_OK;
+    GUARD_END
+}
+
+API int oibvh_scene_get_candidates(oibvh_scene_t s, uint32_t* out4, uint64_t cap, uint64_t* n)
+{
+    GUARD_BEGIN
+    if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
+    if (!s->cands_valid) return fail(OIBVH_ERR_STATE, "no broad phase result (use oibvh_scene_broad)");
+    if (n) *n = s->cand_count;
+    const uint64_t k = std::min(cap, s->cand_count);
+    if (k == 0) return OIBVH_OK;
+    if (!out4) return fail(OIBVH_ERR_ARG, "out4 is NULL");
+    DeviceGuard g(s->device);
+    std::vector<uint64_t> tmp(k);
+    CUDA_TRY(cudaMemcpy(tmp.data(), s->cand.p, k * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    for (uint64_t i = 0; i < k; ++i) {
+        const PairView& pv = s->last_pairs[bvtt_pair(tmp[i])];
+        out4[4 * i + 0] = pv.a;
+        out4[4 * i + 1] = pv.b;
+        out4[4 * i + 2] = bvtt_a(tmp[i]);
+        out4[4 * i + 3] = bvtt_b(tmp[i]);
+    }
+    return OIBVH_OK;
+    GUARD_END
+}
+
+API int oibvh_scene_set_queue_capacity(oibvh_scene_t s, uint32_t front, uint32_t candidates, uint32_t hits)
+{
+    if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
+    if (front > 0x7fffffffu || candidates > 0x7fffffffu || hits > 0x7fffffffu)
+        return fail(OIBVH_ERR_ARG, "capacity above 2^31");
+    // shrinking the hit queue would drop hits of the last detect
+    if (front) {
+        s->front_cap = front;
+        s->front0.release();
+        s->front1.release();
+    }
+    if (candidates) {
+        s->cand_cap = candidates;
+        s->cand.release();
+        s->cands_valid = false;
+    }
+    if (hits) {
+        s->hit_cap = hits;
+        s->hits.release();
+        s->hit_count = 0;
+    }
+    return OIBVH_OK;
+}
+
+API int oibvh_scene_get_stats(oibvh_scene_t s, oibvh_detect_stats* out)
+{
+    if (!s || !out) return fail(OIBVH_ERR_ARG, "scene or out is NULL");
+    *out = s->stats;
+    return OIBVH_OK;
+}
+
+API int oibvh_scene_destroy(oibvh_scene_t s)
+{
+    if (!s) return OIBVH_OK;
+    {
+        DeviceGuard g(s->device);
+        delete s;
+    }
+    return OIBVH_OK;
+}

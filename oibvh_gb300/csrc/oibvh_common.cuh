@@ -1,0 +1,136 @@
+// Shared device/host definitions of the oibvh GB300 collision library.
+//
+// Tree layout (the reference's, include/cuda/oibvh.cuh:56-182): T primitives
+// sorted by Morton code are the leaves of a complete binary tree of height
+// L = log2(nextpow2(T)); the vl = 2^L - T rightmost leaves are "virtual" and
+// every node whose subtree holds only virtual leaves is dropped. The remaining
+// ("real") nodes are stored level by level, root first, left-justified. Level
+// l holds real(l) = 2^l - (vl >> (L-l)) = ceil(real(l+1)/2) nodes, node j of
+// level l merges children 2j and 2j+1 (the latter only when 2j+1 < real(l+1)).
+//
+// In HBM every node is 32 bytes: float4 (min.xyz, 0) then float4 (max.xyz, 0),
+// so a node is one aligned 32-byte sector and loads as two float4.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace oibvh {
+
+constexpr uint32_t kMaxLeafLevel = 23;   // T <= 2^23 triangles per mesh
+constexpr uint32_t kMaxPairsPerPass = 1u << 16;  // pair id field of a BVTT node
+
+// BVTT node / candidate encoding: [pair:16][a:24][b:24], a and b are implicit
+// indices (candidates: leaf indices in Morton order).
+__host__ __device__ __forceinline__ uint64_t bvtt_pack(uint32_t pair, uint32_t a, uint32_t b)
+{
+    return ((uint64_t)pair << 48) | ((uint64_t)a << 24) | (uint64_t)b;
+}
+__host__ __device__ __forceinline__ uint32_t bvtt_pair(uint64_t v) { return (uint32_t)(v >> 48); }
+__host__ __device__ __forceinline__ uint32_t bvtt_a(uint64_t v) { return (uint32_t)(v >> 24) & 0xffffffu; }
+__host__ __device__ __forceinline__ uint32_t bvtt_b(uint64_t v) { return (uint32_t)v & 0xffffffu; }
+
+// next_power_of_two / ilog2 (include/cuda/utils.cuh:66-86)
+__host__ __device__ __forceinline__ uint32_t next_pow2(uint32_t x)
+{
+    x--;
+    x |= x >> 1;
+    x |= x >> 2;
+    x |= x >> 4;
+    x |= x >> 8;
+    x |= x >> 16;
+    return x + 1;
+}
+
+__host__ __device__ __forceinline__ uint32_t ilog2(uint32_t x)
+{
+#ifdef __CUDA_ARCH__
+    return 31u - (uint32_t)__clz(x);
+#else
+    return 31u - (uint32_t)__builtin_clz(x);
+#endif
+}
+
+__host__ __device__ __forceinline__ uint32_t popc(uint32_t x)
+{
+#ifdef __CUDA_ARCH__
+    return (uint32_t)__popc(x);
+#else
+    return (uint32_t)__builtin_popcount(x);
+#endif
+}
+
+// Static shape of one tree (everything derives from T).
+struct TreeShape {
+    uint32_t nT;   // real leaves
+    uint32_t L;    // leaf level
+    uint32_t vl;   // virtual leaves
+    uint32_t size; // real nodes, oibvh_get_size (include/cuda/oibvh.cuh:56-59)
+
+    __host__ __device__ static TreeShape of(uint32_t nT)
+    {
+        TreeShape s;
+        s.nT = nT;
+        const uint32_t p = next_pow2(nT);
+        s.L = ilog2(p);
+        s.vl = p - nT;
+        s.size = 2u * nT + popc(s.vl) - 1u;
+        return s;
+    }
+    // real(l): include/cuda/oibvh.cuh:81-85
+    __host__ __device__ __forceinline__ uint32_t level_count(uint32_t l) const
+    {
+        return (1u << l) - (vl >> (L - l));
+    }
+    // number of virtual nodes above level l (levels 0..l-1): oibvh.cuh:94-99
+    __host__ __device__ __forceinline__ uint32_t virtual_above(uint32_t l) const
+    {
+        if (l == 0) return 0;
+        const uint32_t vc = vl >> (L - (l - 1));
+        return (vc << 1) - popc(vc);
+    }
+    // offset of level l in the real-node array
+    __host__ __device__ __forceinline__ uint32_t level_offset(uint32_t l) const
+    {
+        return (1u << l) - 1u - virtual_above(l);
+    }
+    // implicit index -> real index (include/cuda/oibvh.cuh:108-113)
+    __host__ __device__ __forceinline__ uint32_t real_index(uint32_t implicit) const
+    {
+        return implicit - virtual_above(ilog2(implicit + 1u));
+    }
+};
+
+// Device view of one tree.
+struct TreeView {
+    float4* box;        // 2*size float4: level-ordered real nodes
+    const uint4* face;  // Morton-sorted faces: (v0, v1, v2, original face index)
+    const float* xyz;   // 3 floats per vertex
+    TreeShape shape;
+    uint32_t nV;
+    uint32_t pad0;
+};
+
+// One mesh pair of a detection pass.
+struct PairView {
+    uint32_t a, b;            // tree ids (index into the TreeView table)
+    uint32_t front_off;       // first initial-front node of this pair
+    uint32_t front_cnt_a;     // real nodes of A at the entry level
+    uint32_t front_cnt_b;     // real nodes of B at the entry level
+    uint32_t entry_a, entry_b;
+    uint32_t pad0;
+};
+
+// Status bits a kernel can raise (the host turns them into status codes).
+enum DeviceFlag : uint32_t {
+    kFlagFrontOverflow = 1u << 0,
+    kFlagCandOverflow = 1u << 1,
+    kFlagHitOverflow = 1u << 2,
+    kFlagBadInput = 1u << 3,
+};
+
+// glm::min / glm::max semantics (third/glm/detail/func_common.inl:17-29).
+__host__ __device__ __forceinline__ float gmin(float x, float y) { return (y < x) ? y : x; }
+__host__ __device__ __forceinline__ float gmax(float x, float y) { return (x < y) ? y : x; }
+
+} // namespace oibvh

@@ -1,0 +1,65 @@
+// Host-side launchers of the device kernels (one translation unit per stage).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "oibvh_common.cuh"
+
+namespace oibvh {
+
+// Count of this library's kernel launches (all devices), for benchmarks.
+void note_launches(uint64_t n);
+
+// One tree of a (possibly multi-tree) refit launch.
+struct RefitJob {
+    float4* box;
+    const uint4* face;
+    const float* xyz;
+    TreeShape shape;
+    uint32_t block_begin;  // first CTA of this tree in the launch
+    uint32_t n_blocks;
+    uint32_t* counters;    // refit_counters_per_tree() zeroed words
+    uint32_t pad0;
+};
+
+// build_kernels.cu
+size_t radix_sort_scratch_bytes(uint32_t n);
+cudaError_t launch_mesh_bounds(const float* xyz, uint32_t nV, uint32_t* bound_keys, int num_sms, cudaStream_t s);
+cudaError_t launch_leaf_morton(const uint32_t* tri, const float* xyz, uint32_t nT, const uint32_t* bound_keys,
+                               uint32_t* codes, uint32_t* idx, cudaStream_t s);
+cudaError_t launch_radix_sort(uint32_t* keys, uint32_t* vals, uint32_t n, int key_bits, void* scratch,
+                              cudaStream_t s);
+cudaError_t launch_gather_faces(const uint32_t* tri, const uint32_t* perm, uint32_t nT, uint4* out, cudaStream_t s);
+
+// refit_kernels.cu
+uint32_t refit_blocks_for(uint32_t nT);
+uint32_t refit_counters_per_tree();
+cudaError_t launch_refit_one(const RefitJob& job, cudaStream_t s);
+cudaError_t launch_refit(const RefitJob* d_jobs, uint32_t n_jobs, uint32_t total_blocks, uint32_t* d_counters,
+                         size_t n_counters, cudaStream_t s);
+
+// detect_kernels.cu
+struct DetectArgs {
+    const TreeView* trees;
+    const PairView* pairs;
+    uint32_t n_pairs;
+    uint32_t expand_levels;
+    uint64_t* front[2];
+    uint32_t front_cap;
+    uint64_t* cand;
+    uint32_t cand_cap;
+    uint4* hits;
+    uint32_t hit_cap;
+    uint32_t* counts;  // [0] hits, [1] flags, [2] candidates, [3 + it] front size entering step it
+    uint32_t iters;
+    int grid;          // CTAs for the grid-stride kernels
+};
+cudaError_t launch_init_front(const DetectArgs& a, uint32_t total, cudaStream_t s);
+cudaError_t launch_bvtt_step(const DetectArgs& a, uint32_t it, cudaStream_t s);
+cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s);
+
+constexpr uint32_t kCountHits = 0, kCountFlags = 1, kCountCands = 2, kCountFront0 = 3;
+
+} // namespace oibvh

@@ -1,0 +1,127 @@
+"""The named synthetic workloads (seeded, deterministic).
+
+plain       two icospheres s=5 (20,480 triangles, 10,242 vertices each),
+            radius 1, centres (-0.9,0,0) and (0.9,0,0): build, refit once,
+            broad + narrow, sorted pair set.
+deforming   two noise-displaced icospheres s=8 (1,310,720 triangles each);
+            mesh B gets a seeded random rigid transform placing it so that
+            about 1% of its surface lies inside A (the overlapping cap).
+            Every frame adds fresh per-vertex Gaussian jitter (sigma 1e-3)
+            to the rest positions of both meshes, refits both trees and
+            detects.
+batched     `n_pairs` independent pairs of noise-displaced icospheres whose
+            subdivision is drawn so triangle counts are log-uniform over
+            1k..1M; each pair gets a seeded rigid transform that puts
+            30..70% of B's surface inside A.
+
+"Overlap fraction" of a pair = fraction of B's surface inside A's ball,
+computed from the sphere-cap area: for balls of radii a >= b at distance d
+the cut plane lies x = (d^2 + b^2 - a^2) / (2d) from B's centre and the cap
+inside A is (b - x) / (2b) of B's area.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import meshes as M
+
+
+@dataclass
+class PairWorkload:
+    name: str
+    meshes: list                       # rest meshes
+    pairs: list                        # (i, j) mesh pairs tested
+    jitter_sigma: float = 0.0
+    seed: int = 0
+    info: dict = field(default_factory=dict)
+
+    def frame_positions(self, frame: int) -> list:
+        """Positions of every mesh at `frame` (frame 0 = rest positions)."""
+        if frame == 0 or self.jitter_sigma == 0.0:
+            return [m.xyz for m in self.meshes]
+        return [M.jitter(m.xyz, self.jitter_sigma, self.seed * 1000 + i, frame) for i, m in enumerate(self.meshes)]
+
+
+def plain() -> PairWorkload:
+    a = M.icosphere(5, 1.0, (-0.9, 0.0, 0.0))
+    b = M.icosphere(5, 1.0, (0.9, 0.0, 0.0))
+    return PairWorkload("plain: 2 icospheres s=5, centres 1.8 apart", [a, b], [(0, 1)])
+
+
+def _unit_vector(rng: np.random.Generator) -> np.ndarray:
+    while True:
+        v = rng.uniform(-1.0, 1.0, 3)
+        n2 = float(v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
+        if 1e-6 < n2 <= 1.0:
+            return v / math.sqrt(n2)
+
+
+def distance_for_overlap(a: float, b: float, frac: float) -> float:
+    """Centre distance at which `frac` of sphere B (radius b <= a) lies inside ball A."""
+    x = b * (1.0 - 2.0 * frac)
+    return x + math.sqrt(x * x - b * b + a * a)
+
+
+def deforming(subdiv: int = 8, seed: int = 2024, overlap: float = 0.01, noise: float = 0.05,
+              sigma: float = 1e-3) -> PairWorkload:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    base = M.icosphere(subdiv)
+    a = M.noise_displace(base, noise, seed=seed + 1)
+    b0 = M.noise_displace(base, noise, seed=seed + 2)
+    R = M.random_rotation(rng)
+    d = distance_for_overlap(1.0, 1.0, overlap)
+    t = _unit_vector(rng) * d
+    b = M.rigid_transform(b0, R, t)
+    w = PairWorkload(f"deforming: 2 noise icospheres s={subdiv}, {overlap:.0%} overlap, jitter {sigma:g}",
+                     [a, b], [(0, 1)], jitter_sigma=sigma, seed=seed)
+    w.info = {"subdiv": subdiv, "triangles_per_mesh": a.n_triangles, "vertices_per_mesh": a.n_vertices,
+              "centre_distance": d, "overlap_target": overlap}
+    return w
+
+
+# icosphere subdivision -> triangles: 20 * 4^s (s=3: 1,280 ... s=7: 327,680)
+_BATCH_SUBDIVS = (3, 4, 5, 6, 7)
+
+
+def _subdiv_probs(lo: float = 1e3, hi: float = 1e6) -> np.ndarray:
+    """Probability of each subdivision so that log(T) is uniform over [lo, hi]:
+    each s takes the log-mass of the interval around its T (midpoints in log space)."""
+    logs = np.array([math.log(20 * 4 ** s) for s in _BATCH_SUBDIVS])
+    edges = np.concatenate([[math.log(lo)], (logs[1:] + logs[:-1]) / 2, [math.log(hi)]])
+    w = np.clip(np.diff(edges), 0, None)
+    return w / w.sum()
+
+
+def batched(n_pairs: int = 512, seed: int = 77, noise: float = 0.05, frac_lo: float = 0.3,
+            frac_hi: float = 0.7, sigma: float = 1e-3) -> PairWorkload:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    probs = _subdiv_probs()
+    cache = {}
+
+    def sphere(s):
+        if s not in cache:
+            cache[s] = M.icosphere(s)
+        return cache[s]
+
+    meshes, pairs, fracs = [], [], []
+    for p in range(n_pairs):
+        sa, sb = (int(x) for x in rng.choice(_BATCH_SUBDIVS, size=2, p=probs))
+        rb = float(rng.uniform(0.6, 1.0))
+        frac = float(rng.uniform(frac_lo, frac_hi))
+        a = M.noise_displace(sphere(sa), noise, seed=seed * 100000 + 2 * p)
+        b0 = M.noise_displace(sphere(sb), noise * rb, seed=seed * 100000 + 2 * p + 1)
+        b0 = M.Mesh((b0.xyz.astype(np.float64) * rb).astype(np.float32), b0.tri)
+        d = distance_for_overlap(1.0, rb, frac)
+        b = M.rigid_transform(b0, M.random_rotation(rng), _unit_vector(rng) * d)
+        meshes += [a, b]
+        pairs.append((2 * p, 2 * p + 1))
+        fracs.append(frac)
+    w = PairWorkload(f"batched: {n_pairs} pairs of noise icospheres, T log-uniform 1k-1M, 30-70% overlap",
+                     meshes, pairs, jitter_sigma=sigma, seed=seed)
+    tri = np.array([m.n_triangles for m in meshes])
+    w.info = {"n_pairs": n_pairs, "triangles_total": int(tri.sum()), "triangles_min": int(tri.min()),
+              "triangles_max": int(tri.max()), "overlap_mean": float(np.mean(fracs))}
+    return w

@@ -1,0 +1,26 @@
+#!/usr/bin/env bash
+# ORACLE — test infrastructure only.
+# Compiles the reference's own CPU collision path, from the reference sources
+# where they lie, into oracle/_ref/libref_cpu.so. Needs the reference checkout
+# (default /root/reference, override with OIBVH_REFERENCE) and g++; it does not
+# use the reference's CMake build. Flags: -O2 -DNDEBUG (the reference asserts
+# on triangle 0, src/cpu/simpleCollide.cpp:91-92, and is built release) and
+# -ffp-contract=off (no fused multiply-add, as MSVC's default /fp:precise and
+# x86-64 without FMA give the reference's own build).
+set -euo pipefail
+REF="${OIBVH_REFERENCE:-/root/reference}"
+HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+OUT="$HERE/_ref"
+CUDA_INC="${CUDA_HOME:-/usr/local/cuda}/include"
+if [ ! -f "$REF/src/cpu/simpleBVH.cpp" ]; then
+  echo "reference sources not found under $REF" >&2
+  exit 2
+fi
+mkdir -p "$OUT"
+g++ -std=c++17 -O2 -DNDEBUG -ffp-contract=off -fPIC -shared -w \
+  -include "$HERE/ref_compat.h" \
+  -I"$REF/include" -I"$REF/third" -I"$REF/third/glad/include" -I"$CUDA_INC" \
+  "$REF/src/cpu/simpleBVH.cpp" "$REF/src/utils/utils.cpp" "$HERE/ref_harness.cpp" \
+  -o "$OUT/libref_cpu.so.tmp"
+mv "$OUT/libref_cpu.so.tmp" "$OUT/libref_cpu.so"
+echo "built $OUT/libref_cpu.so"

@@ -1,0 +1,146 @@
+"""Behaviour of the C ABI on the GPU: errors, split stages, copies, device
+pointers, queue regrowth."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from oracle.oracle import Port, sort_pairs
+
+pytestmark = pytest.mark.gpu
+
+
+def _scene(meshes):
+    from oibvh_gb300 import OibvhTree, Scene
+
+    trees = [OibvhTree(m) for m in meshes]
+    for t in trees:
+        t.build()
+    sc = Scene()
+    for t in trees:
+        sc.addOibvhTree(t)
+    return sc, trees
+
+
+def test_cpu_device_type_is_refused(gpu):
+    from oibvh_gb300 import DeviceType, OibvhError
+
+    g = load_golden("config1")
+    sc, _ = _scene(g["meshes"])
+    with pytest.raises(OibvhError) as e:
+        sc.detectCollision(DeviceType.CPU, 4, 3)
+    assert e.value.status == 6
+
+
+def test_bad_arguments(gpu):
+    from oibvh_gb300 import DeviceType, OibvhError, OibvhTree, Scene
+
+    g = load_golden("config1")
+    sc, trees = _scene(g["meshes"])
+    with pytest.raises(OibvhError) as e:
+        sc.detectCollision(DeviceType.GPU0, 4, 0)
+    assert e.value.status == 1
+    with pytest.raises(OibvhError):
+        sc.set_pairs([(0, 0)])
+    with pytest.raises(OibvhError):
+        sc.set_pairs([(0, 5)])
+    unbuilt = OibvhTree(g["meshes"][0])
+    with pytest.raises(OibvhError) as e:
+        Scene().addOibvhTree(unbuilt)
+    assert e.value.status == 5
+    with pytest.raises(OibvhError):
+        unbuilt.refit()
+
+
+def test_broad_then_narrow_equals_detect(gpu):
+    from oibvh_gb300 import DeviceType
+
+    g = load_golden("config1")
+    sc, trees = _scene(g["meshes"])
+    sc.broad(DeviceType.GPU0, 4, 3)
+    assert sc.candidate_count() == g["candidates"][0]
+    cands = sc.candidates()
+    assert cands.shape == (g["candidates"][0], 4)
+    # candidates are leaf pairs in Morton order: map to original faces and
+    # check against the oracle's leaf-box overlap set
+    perms = [t.sorted_faces()[1] for t in trees]
+    orig = np.stack([perms[0][cands[:, 2]], perms[1][cands[:, 3]]], 1)
+    assert len({tuple(r) for r in orig}) == orig.shape[0]
+    sc.narrow()
+    assert np.array_equal(sc.int_tri_pairs(), g["hits"][0])
+
+
+def test_queue_regrowth(gpu):
+    from oibvh_gb300 import DeviceType
+
+    g = load_golden("identical")
+    sc, _ = _scene(g["meshes"])
+    sc.set_queue_capacity(front=8, candidates=8, hits=4)
+    sc.detectCollision(DeviceType.GPU0, 2, 1)
+    assert np.array_equal(sc.int_tri_pairs(), g["hits"][0])
+    assert sc.stats()["retries"] >= 1
+
+
+def test_copy_tree_then_refit(gpu):
+    """OibvhTree(other, mesh) + refit, the sequence of src/main.cpp:129-135."""
+    from oibvh_gb300 import DeviceType, OibvhTree, Scene
+    from oibvh_gb300 import meshes as M
+
+    a = M.noise_displace(M.icosphere(4), 0.05, seed=3)
+    b = M.Mesh(a.xyz + np.array([1.0, 0.0, 0.0], np.float32), a.tri)  # translate(+1, 0, 0)
+    ta = OibvhTree(a)
+    ta.build()
+    tb = OibvhTree.copy_of(ta, b)
+    tb.refit()
+    sc = Scene()
+    sc.addOibvhTree(ta)
+    sc.addOibvhTree(tb)
+    sc.detectCollision(DeviceType.GPU0, 4, 3)
+    p = Port()
+    p.add_mesh(a.xyz, a.tri)
+    p.add_mesh(b.xyz, b.tri)
+    want, wc = p.detect()
+    assert np.array_equal(sc.int_tri_pairs(), sort_pairs(want))
+    assert sc.candidate_count() == wc
+    assert sc.getIntTriPairCount() == want.shape[0]
+
+
+def test_refit_from_device_pointer(gpu):
+    import torch
+
+    from oibvh_gb300 import DeviceType
+
+    g = load_golden("deforming")
+    sc, trees = _scene(g["meshes"])
+    fr = g["frames"][1]
+    dev = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in fr]
+    torch.cuda.synchronize()
+    for t, d in zip(trees, dev):
+        t.refit_device(d.data_ptr())
+    sc.detectCollision(DeviceType.GPU0, 4, 3)
+    assert np.array_equal(sc.int_tri_pairs(), g["hits"][2])
+
+
+def test_one_triangle_meshes(gpu):
+    from oibvh_gb300 import DeviceType
+    from oibvh_gb300 import meshes as M
+
+    a = M.Mesh(np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32), np.array([[0, 1, 2]], np.uint32))
+    b = M.Mesh(np.array([[0.2, 0.2, -1], [0.2, 0.2, 1], [0.3, 0.1, 0]], np.float32), np.array([[0, 1, 2]], np.uint32))
+    sc, trees = _scene([a, b])
+    assert trees[0].size == 1 and trees[0].getDepth() == 0
+    sc.detectCollision(DeviceType.GPU0, 0, 1)
+    assert sc.int_tri_pairs().tolist() == [[0, 1, 0, 0]]
+
+
+def test_stream_argument(gpu):
+    import torch
+
+    from oibvh_gb300 import DeviceType
+
+    g = load_golden("noise_spheres")
+    sc, trees = _scene(g["meshes"])
+    s = torch.cuda.Stream()
+    sc.detectCollision(DeviceType.GPU0, 4, 3, stream=s)
+    assert np.array_equal(sc.int_tri_pairs(), g["hits"][0])

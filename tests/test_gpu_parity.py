@@ -1,0 +1,126 @@
+"""CUDA path vs the reference's pair sets (golden fixtures) and vs the oracle port.
+
+Bit-exact: the colliding-pair set, the candidate count, the Morton order and
+every node box of the tree (integer / min-max work, no tolerance)."""
+import numpy as np
+import pytest
+
+from cases import CASES
+from conftest import load_golden
+from oracle.oracle import Port, sort_pairs
+
+pytestmark = pytest.mark.gpu
+
+
+def run_gpu(meshes, pairs, frames, entry, expand):
+    from oibvh_gb300 import DeviceType, OibvhTree, Scene
+
+    trees = [OibvhTree(m) for m in meshes]
+    for t in trees:
+        t.build()
+    sc = Scene()
+    for t in trees:
+        sc.addOibvhTree(t)
+    if pairs is not None:
+        sc.set_pairs(pairs)
+    out = []
+    sc.detectCollision(DeviceType.GPU0, entry, expand)
+    out.append((sc.int_tri_pairs(), sc.candidate_count()))
+    for fr in frames:
+        for t, xyz in zip(trees, fr):
+            t.refit(xyz)
+        sc.detectCollision(DeviceType.GPU0, entry, expand)
+        out.append((sc.int_tri_pairs(), sc.candidate_count()))
+    return out
+
+
+@pytest.mark.parametrize("entry,expand", [(0, 1), (4, 3), (2, 2), (30, 1)])
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_golden_pair_sets(gpu, name, entry, expand):
+    g = load_golden(name)
+    res = run_gpu(g["meshes"], g["pairs"], g["frames"], entry, expand)
+    for f, (hits, ncand) in enumerate(res):
+        assert hits.shape == g["hits"][f].shape, f"frame {f}: {hits.shape[0]} hits, expected {g['hits'][f].shape[0]}"
+        assert np.array_equal(hits, g["hits"][f]), f"frame {f}"
+        assert ncand == g["candidates"][f], f"frame {f}"
+
+
+@pytest.mark.parametrize("name", ["config1", "noise_spheres", "soups", "three_bodies"])
+def test_tree_layout_bit_exact(gpu, name):
+    from oibvh_gb300 import OibvhTree
+
+    g = load_golden(name)
+    for m in g["meshes"]:
+        t = OibvhTree(m)
+        t.build()
+        aabbs, st, perm = Port.oibvh_build(m.xyz, m.tri)
+        f, p = t.sorted_faces()
+        assert np.array_equal(p, perm)
+        assert np.array_equal(f, st)
+        got = t.aabb_tree()
+        assert got.shape == aabbs.shape
+        assert np.array_equal(got.view(np.uint32), aabbs.view(np.uint32))
+        assert t.getPrimCount() == m.n_triangles
+        assert t.getDepth() == int(np.floor(np.log2(aabbs.shape[0])))
+
+
+def test_refit_layout_bit_exact(gpu):
+    from oibvh_gb300 import OibvhTree
+
+    g = load_golden("deforming")
+    m = g["meshes"][0]
+    t = OibvhTree(m)
+    t.build()
+    st, _ = t.sorted_faces()
+    for fr in g["frames"]:
+        t.refit(fr[0])
+        want = Port.oibvh_refit(fr[0], st)
+        assert np.array_equal(t.aabb_tree().view(np.uint32), want.view(np.uint32))
+
+
+def _oracle_pairs(meshes, pairs=None):
+    p = Port()
+    for m in meshes:
+        p.add_mesh(m.xyz, m.tri)
+    h, c = p.detect(pairs)
+    return sort_pairs(h), c
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_soups_vs_oracle(gpu, seed):
+    from tests_support import soup_pair
+
+    meshes = soup_pair(seed)
+    want, wc = _oracle_pairs(meshes)
+    got = run_gpu(meshes, None, [], seed % 5, 1 + seed % 3)[0]
+    assert np.array_equal(got[0], want) and got[1] == wc
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_random_scenes_vs_oracle(gpu, seed):
+    """4-6 meshes of mixed kinds, all pairs or a random subset of pairs."""
+    from tests_support import mixed_scene
+
+    meshes, pairs = mixed_scene(seed)
+    want, wc = _oracle_pairs(meshes, pairs)
+    got = run_gpu(meshes, pairs, [], 3, 2)[0]
+    assert np.array_equal(got[0], want) and got[1] == wc
+
+
+def test_deforming_s8_frames_vs_oracle(gpu):
+    """The deforming workload at full size (1,310,720 triangles per mesh), two frames."""
+    from oibvh_gb300 import workloads as W
+
+    w = W.deforming()
+    frames = [w.frame_positions(f) for f in (1, 2)]
+    res = run_gpu(w.meshes, None, frames, 4, 3)
+    p = Port()
+    for m in w.meshes:
+        p.add_mesh(m.xyz, m.tri)
+    for f in range(3):
+        if f:
+            for i, xyz in enumerate(frames[f - 1]):
+                p.set_positions(i, xyz)
+        want, wc = p.detect()
+        assert np.array_equal(res[f][0], sort_pairs(want)), f"frame {f}"
+        assert res[f][1] == wc
