@@ -42,6 +42,7 @@ enum oibvh_status {
     OIBVH_ERR_OVERFLOW = 4,    /* a work queue stayed too small after regrowing */
     OIBVH_ERR_STATE = 5,       /* call out of order (e.g. detect before build) */
     OIBVH_ERR_UNSUPPORTED = 6, /* e.g. the CPU device type */
+    OIBVH_ERR_TIMEOUT = 7,     /* a bounded device-side wait gave up (the context stays usable) */
 };
 
 /* DeviceType (include/cuda/scene.cuh:12-24): CPU = -1, GPU0..GPU8 = 0..8. */
@@ -89,6 +90,14 @@ int oibvh_tree_refit(oibvh_tree_t t, const float* xyz, void* stream);
  * it alive and unchanged until every detect that uses this tree is done. */
 int oibvh_tree_refit_device(oibvh_tree_t t, const float* d_xyz, void* stream);
 
+/* Set the positions the next refit (of this tree, or of its scene) uses,
+ * without refitting: from a host array (copied, stream-ordered) or from
+ * device memory (borrowed, same rules as oibvh_tree_refit_device). The
+ * reference moves vertices through Mesh::transform and reads them back in
+ * OibvhTree::refit (src/utils/mesh.cpp:187-214, src/cuda/oibvhTree.cu:196-199). */
+int oibvh_tree_set_positions(oibvh_tree_t t, const float* xyz, void* stream);
+int oibvh_tree_set_positions_device(oibvh_tree_t t, const float* d_xyz);
+
 /* OibvhTree::getDepth() (src/cuda/oibvhTree.cu:46-49) = floor(log2(size)). */
 uint32_t oibvh_tree_get_depth(oibvh_tree_t t);
 /* OibvhTree::getPrimCount() (src/cuda/oibvhTree.cu:51-54). */
@@ -124,8 +133,11 @@ int oibvh_scene_set_pairs(oibvh_scene_t s, const uint32_t* pairs, uint32_t n_pai
 /* Scene::detectCollision(deviceType, entryLevel, expandLevels)
  * (src/cuda/scene.cu:157-185,225-446): BVTT broad phase from the cross
  * product of the nodes at entry_level (clamped to each tree's leaf level),
- * expanding expand_levels (1..16) levels per step, then the triangle test.
- * Blocking: returns once the pair count is known. */
+ * each step expanding a pair expand_levels levels down on both sides
+ * (1..16 accepted; steps deeper than 3 levels run as 3), with the triangle
+ * test fused into the traversal. The pair set does not depend on
+ * entry_level or expand_levels: they only shape the work. Blocking:
+ * returns once the pair count is known. */
 int oibvh_scene_detect(oibvh_scene_t s, int device_type, uint32_t entry_level, uint32_t expand_levels, void* stream);
 
 /* The two halves of detect (src/cuda/scene.cu:270-311 and :382-423):
@@ -133,6 +145,12 @@ int oibvh_scene_detect(oibvh_scene_t s, int device_type, uint32_t entry_level, u
  * their count); narrow tests them (blocking). */
 int oibvh_scene_broad(oibvh_scene_t s, int device_type, uint32_t entry_level, uint32_t expand_levels, void* stream);
 int oibvh_scene_narrow(oibvh_scene_t s, void* stream);
+
+/* OibvhTree::refit() for every tree of the scene in ONE kernel launch, each
+ * to its current positions (oibvh_tree_set_positions*). Stream-ordered. The
+ * reference refits tree by tree with a host round trip each
+ * (src/main.cpp:210-214,247-251, src/cuda/oibvhTree.cu:193-235). */
+int oibvh_scene_refit(oibvh_scene_t s, void* stream);
 
 /* Scene::getIntTriPairCount() (src/cuda/scene.cu:50-53). */
 uint32_t oibvh_scene_get_int_tri_pair_count(oibvh_scene_t s);

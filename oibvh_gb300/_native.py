@@ -25,6 +25,7 @@ ERR_CUDA = 3
 ERR_OVERFLOW = 4
 ERR_STATE = 5
 ERR_UNSUPPORTED = 6
+ERR_TIMEOUT = 7
 
 DEVICE_CPU = -1
 
@@ -53,6 +54,8 @@ SIGNATURES = [
     ("oibvh_tree_build", ctypes.c_int, [_vp, _vp]),
     ("oibvh_tree_refit", ctypes.c_int, [_vp, _f32p, _vp]),
     ("oibvh_tree_refit_device", ctypes.c_int, [_vp, _vp, _vp]),
+    ("oibvh_tree_set_positions", ctypes.c_int, [_vp, _f32p, _vp]),
+    ("oibvh_tree_set_positions_device", ctypes.c_int, [_vp, _vp]),
     ("oibvh_tree_get_depth", _u32, [_vp]),
     ("oibvh_tree_get_prim_count", _u32, [_vp]),
     ("oibvh_tree_get_size", _u32, [_vp]),
@@ -65,6 +68,7 @@ SIGNATURES = [
     ("oibvh_scene_detect", ctypes.c_int, [_vp, ctypes.c_int, _u32, _u32, _vp]),
     ("oibvh_scene_broad", ctypes.c_int, [_vp, ctypes.c_int, _u32, _u32, _vp]),
     ("oibvh_scene_narrow", ctypes.c_int, [_vp, _vp]),
+    ("oibvh_scene_refit", ctypes.c_int, [_vp, _vp]),
     ("oibvh_scene_get_int_tri_pair_count", _u32, [_vp]),
     ("oibvh_scene_get_candidate_count", _u64, [_vp]),
     ("oibvh_scene_get_int_tri_pairs", ctypes.c_int, [_vp, _u32p, _u64, ctypes.POINTER(_u64)]),
@@ -123,7 +127,7 @@ def status_string(status: int) -> str:
         return lib().oibvh_status_string(status).decode()
     except Exception:  # library not loadable: still give a name
         return {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "queue overflow",
-                5: "invalid state", 6: "unsupported"}.get(status, "unknown status")
+                5: "invalid state", 6: "unsupported", 7: "device wait timed out"}.get(status, "unknown status")
 
 
 def check(status: int, func: str) -> None:

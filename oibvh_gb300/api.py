@@ -126,6 +126,20 @@ class OibvhTree:
         N.check(N.lib().oibvh_tree_refit_device(self._h, ctypes.c_void_p(int(d_xyz_ptr)), _stream_handle(stream)),
                 "oibvh_tree_refit_device")
 
+    def set_positions(self, xyz, stream=None) -> None:
+        """Host positions for the next refit (copied, stream-ordered), no refit."""
+        x = _f32(xyz)
+        if x.size != 3 * self.vertex_count:
+            raise ValueError("positions must be float32[V,3]")
+        N.check(N.lib().oibvh_tree_set_positions(self._h, x.ctypes.data_as(N._f32p), _stream_handle(stream)),
+                "oibvh_tree_set_positions")
+        self._keep = x
+
+    def set_positions_device(self, d_xyz_ptr: int) -> None:
+        """Device positions (raw pointer) for the next refit, borrowed, no refit."""
+        N.check(N.lib().oibvh_tree_set_positions_device(self._h, ctypes.c_void_p(int(d_xyz_ptr))),
+                "oibvh_tree_set_positions_device")
+
     # reference accessors
     def getDepth(self) -> int:
         return int(N.lib().oibvh_tree_get_depth(self._h))
@@ -207,6 +221,10 @@ class Scene:
 
     def narrow(self, stream=None) -> None:
         N.check(N.lib().oibvh_scene_narrow(self._h, _stream_handle(stream)), "oibvh_scene_narrow")
+
+    def refit(self, stream=None) -> None:
+        """Refit every tree of the scene in one launch (to the positions set last)."""
+        N.check(N.lib().oibvh_scene_refit(self._h, _stream_handle(stream)), "oibvh_scene_refit")
 
     def getIntTriPairCount(self) -> int:
         return int(N.lib().oibvh_scene_get_int_tri_pair_count(self._h))

@@ -6,10 +6,13 @@
 // triangle_intersect_kernel (src/cuda/collide.cu:248-299) with
 // triangleIntersection2 (third/gProximity/cuda_intersect_tritri.h:350-434).
 //
-// Every BVTT level is one grid-stride launch that reads its front size from
-// device memory, so the host enqueues all levels without reading anything
-// back. Appends (next front, candidates, hits) are warp-aggregated: one
-// atomicAdd per warp, positions from ballot/shuffle prefix sums.
+// The broad phase is one persistent cooperative kernel (k_traverse) that
+// walks the BVTT front level by level with a bounded grid barrier between
+// levels, so the host enqueues one launch and reads counters back once.
+// Appends (next front, candidates, hits) are warp-aggregated: one atomicAdd
+// per warp, positions from ballot/shuffle prefix sums. The narrow phase is
+// fused: overlapping leaf pairs are buffered per warp in shared memory and
+// tested 32 at a time.
 //
 // The triangle test reproduces the reference's CPU arithmetic
 // (src/utils/utils.cpp:71-169, glm scalar dot/cross): every product, sum and
@@ -21,12 +24,6 @@
 namespace oibvh {
 
 constexpr int kDetectThreads = 256;
-
-__device__ __forceinline__ bool box_overlap(const float4& a0, const float4& a1, const float4& b0, const float4& b1)
-{
-    // aabb_box_t::overlap (include/utils/utils.h:39-44; src/cuda/collide.cu:12-17)
-    return (a0.x <= b1.x && a1.x >= b0.x) && (a0.y <= b1.y && a1.y >= b0.y) && (a0.z <= b1.z && a1.z >= b0.z);
-}
 
 // ---------------------------------------------------------------------------
 // Exact-rounding SAT
@@ -98,9 +95,6 @@ __device__ __forceinline__ V3 load_vertex(const float* __restrict__ xyz, uint32_
     return V3{__ldg(xyz + 3 * (size_t)v), __ldg(xyz + 3 * (size_t)v + 1), __ldg(xyz + 3 * (size_t)v + 2)};
 }
 
-// ---------------------------------------------------------------------------
-// Counters: [0] hits, [1] flags, [2] candidates, [3 + it] front size at step it
-// ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred, uint32_t lane)
 {
     const uint32_t mask = __ballot_sync(0xffffffffu, pred);
@@ -112,28 +106,9 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred, ui
     return base + __popc(mask & ((1u << lane) - 1u));
 }
 
-// Initial front: for every pair, all real nodes of A at its entry level x all
-// real nodes of B at its entry level (Scene::expandBvttNodes).
-__global__ void __launch_bounds__(kDetectThreads) k_init_front(DetectArgs a, uint32_t total)
-{
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.counts[3] = total;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        uint32_t lo = 0, hi = a.n_pairs - 1;
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi + 1) >> 1;
-            if (a.pairs[mid].front_off <= i) lo = mid;
-            else hi = mid - 1;
-        }
-        const PairView pv = a.pairs[lo];
-        const uint32_t k = i - pv.front_off;
-        const uint32_t x = k / pv.front_cnt_b, y = k - x * pv.front_cnt_b;
-        a.front[0][i] = bvtt_pack(lo, (1u << pv.entry_a) - 1u + x, (1u << pv.entry_b) - 1u + y);
-    }
-}
-
 // Children of implicit node `ia` (level la) `e` levels down, clamped at the
 // leaf level: the first child and the count of real ones
-// (src/cuda/collide.cu:165-176).
+// (src/cuda/collide.cu:165-176). A leaf is its own only child.
 __device__ __forceinline__ void expand_side(const TreeShape& S, uint32_t ia, uint32_t la, uint32_t e,
                                             uint32_t& first, uint32_t& count)
 {
@@ -149,76 +124,233 @@ __device__ __forceinline__ void expand_side(const TreeShape& S, uint32_t ia, uin
     count = min(1u << d, right_valid - first + 1u);
 }
 
-__global__ void __launch_bounds__(kDetectThreads) k_bvtt_step(DetectArgs a, uint32_t it)
+// ---------------------------------------------------------------------------
+// Grid-wide barrier for the cooperative traversal. Co-residency of every CTA
+// is guaranteed by the cooperative launch; the wait is still bounded: after
+// kSpinLimit polls the CTA raises kFlagTimeout and reports failure, and the
+// kernel returns.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kSpinLimit = 1u << 22;  // x ~100 ns per poll: well under a second
+
+__device__ __forceinline__ bool grid_barrier(uint32_t* bar, uint32_t* flags, uint32_t n_blocks, uint32_t* s_ok)
 {
-    const uint32_t n = min(a.counts[3 + it], a.front_cap);
-    const uint64_t* __restrict__ src = (it & 1) ? a.front[1] : a.front[0];
-    uint64_t* __restrict__ dst = (it & 1) ? a.front[0] : a.front[1];
-    uint32_t* dst_count = a.counts + 3 + it + 1;
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t base = warp * 32; base < n; base += n_warps * 32) {
-        const uint32_t i = base + lane;
-        bool cand = false;
-        uint64_t cval = 0;
-        uint32_t pair = 0, firstA = 0, firstB = 0, ncA = 0, ncB = 0;
-        if (i < n) {
-            const uint64_t node = src[i];
-            pair = bvtt_pair(node);
-            const uint32_t ia = bvtt_a(node), ib = bvtt_b(node);
-            const PairView pv = a.pairs[pair];
-            const TreeView& TA = a.trees[pv.a];
-            const TreeView& TB = a.trees[pv.b];
-            const TreeShape SA = TA.shape, SB = TB.shape;
-            const uint32_t la = ilog2(ia + 1u), lb = ilog2(ib + 1u);
-            const uint32_t ra = SA.real_index(ia), rb = SB.real_index(ib);
-            const float4* ba = TA.box + 2 * (size_t)ra;
-            const float4* bb = TB.box + 2 * (size_t)rb;
-            const float4 a0 = __ldg(ba), a1 = __ldg(ba + 1), b0 = __ldg(bb), b1 = __ldg(bb + 1);
-            if (box_overlap(a0, a1, b0, b1)) {
-                if (la == SA.L && lb == SB.L) {
-                    cand = true;
-                    cval = bvtt_pack(pair, ia - ((1u << SA.L) - 1u), ib - ((1u << SB.L) - 1u));
-                } else {
-                    expand_side(SA, ia, la, a.expand_levels, firstA, ncA);
-                    expand_side(SB, ib, lb, a.expand_levels, firstB, ncB);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile uint32_t* vgen = bar + 1;
+        const uint32_t gen = *vgen;
+        __threadfence();
+        const uint32_t arrived = atomicAdd(bar, 1u);
+        uint32_t ok = 1;
+        if (arrived == n_blocks - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            uint32_t spins = 0;
+            while (*vgen == gen) {
+                if (++spins > kSpinLimit) {
+                    atomicOr(flags, (uint32_t)kFlagTimeout);
+                    ok = 0;
+                    break;
                 }
+                __nanosleep(64);
             }
         }
-        const uint32_t cpos = warp_append(a.counts + 2, cand, lane);
-        if (cand) {
-            if (cpos < a.cand_cap) a.cand[cpos] = cval;
-            else atomicOr(a.counts + 1, (uint32_t)kFlagCandOverflow);
+        __threadfence();
+        *s_ok = ok;
+    }
+    __syncthreads();
+    return *s_ok != 0;
+}
+
+// ---------------------------------------------------------------------------
+// Per-warp candidate buffer: leaf pairs whose boxes overlap are queued in
+// shared memory and tested 32 at a time, one per lane, so the 17-axis test
+// runs at full SIMT width however sparse the candidates are.
+// ---------------------------------------------------------------------------
+constexpr int kCandBuf = 64;
+
+struct WarpCands {
+    uint64_t* buf;  // kCandBuf entries
+    uint32_t n;     // warp-uniform
+};
+
+__device__ __forceinline__ void test_candidates(const DetectArgs& a, const uint64_t* buf, uint32_t count,
+                                                uint32_t lane)
+{
+    bool hit = false;
+    uint4 rec = make_uint4(0, 0, 0, 0);
+    if (lane < count) {
+        const uint64_t c = buf[lane];
+        const PairView pv = a.pairs[bvtt_pair(c)];
+        const TreeView& TA = a.trees[pv.a];
+        const TreeView& TB = a.trees[pv.b];
+        const uint4 fa = __ldg(TA.face + bvtt_a(c));
+        const uint4 fb = __ldg(TB.face + bvtt_b(c));
+        hit = tri_intersect_exact(load_vertex(TA.xyz, fa.x), load_vertex(TA.xyz, fa.y), load_vertex(TA.xyz, fa.z),
+                                  load_vertex(TB.xyz, fb.x), load_vertex(TB.xyz, fb.y), load_vertex(TB.xyz, fb.z));
+        rec = make_uint4(pv.a, pv.b, fa.w, fb.w);
+    }
+    const uint32_t pos = warp_append(a.counts + kCountHits, hit, lane);
+    if (hit) {
+        if (pos < a.hit_cap) a.hits[pos] = rec;
+        else atomicOr(a.counts + kCountFlags, (uint32_t)kFlagHitOverflow);
+    }
+}
+
+// Queue (or, in broad-only mode, store) one candidate per lane where `pred`.
+__device__ __forceinline__ void push_candidate(const DetectArgs& a, WarpCands& wc, bool pred, uint64_t cval,
+                                               uint32_t lane)
+{
+    const uint32_t mask = __ballot_sync(0xffffffffu, pred);
+    if (mask == 0) return;
+    if (lane == 0) atomicAdd(a.counts + kCountCands, (uint32_t)__popc(mask));
+    if (!a.fuse_narrow) {
+        // broad phase only: candidates go to the global queue
+        uint32_t base = 0;
+        const int leader = __ffs(mask) - 1;
+        if ((int)lane == leader) base = atomicAdd(a.counts + kCountCandSlots, (uint32_t)__popc(mask));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (pred) {
+            const uint32_t pos = base + __popc(mask & ((1u << lane) - 1u));
+            if (pos < a.cand_cap) a.cand[pos] = cval;
+            else atomicOr(a.counts + kCountFlags, (uint32_t)kFlagCandOverflow);
         }
-        // next front: warp inclusive scan of the child counts
-        const uint32_t nch = ncA * ncB;
-        uint32_t incl = nch;
-#pragma unroll
-        for (int s = 1; s < 32; s <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, s);
-            if ((int)lane >= s) incl += y;
-        }
-        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-        if (total) {
-            uint32_t wbase = 0;
-            if (lane == 31) wbase = atomicAdd(dst_count, total);
-            wbase = __shfl_sync(0xffffffffu, wbase, 31);
-            uint32_t pos = wbase + incl - nch;
-            bool overflow = false;
-            for (uint32_t x = 0; x < ncA; ++x)
-                for (uint32_t y = 0; y < ncB; ++y, ++pos) {
-                    if (pos < a.front_cap) dst[pos] = bvtt_pack(pair, firstA + x, firstB + y);
-                    else overflow = true;
-                }
-            if (overflow) atomicOr(a.counts + 1, (uint32_t)kFlagFrontOverflow);
+        return;
+    }
+    if (pred) wc.buf[wc.n + __popc(mask & ((1u << lane) - 1u))] = cval;
+    wc.n += __popc(mask);
+    __syncwarp();
+    if (wc.n >= 32) {
+        test_candidates(a, wc.buf + wc.n - 32, 32, lane);
+        wc.n -= 32;
+        __syncwarp();
+    }
+}
+
+// One BVTT pair: expand both sides `e` levels (clamped at the leaves), test
+// every child pair and queue the overlapping ones (or pass them on as
+// candidates when both children are leaves). All lanes of the warp run the
+// loops together; `valid` lanes contribute.
+__device__ __forceinline__ void expand_pair(const DetectArgs& a, WarpCands& wc, bool valid, uint64_t node,
+                                            uint64_t* __restrict__ dst, uint32_t* dst_count, uint32_t lane)
+{
+    uint32_t pair = 0, firstA = 0, firstB = 0, ncA = 0, ncB = 0, LA = 0, LB = 0, lca = 0, lcb = 0;
+    const TreeView* TA = nullptr;
+    const TreeView* TB = nullptr;
+    if (valid) {
+        pair = bvtt_pair(node);
+        const uint32_t ia = bvtt_a(node), ib = bvtt_b(node);
+        const PairView pv = a.pairs[pair];
+        TA = a.trees + pv.a;
+        TB = a.trees + pv.b;
+        const TreeShape SA = TA->shape, SB = TB->shape;
+        LA = SA.L;
+        LB = SB.L;
+        const uint32_t la = ilog2(ia + 1u), lb = ilog2(ib + 1u);
+        expand_side(SA, ia, la, a.expand_levels, firstA, ncA);
+        expand_side(SB, ib, lb, a.expand_levels, firstB, ncB);
+        lca = ilog2(firstA + 1u);
+        lcb = ilog2(firstB + 1u);
+    }
+    const uint32_t maxA = __reduce_max_sync(0xffffffffu, ncA);
+    const uint32_t maxB = __reduce_max_sync(0xffffffffu, ncB);
+    const uint32_t tested = __reduce_add_sync(0xffffffffu, ncA * ncB);
+    if (lane == 0 && tested) atomicAdd(a.counts + kCountTested, tested);
+    for (uint32_t x = 0; x < maxA; ++x) {
+        Box ba{};
+        const bool va = x < ncA;
+        if (va) ba = node_box(*TA, firstA + x, lca);
+        for (uint32_t y = 0; y < maxB; ++y) {
+            bool ov = false;
+            if (va && y < ncB) ov = overlap(ba, node_box(*TB, firstB + y, lcb));
+            const bool leafpair = ov && lca == LA && lcb == LB;
+            const bool push = ov && !leafpair;
+            const uint64_t child = bvtt_pack(pair, firstA + x, firstB + y);
+            push_candidate(a, wc, leafpair,
+                           bvtt_pack(pair, firstA + x - ((1u << LA) - 1u), firstB + y - ((1u << LB) - 1u)), lane);
+            const uint32_t pos = warp_append(dst_count, push, lane);
+            if (push) {
+                if (pos < a.front_cap) dst[pos] = child;
+                else atomicOr(a.counts + kCountFlags, (uint32_t)kFlagFrontOverflow);
+            }
         }
     }
 }
 
+// The whole broad phase (and, fused, the narrow phase) in one cooperative
+// launch: level-synchronous BVTT front in HBM, one grid barrier per level.
+//   step 0: the initial front, every entry-level node pair of every mesh
+//           pair (Scene::expandBvttNodes), is tested; overlapping pairs are
+//           queued;
+//   step k: every queued pair is expanded, its child pairs tested, the
+//           overlapping ones queued for step k+1 (leaf pairs go to the
+//           candidate buffers).
+// A pair is queued only after its own boxes overlapped, so the front holds
+// exactly the overlapping BVTT nodes of each level.
+__global__ void __launch_bounds__(kDetectThreads) k_traverse(DetectArgs a, uint32_t total0)
+{
+    __shared__ uint64_t s_cand[kDetectThreads / 32][kCandBuf];
+    __shared__ uint32_t s_ok;
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+    uint32_t* bar = a.counts + kCountBarrier;
+    WarpCands wc{s_cand[wib], 0};
+
+    // step 0: initial front (test, queue the overlapping pairs)
+    for (uint32_t base = warp * 32; base < total0; base += n_warps * 32) {
+        const uint32_t i = base + lane;
+        bool ov = false, leafpair = false;
+        uint64_t node = 0, cval = 0;
+        if (i < total0) {
+            uint32_t lo = 0, hi = a.n_pairs - 1;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1) >> 1;
+                if (a.pairs[mid].front_off <= i) lo = mid;
+                else hi = mid - 1;
+            }
+            const PairView pv = a.pairs[lo];
+            const uint32_t k = i - pv.front_off;
+            const uint32_t x = k / pv.front_cnt_b, y = k - x * pv.front_cnt_b;
+            const uint32_t ia = (1u << pv.entry_a) - 1u + x, ib = (1u << pv.entry_b) - 1u + y;
+            const TreeView& TA = a.trees[pv.a];
+            const TreeView& TB = a.trees[pv.b];
+            ov = overlap(node_box(TA, ia, pv.entry_a), node_box(TB, ib, pv.entry_b));
+            leafpair = ov && pv.entry_a == TA.shape.L && pv.entry_b == TB.shape.L;
+            node = bvtt_pack(lo, ia, ib);
+            cval = bvtt_pack(lo, x, y);
+        }
+        push_candidate(a, wc, leafpair, cval, lane);
+        const bool push = ov && !leafpair;
+        const uint32_t pos = warp_append(a.counts + kCountFront0, push, lane);
+        if (push) {
+            if (pos < a.front_cap) a.front[0][pos] = node;
+            else atomicOr(a.counts + kCountFlags, (uint32_t)kFlagFrontOverflow);
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.counts + kCountTested, total0);
+
+    for (uint32_t it = 0; it < a.iters; ++it) {
+        if (!grid_barrier(bar, a.counts + kCountFlags, gridDim.x, &s_ok)) return;
+        const uint32_t n = min(*(volatile uint32_t*)(a.counts + kCountFront0 + it), a.front_cap);
+        if (n == 0) break;
+        const uint64_t* __restrict__ src = (it & 1) ? a.front[1] : a.front[0];
+        uint64_t* __restrict__ dst = (it & 1) ? a.front[0] : a.front[1];
+        for (uint32_t base = warp * 32; base < n; base += n_warps * 32) {
+            const uint32_t i = base + lane;
+            const bool valid = i < n;
+            const uint64_t node = valid ? __ldcg(src + i) : 0ull;
+            expand_pair(a, wc, valid, node, dst, a.counts + kCountFront0 + it + 1, lane);
+        }
+    }
+    // flush the partial candidate buffers
+    if (a.fuse_narrow && wc.n > 0) test_candidates(a, wc.buf, wc.n, lane);
+}
+
 __global__ void __launch_bounds__(kDetectThreads) k_narrow(DetectArgs a)
 {
-    const uint32_t n = min(a.counts[2], a.cand_cap);
+    const uint32_t n = min(a.counts[kCountCandSlots], a.cand_cap);
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
@@ -239,29 +371,26 @@ __global__ void __launch_bounds__(kDetectThreads) k_narrow(DetectArgs a)
                                       load_vertex(xb, fb.x), load_vertex(xb, fb.y), load_vertex(xb, fb.z));
             rec = make_uint4(pv.a, pv.b, fa.w, fb.w);
         }
-        const uint32_t pos = warp_append(a.counts + 0, hit, lane);
+        const uint32_t pos = warp_append(a.counts + kCountHits, hit, lane);
         if (hit) {
             if (pos < a.hit_cap) a.hits[pos] = rec;
-            else atomicOr(a.counts + 1, (uint32_t)kFlagHitOverflow);
+            else atomicOr(a.counts + kCountFlags, (uint32_t)kFlagHitOverflow);
         }
     }
 }
 
-cudaError_t launch_init_front(const DetectArgs& a, uint32_t total, cudaStream_t s)
+cudaError_t launch_traverse(const DetectArgs& a, uint32_t total0, cudaStream_t s)
 {
-    uint32_t blocks = (total + kDetectThreads - 1) / kDetectThreads;
-    if (blocks > (uint32_t)a.grid) blocks = (uint32_t)a.grid;
-    if (blocks == 0) blocks = 1;
+    void* args[] = {(void*)&a, (void*)&total0};
     note_launches(1);
-    k_init_front<<<blocks, kDetectThreads, 0, s>>>(a, total);
-    return cudaGetLastError();
+    return cudaLaunchCooperativeKernel((const void*)k_traverse, dim3(a.grid), dim3(kDetectThreads), args, 0, s);
 }
 
-cudaError_t launch_bvtt_step(const DetectArgs& a, uint32_t it, cudaStream_t s)
+int traverse_blocks_per_sm()
 {
-    note_launches(1);
-    k_bvtt_step<<<a.grid, kDetectThreads, 0, s>>>(a, it);
-    return cudaGetLastError();
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_traverse, kDetectThreads, 0) != cudaSuccess) return 1;
+    return n > 0 ? n : 1;
 }
 
 cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s)

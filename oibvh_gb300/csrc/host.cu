@@ -185,7 +185,7 @@ struct oibvh_tree_s {
     const float* cur_xyz = nullptr;  // positions of the last build/refit
     DevBuf<uint32_t> tri;       // faces as given (3 * nT)
     DevBuf<uint4> face;         // Morton-ordered faces (v0, v1, v2, original index)
-    DevBuf<float4> box;         // 2 * size
+    DevBuf<float4> box;         // 2 * (size - nT): internal nodes only
     DevBuf<uint32_t> counters;  // refit climbing counters
     bool built = false;
 
@@ -208,7 +208,7 @@ static int tree_alloc(oibvh_tree_t t)
     OK_TRY(t->xyz.ensure(3 * (size_t)t->nV, "cudaMalloc(positions)"));
     OK_TRY(t->tri.ensure(3 * (size_t)t->nT, "cudaMalloc(faces)"));
     OK_TRY(t->face.ensure(t->nT, "cudaMalloc(sorted faces)"));
-    OK_TRY(t->box.ensure(2 * (size_t)t->shape.size, "cudaMalloc(tree)"));
+    OK_TRY(t->box.ensure(2 * (size_t)std::max(1u, t->shape.size - t->nT), "cudaMalloc(tree)"));
     OK_TRY(t->counters.ensure(refit_counters_per_tree(), "cudaMalloc(counters)"));
     return OIBVH_OK;
 }
@@ -298,6 +298,13 @@ struct oibvh_scene_s {
     uint32_t cand_cap = 1u << 20;
     uint32_t hit_cap = 1u << 18;
 
+    // multi-tree refit: job table as last uploaded
+    DevBuf<RefitJob> refit_jobs;
+    DevBuf<uint32_t> refit_counters;
+    PinnedBuf<RefitJob> h_refit_jobs;
+    std::vector<RefitJob> refit_cache;
+    uint32_t refit_blocks = 0;
+
     uint64_t hit_count = 0;
     uint64_t cand_count = 0;
     bool cands_valid = false;    // candidates of a single pass are on the device
@@ -332,7 +339,7 @@ int plan_pass(const oibvh_scene_s* s, const uint32_t* pr, uint32_t n, uint32_t e
 {
     plan.pv.resize(n);
     plan.front0 = 0;
-    plan.iters = 1;
+    plan.iters = 0;
     for (uint32_t p = 0; p < n; ++p) {
         const TreeShape& A = s->trees[pr[2 * p]]->shape;
         const TreeShape& B = s->trees[pr[2 * p + 1]]->shape;
@@ -347,7 +354,7 @@ int plan_pass(const oibvh_scene_s* s, const uint32_t* pr, uint32_t n, uint32_t e
         v.front_off = (uint32_t)plan.front0;
         plan.front0 += (uint64_t)v.front_cnt_a * v.front_cnt_b;
         const uint32_t depth = std::max(A.L - v.entry_a, B.L - v.entry_b);
-        const uint32_t it = (depth + expand - 1) / expand + 1;
+        const uint32_t it = (depth + expand - 1) / expand;  // expansion steps after the initial front
         plan.iters = std::max(plan.iters, it);
         plan.pv[p] = v;
     }
@@ -407,7 +414,7 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
     OK_TRY(upload_views(s, st));
     OK_TRY(s->hits.ensure(s->hit_cap, "cudaMalloc(hits)"));
 
-    const int grid = sm_count(s->device) * 8;
+    const int grid = sm_count(s->device) * std::min(4, traverse_blocks_per_sm());
     for (uint32_t p0 = 0; p0 < n_pairs; p0 += kMaxPairsPerPass) {
         const uint32_t np = std::min(kMaxPairsPerPass, n_pairs - p0);
         PassPlan plan;
@@ -423,37 +430,38 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
         const uint64_t hits_before = s->hit_count;
         for (int attempt = 0;; ++attempt) {
             if (attempt > 12) return fail(OIBVH_ERR_OVERFLOW, "BVTT queues kept overflowing after regrowing");
-            if (plan.front0 > s->front_cap) s->front_cap = grow_cap(plan.front0, s->front_cap);
             OK_TRY(s->front0.ensure(s->front_cap, "cudaMalloc(front)"));
             OK_TRY(s->front1.ensure(s->front_cap, "cudaMalloc(front)"));
-            OK_TRY(s->cand.ensure(s->cand_cap, "cudaMalloc(candidates)"));
+            if (!narrow) OK_TRY(s->cand.ensure(s->cand_cap, "cudaMalloc(candidates)"));
             CUDA_TRY(cudaMemsetAsync(s->counts.p, 0, n_counts * sizeof(uint32_t), st));
-            s->h_counts.p[0] = (uint32_t)hits_before;
-            CUDA_TRY(cudaMemcpyAsync(s->counts.p, s->h_counts.p, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+            if (hits_before) {
+                s->h_counts.p[0] = (uint32_t)hits_before;
+                CUDA_TRY(cudaMemcpyAsync(s->counts.p, s->h_counts.p, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+            }
             DetectArgs a{};
             a.trees = s->views.p;
             a.pairs = s->pairv.p;
             a.n_pairs = np;
-            a.expand_levels = expand;
+            a.expand_levels = std::min(expand, 3u);
             a.front[0] = s->front0.p;
             a.front[1] = s->front1.p;
             a.front_cap = s->front_cap;
-            a.cand = s->cand.p;
-            a.cand_cap = s->cand_cap;
+            a.cand = narrow ? nullptr : s->cand.p;
+            a.cand_cap = narrow ? 0 : s->cand_cap;
             a.hits = s->hits.p;
             a.hit_cap = s->hit_cap;
             a.counts = s->counts.p;
             a.iters = plan.iters;
+            a.fuse_narrow = narrow ? 1u : 0u;
             a.grid = grid;
-            CUDA_TRY(launch_init_front(a, (uint32_t)plan.front0, st));
-            for (uint32_t it = 0; it < plan.iters; ++it) CUDA_TRY(launch_bvtt_step(a, it, st));
-            if (narrow) CUDA_TRY(launch_narrow(a, st));
+            CUDA_TRY(launch_traverse(a, (uint32_t)plan.front0, st));
             CUDA_TRY(cudaMemcpyAsync(s->h_counts.p, s->counts.p, n_counts * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                                      st));
             CUDA_TRY(cudaStreamSynchronize(st));
             const uint32_t* c = s->h_counts.p;
             const uint32_t flags = c[kCountFlags];
-            if (c[kCountFront0 + plan.iters] != 0)
+            if (flags & kFlagTimeout) return fail(OIBVH_ERR_TIMEOUT, "traversal grid barrier timed out");
+            if (!(flags & kFlagFrontOverflow) && c[kCountFront0 + plan.iters] != 0)
                 return fail(OIBVH_ERR_STATE, "internal: BVTT front not empty after the last level");
             if (flags) {
                 s->stats.retries++;
@@ -462,7 +470,7 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
                     for (uint32_t k = 0; k <= plan.iters; ++k) peak = std::max<uint64_t>(peak, c[kCountFront0 + k]);
                     s->front_cap = grow_cap(peak, s->front_cap);
                 }
-                if (flags & kFlagCandOverflow) s->cand_cap = grow_cap(c[kCountCands], s->cand_cap);
+                if (flags & kFlagCandOverflow) s->cand_cap = grow_cap(c[kCountCandSlots], s->cand_cap);
                 if (flags & kFlagHitOverflow) {
                     const uint32_t want = grow_cap(c[kCountHits], s->hit_cap);
                     OK_TRY(s->hits.grow_keep(want, hits_before, st, "cudaMalloc(hits)"));
@@ -470,14 +478,11 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
                 }
                 continue;
             }
-            uint64_t nodes = 0, peak = 0;
-            for (uint32_t k = 0; k < plan.iters; ++k) {
-                nodes += c[kCountFront0 + k];
-                peak = std::max<uint64_t>(peak, c[kCountFront0 + k]);
-            }
-            s->stats.nodes_tested += nodes;
+            uint64_t peak = 0;
+            for (uint32_t k = 0; k <= plan.iters; ++k) peak = std::max<uint64_t>(peak, c[kCountFront0 + k]);
+            s->stats.nodes_tested += c[kCountTested];
             s->stats.front_peak = std::max(s->stats.front_peak, peak);
-            s->stats.steps = plan.iters;
+            s->stats.steps = plan.iters + 1;
             s->cand_count += c[kCountCands];
             if (narrow) s->hit_count = c[kCountHits];
             break;
@@ -502,7 +507,7 @@ int narrow_impl(oibvh_scene_s* s, cudaStream_t st)
     const uint32_t np = (uint32_t)s->last_pairs.size();
     for (int attempt = 0;; ++attempt) {
         if (attempt > 12) return fail(OIBVH_ERR_OVERFLOW, "hit queue kept overflowing");
-        // counts[2] still holds the candidate count of the broad phase
+        // counts[kCountCandSlots] still holds the candidate count of the broad phase
         uint32_t z[2] = {0, 0};
         std::memcpy(s->h_counts.p, z, sizeof(z));
         CUDA_TRY(cudaMemcpyAsync(s->counts.p, s->h_counts.p, 2 * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
@@ -516,8 +521,10 @@ int narrow_impl(oibvh_scene_s* s, cudaStream_t st)
         a.hit_cap = s->hit_cap;
         a.counts = s->counts.p;
         a.grid = sm_count(s->device) * 8;
+        a.fuse_narrow = 1;
         CUDA_TRY(launch_narrow(a, st));
-        CUDA_TRY(cudaMemcpyAsync(s->h_counts.p, s->counts.p, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(s->h_counts.p, s->counts.p, kCountFront0 * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                 st));
         CUDA_TRY(cudaStreamSynchronize(st));
         if (s->h_counts.p[kCountFlags] & kFlagHitOverflow) {
             const uint32_t want = grow_cap(s->h_counts.p[kCountHits], s->hit_cap);
@@ -560,6 +567,7 @@ API const char* oibvh_status_string(int status)
     case OIBVH_ERR_OVERFLOW: return "queue overflow";
     case OIBVH_ERR_STATE: return "invalid state";
     case OIBVH_ERR_UNSUPPORTED: return "unsupported";
+    case OIBVH_ERR_TIMEOUT: return "device wait timed out";
     default: return "unknown status";
     }
 }
@@ -600,7 +608,8 @@ API int oibvh_tree_create_copy(oibvh_tree_t other, const float* xyz, uint32_t n_
         if (e == cudaSuccess)
             e = cudaMemcpy(t->face.p, other->face.p, (size_t)t->nT * sizeof(uint4), cudaMemcpyDeviceToDevice);
         if (e == cudaSuccess)
-            e = cudaMemcpy(t->box.p, other->box.p, 2 * (size_t)t->shape.size * sizeof(float4), cudaMemcpyDeviceToDevice);
+            e = cudaMemcpy(t->box.p, other->box.p, 2 * (size_t)(t->shape.size - t->nT) * sizeof(float4),
+                           cudaMemcpyDeviceToDevice);
         if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpy(copy tree)");
     }
     if (st != OIBVH_OK) {
@@ -652,6 +661,32 @@ API int oibvh_tree_refit_device(oibvh_tree_t t, const float* d_xyz, void* stream
     GUARD_END
 }
 
+API int oibvh_tree_set_positions(oibvh_tree_t t, const float* xyz, void* stream)
+{
+    GUARD_BEGIN
+    if (!t || !xyz) return fail(OIBVH_ERR_ARG, "tree or xyz is NULL");
+    DeviceGuard g(t->device);
+    CUDA_TRY(cudaMemcpyAsync(t->xyz.p, xyz, 3 * (size_t)t->nV * sizeof(float), cudaMemcpyHostToDevice,
+                             (cudaStream_t)stream));
+    t->cur_xyz = t->xyz.p;
+    return OIBVH_OK;
+    GUARD_END
+}
+
+API int oibvh_tree_set_positions_device(oibvh_tree_t t, const float* d_xyz)
+{
+    GUARD_BEGIN
+    if (!t || !d_xyz) return fail(OIBVH_ERR_ARG, "tree or d_xyz is NULL");
+    DeviceGuard g(t->device);
+    cudaPointerAttributes attr{};
+    CUDA_TRY(cudaPointerGetAttributes(&attr, d_xyz));
+    if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
+        return fail(OIBVH_ERR_ARG, "d_xyz is not device memory");
+    t->cur_xyz = d_xyz;
+    return OIBVH_OK;
+    GUARD_END
+}
+
 API uint32_t oibvh_tree_get_depth(oibvh_tree_t t) { return t ? ilog2(t->shape.size) : 0; }
 API uint32_t oibvh_tree_get_prim_count(oibvh_tree_t t) { return t ? t->nT : 0; }
 API uint32_t oibvh_tree_get_size(oibvh_tree_t t) { return t ? t->shape.size : 0; }
@@ -662,10 +697,20 @@ API int oibvh_tree_get_aabbs(oibvh_tree_t t, float* out6, uint64_t cap_nodes)
     if (!t || !out6) return fail(OIBVH_ERR_ARG, "tree or out6 is NULL");
     if (!t->built) return fail(OIBVH_ERR_STATE, "tree not built");
     DeviceGuard g(t->device);
+    const size_t internal = t->shape.size - t->nT;
     const size_t n = std::min<uint64_t>(cap_nodes, t->shape.size);
-    std::vector<float4> tmp(2 * n);
+    std::vector<float4> tmp(2 * (size_t)t->shape.size);
     CUDA_TRY(cudaDeviceSynchronize());
-    CUDA_TRY(cudaMemcpy(tmp.data(), t->box.p, 2 * n * sizeof(float4), cudaMemcpyDeviceToHost));
+    if (internal)
+        CUDA_TRY(cudaMemcpy(tmp.data(), t->box.p, 2 * internal * sizeof(float4), cudaMemcpyDeviceToHost));
+    {
+        // leaves are not stored: rebuild them from the faces and positions
+        DevBuf<float4> leaves;
+        OK_TRY(leaves.ensure(2 * (size_t)t->nT, "cudaMalloc(leaf boxes)"));
+        CUDA_TRY(launch_leaf_boxes(t->face.p, t->cur_xyz, t->nT, leaves.p, 0));
+        CUDA_TRY(cudaMemcpy(tmp.data() + 2 * internal, leaves.p, 2 * (size_t)t->nT * sizeof(float4),
+                            cudaMemcpyDeviceToHost));
+    }
     for (size_t i = 0; i < n; ++i) {
         out6[6 * i + 0] = tmp[2 * i].x;
         out6[6 * i + 1] = tmp[2 * i].y;
@@ -777,6 +822,44 @@ API int oibvh_scene_narrow(oibvh_scene_t s, void* stream)
     GUARD_BEGIN
     if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
     return narrow_impl(s, (cudaStream_t)stream);
+    GUARD_END
+}
+
+API int oibvh_scene_refit(oibvh_scene_t s, void* stream)
+{
+    GUARD_BEGIN
+    if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
+    DeviceGuard g(s->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t n = s->trees.size();
+    if (n == 0) return OIBVH_OK;
+    std::vector<RefitJob> jobs(n);
+    uint32_t blocks = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const oibvh_tree_t t = s->trees[i];
+        if (!t->built) return fail(OIBVH_ERR_STATE, "every tree must be built before refit");
+        RefitJob j = t->job();
+        j.block_begin = blocks;
+        j.counters = nullptr;  // filled below
+        blocks += j.n_blocks;
+        jobs[i] = j;
+    }
+    const size_t per = refit_counters_per_tree();
+    OK_TRY(s->refit_counters.ensure(per * n, "cudaMalloc(refit counters)"));
+    for (size_t i = 0; i < n; ++i) jobs[i].counters = s->refit_counters.p + per * i;
+    bool same = s->refit_cache.size() == n && s->refit_jobs.p;
+    for (size_t i = 0; same && i < n; ++i) same = std::memcmp(&jobs[i], &s->refit_cache[i], sizeof(RefitJob)) == 0;
+    if (!same) {
+        OK_TRY(s->refit_jobs.ensure(n, "cudaMalloc(refit jobs)"));
+        OK_TRY(s->h_refit_jobs.ensure(n, "cudaMallocHost(refit jobs)"));
+        CUDA_TRY(cudaStreamSynchronize(st));  // the staging buffer may feed an earlier copy
+        std::memcpy(s->h_refit_jobs.p, jobs.data(), n * sizeof(RefitJob));
+        CUDA_TRY(cudaMemcpyAsync(s->refit_jobs.p, s->h_refit_jobs.p, n * sizeof(RefitJob), cudaMemcpyHostToDevice, st));
+        s->refit_cache = jobs;
+    }
+    s->refit_blocks = blocks;
+    CUDA_TRY(launch_refit(s->refit_jobs.p, (uint32_t)n, blocks, s->refit_counters.p, per * n, st));
+    return OIBVH_OK;
     GUARD_END
 }
 

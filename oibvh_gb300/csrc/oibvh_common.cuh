@@ -8,8 +8,11 @@
 // l holds real(l) = 2^l - (vl >> (L-l)) = ceil(real(l+1)/2) nodes, node j of
 // level l merges children 2j and 2j+1 (the latter only when 2j+1 < real(l+1)).
 //
-// In HBM every node is 32 bytes: float4 (min.xyz, 0) then float4 (max.xyz, 0),
-// so a node is one aligned 32-byte sector and loads as two float4.
+// In HBM only the internal nodes (levels 0..L-1, the first size-T real nodes)
+// are stored, 32 bytes each: float4 (min.xyz, 0) then float4 (max.xyz, 0), so
+// a node is one aligned 32-byte sector and loads as two float4. A leaf's box
+// is rebuilt from its 16-byte face record (v0, v1, v2, original index) and
+// the three vertices when it is needed.
 #pragma once
 
 #include <cstdint>
@@ -103,7 +106,7 @@ struct TreeShape {
 
 // Device view of one tree.
 struct TreeView {
-    float4* box;        // 2*size float4: level-ordered real nodes
+    float4* box;        // 2*(size-nT) float4: level-ordered real internal nodes
     const uint4* face;  // Morton-sorted faces: (v0, v1, v2, original face index)
     const float* xyz;   // 3 floats per vertex
     TreeShape shape;
@@ -127,10 +130,53 @@ enum DeviceFlag : uint32_t {
     kFlagCandOverflow = 1u << 1,
     kFlagHitOverflow = 1u << 2,
     kFlagBadInput = 1u << 3,
+    kFlagTimeout = 1u << 4,
 };
 
 // glm::min / glm::max semantics (third/glm/detail/func_common.inl:17-29).
 __host__ __device__ __forceinline__ float gmin(float x, float y) { return (y < x) ? y : x; }
 __host__ __device__ __forceinline__ float gmax(float x, float y) { return (x < y) ? y : x; }
+
+// An axis-aligned box in registers: min xyz, max xyz.
+struct Box {
+    float nx, ny, nz, xx, xy, xz;
+};
+
+// merge_aabb (src/cuda/oibvh.cu:72-78): glm::min(left, right), glm::max(left, right)
+__device__ __forceinline__ Box merge(const Box& l, const Box& r)
+{
+    return Box{gmin(l.nx, r.nx), gmin(l.ny, r.ny), gmin(l.nz, r.nz),
+               gmax(l.xx, r.xx), gmax(l.xy, r.xy), gmax(l.xz, r.xz)};
+}
+
+// Box of one face (v0, v1, v2, .): glm::min(glm::min(v0, v1), v2) and the
+// max likewise, as calculate_aabb_kernel (src/cuda/oibvh.cu:24-40).
+__device__ __forceinline__ Box leaf_box(const float* __restrict__ xyz, uint4 f)
+{
+    const float ax = __ldg(xyz + 3 * (size_t)f.x), ay = __ldg(xyz + 3 * (size_t)f.x + 1),
+                az = __ldg(xyz + 3 * (size_t)f.x + 2);
+    const float bx = __ldg(xyz + 3 * (size_t)f.y), by = __ldg(xyz + 3 * (size_t)f.y + 1),
+                bz = __ldg(xyz + 3 * (size_t)f.y + 2);
+    const float cx = __ldg(xyz + 3 * (size_t)f.z), cy = __ldg(xyz + 3 * (size_t)f.z + 1),
+                cz = __ldg(xyz + 3 * (size_t)f.z + 2);
+    return Box{gmin(gmin(ax, bx), cx), gmin(gmin(ay, by), cy), gmin(gmin(az, bz), cz),
+               gmax(gmax(ax, bx), cx), gmax(gmax(ay, by), cy), gmax(gmax(az, bz), cz)};
+}
+
+// Box of a node given by implicit index and level: internal nodes are read
+// from the tree (32 B, two float4), leaves are rebuilt from their face.
+__device__ __forceinline__ Box node_box(const TreeView& T, uint32_t implicit, uint32_t level)
+{
+    if (level == T.shape.L) return leaf_box(T.xyz, __ldg(T.face + implicit - ((1u << level) - 1u)));
+    const float4* p = T.box + 2 * (size_t)T.shape.real_index(implicit);
+    const float4 a = __ldg(p), b = __ldg(p + 1);
+    return Box{a.x, a.y, a.z, b.x, b.y, b.z};
+}
+
+// aabb_box_t::overlap (include/utils/utils.h:39-44; src/cuda/collide.cu:12-17)
+__device__ __forceinline__ bool overlap(const Box& a, const Box& b)
+{
+    return (a.nx <= b.xx && a.xx >= b.nx) && (a.ny <= b.xy && a.xy >= b.ny) && (a.nz <= b.xz && a.xz >= b.nz);
+}
 
 } // namespace oibvh

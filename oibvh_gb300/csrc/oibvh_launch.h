@@ -14,7 +14,7 @@ void note_launches(uint64_t n);
 
 // One tree of a (possibly multi-tree) refit launch.
 struct RefitJob {
-    float4* box;
+    float4* box;           // internal nodes
     const uint4* face;
     const float* xyz;
     TreeShape shape;
@@ -37,6 +37,7 @@ cudaError_t launch_gather_faces(const uint32_t* tri, const uint32_t* perm, uint3
 uint32_t refit_blocks_for(uint32_t nT);
 uint32_t refit_counters_per_tree();
 cudaError_t launch_refit_one(const RefitJob& job, cudaStream_t s);
+cudaError_t launch_leaf_boxes(const uint4* face, const float* xyz, uint32_t nT, float4* out, cudaStream_t s);
 cudaError_t launch_refit(const RefitJob* d_jobs, uint32_t n_jobs, uint32_t total_blocks, uint32_t* d_counters,
                          size_t n_counters, cudaStream_t s);
 
@@ -52,14 +53,18 @@ struct DetectArgs {
     uint32_t cand_cap;
     uint4* hits;
     uint32_t hit_cap;
-    uint32_t* counts;  // [0] hits, [1] flags, [2] candidates, [3 + it] front size entering step it
-    uint32_t iters;
-    int grid;          // CTAs for the grid-stride kernels
+    uint32_t* counts;  // see kCount* below
+    uint32_t iters;    // BVTT steps after the initial front
+    uint32_t fuse_narrow;  // 1: test candidates in the traversal; 0: store them
+    int grid;          // CTAs (cooperative: all co-resident)
 };
-cudaError_t launch_init_front(const DetectArgs& a, uint32_t total, cudaStream_t s);
-cudaError_t launch_bvtt_step(const DetectArgs& a, uint32_t it, cudaStream_t s);
+cudaError_t launch_traverse(const DetectArgs& a, uint32_t total0, cudaStream_t s);
+int traverse_blocks_per_sm();
 cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s);
 
-constexpr uint32_t kCountHits = 0, kCountFlags = 1, kCountCands = 2, kCountFront0 = 3;
+// counts[]: hits, flags, candidates found, candidate slots used (broad-only),
+// nodes tested, grid barrier (2 words), then the front size entering each step.
+constexpr uint32_t kCountHits = 0, kCountFlags = 1, kCountCands = 2, kCountCandSlots = 3, kCountTested = 4,
+                   kCountBarrier = 5, kCountFront0 = 7;
 
 } // namespace oibvh
