@@ -130,7 +130,7 @@ __device__ __forceinline__ void expand_side(const TreeShape& S, uint32_t ia, uin
 // kSpinLimit polls the CTA raises kFlagTimeout and reports failure, and the
 // kernel returns.
 // ---------------------------------------------------------------------------
-constexpr uint32_t kSpinLimit = 1u << 22;  // x ~100 ns per poll: well under a second
+constexpr uint32_t kSpinLimit = 1u << 24;  // polls; with 32 ns sleeps after the first 2048, about a second
 
 __device__ __forceinline__ bool grid_barrier(uint32_t* bar, uint32_t* flags, uint32_t n_blocks, uint32_t* s_ok)
 {
@@ -153,7 +153,7 @@ __device__ __forceinline__ bool grid_barrier(uint32_t* bar, uint32_t* flags, uin
                     ok = 0;
                     break;
                 }
-                __nanosleep(64);
+                if (spins > 2048) __nanosleep(32);
             }
         }
         __threadfence();
@@ -168,7 +168,7 @@ __device__ __forceinline__ bool grid_barrier(uint32_t* bar, uint32_t* flags, uin
 // shared memory and tested 32 at a time, one per lane, so the 17-axis test
 // runs at full SIMT width however sparse the candidates are.
 // ---------------------------------------------------------------------------
-constexpr int kCandBuf = 64;
+constexpr int kCandBuf = 64;  // <= 31 left over + 32 added per round
 
 struct WarpCands {
     uint64_t* buf;  // kCandBuf entries
@@ -228,54 +228,81 @@ __device__ __forceinline__ void push_candidate(const DetectArgs& a, WarpCands& w
     }
 }
 
-// One BVTT pair: expand both sides `e` levels (clamped at the leaves), test
-// every child pair and queue the overlapping ones (or pass them on as
-// candidates when both children are leaves). All lanes of the warp run the
-// loops together; `valid` lanes contribute.
+// One BVTT pair per lane, one level down on both sides (a leaf stays put):
+// all child boxes are loaded first (independent loads), the up to 4 child
+// pairs are tested, overlapping leaf pairs become candidates and the other
+// overlapping pairs are queued with one warp-aggregated append.
 __device__ __forceinline__ void expand_pair(const DetectArgs& a, WarpCands& wc, bool valid, uint64_t node,
                                             uint64_t* __restrict__ dst, uint32_t* dst_count, uint32_t lane)
 {
-    uint32_t pair = 0, firstA = 0, firstB = 0, ncA = 0, ncB = 0, LA = 0, LB = 0, lca = 0, lcb = 0;
-    const TreeView* TA = nullptr;
-    const TreeView* TB = nullptr;
+    uint32_t pair = 0, fa = 0, fb = 0, na = 0, nb = 0, lca = 0, lcb = 0, leaf_a = 0, leaf_b = 0;
+    bool leaves = false;
+    Box A0{}, A1{}, B0{}, B1{};
     if (valid) {
         pair = bvtt_pair(node);
         const uint32_t ia = bvtt_a(node), ib = bvtt_b(node);
         const PairView pv = a.pairs[pair];
-        TA = a.trees + pv.a;
-        TB = a.trees + pv.b;
-        const TreeShape SA = TA->shape, SB = TB->shape;
-        LA = SA.L;
-        LB = SB.L;
+        const TreeView& TA = a.trees[pv.a];
+        const TreeView& TB = a.trees[pv.b];
         const uint32_t la = ilog2(ia + 1u), lb = ilog2(ib + 1u);
-        expand_side(SA, ia, la, a.expand_levels, firstA, ncA);
-        expand_side(SB, ib, lb, a.expand_levels, firstB, ncB);
-        lca = ilog2(firstA + 1u);
-        lcb = ilog2(firstB + 1u);
+        expand_side(TA.shape, ia, la, 1, fa, na);
+        expand_side(TB.shape, ib, lb, 1, fb, nb);
+        lca = ilog2(fa + 1u);
+        lcb = ilog2(fb + 1u);
+        leaves = lca == TA.shape.L && lcb == TB.shape.L;
+        leaf_a = fa - ((1u << lca) - 1u);  // Morton-order leaf index when lca is the leaf level
+        leaf_b = fb - ((1u << lcb) - 1u);
+        A0 = node_box(TA, fa, lca);
+        if (na > 1) A1 = node_box(TA, fa + 1, lca);
+        B0 = node_box(TB, fb, lcb);
+        if (nb > 1) B1 = node_box(TB, fb + 1, lcb);
     }
-    const uint32_t maxA = __reduce_max_sync(0xffffffffu, ncA);
-    const uint32_t maxB = __reduce_max_sync(0xffffffffu, ncB);
-    const uint32_t tested = __reduce_add_sync(0xffffffffu, ncA * ncB);
+    // bit (2x + y): child pair (fa + x, fb + y) overlaps
+    uint32_t m = 0;
+    if (valid) {
+        m |= overlap(A0, B0) ? 1u : 0u;
+        if (nb > 1) m |= overlap(A0, B1) ? 2u : 0u;
+        if (na > 1) m |= overlap(A1, B0) ? 4u : 0u;
+        if (na > 1 && nb > 1) m |= overlap(A1, B1) ? 8u : 0u;
+    }
+    const uint32_t tested = __reduce_add_sync(0xffffffffu, na * nb);
     if (lane == 0 && tested) atomicAdd(a.counts + kCountTested, tested);
-    for (uint32_t x = 0; x < maxA; ++x) {
-        Box ba{};
-        const bool va = x < ncA;
-        if (va) ba = node_box(*TA, firstA + x, lca);
-        for (uint32_t y = 0; y < maxB; ++y) {
-            bool ov = false;
-            if (va && y < ncB) ov = overlap(ba, node_box(*TB, firstB + y, lcb));
-            const bool leafpair = ov && lca == LA && lcb == LB;
-            const bool push = ov && !leafpair;
-            const uint64_t child = bvtt_pack(pair, firstA + x, firstB + y);
-            push_candidate(a, wc, leafpair,
-                           bvtt_pack(pair, firstA + x - ((1u << LA) - 1u), firstB + y - ((1u << LB) - 1u)), lane);
-            const uint32_t pos = warp_append(dst_count, push, lane);
-            if (push) {
-                if (pos < a.front_cap) dst[pos] = child;
-                else atomicOr(a.counts + kCountFlags, (uint32_t)kFlagFrontOverflow);
-            }
+    // candidates, one bit per round (at most 4 rounds); every lane joins each round
+    uint32_t cm = leaves ? m : 0u;
+    while (__any_sync(0xffffffffu, cm != 0)) {
+        const bool pred = cm != 0;
+        uint64_t c = 0;
+        if (pred) {
+            const uint32_t k = __ffs(cm) - 1;
+            cm &= cm - 1;
+            c = bvtt_pack(pair, leaf_a + (k >> 1), leaf_b + (k & 1));
         }
+        push_candidate(a, wc, pred, c, lane);
     }
+    // queue the overlapping internal pairs: one atomic per warp
+    const uint32_t cnt = leaves ? 0u : (uint32_t)__popc(m);
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int s = 1; s < 32; s <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, s);
+        if ((int)lane >= s) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0) return;
+    uint32_t wbase = 0;
+    if (lane == 31) wbase = atomicAdd(dst_count, total);
+    wbase = __shfl_sync(0xffffffffu, wbase, 31);
+    uint32_t pos = wbase + incl - cnt;
+    bool overflow = false;
+    uint32_t mm = leaves ? 0u : m;
+    while (mm) {
+        const uint32_t k = __ffs(mm) - 1;
+        mm &= mm - 1;
+        if (pos < a.front_cap) dst[pos] = bvtt_pack(pair, fa + (k >> 1), fb + (k & 1));
+        else overflow = true;
+        ++pos;
+    }
+    if (overflow) atomicOr(a.counts + kCountFlags, (uint32_t)kFlagFrontOverflow);
 }
 
 // The whole broad phase (and, fused, the narrow phase) in one cooperative

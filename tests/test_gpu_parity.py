@@ -124,3 +124,27 @@ def test_deforming_s8_frames_vs_oracle(gpu):
         want, wc = p.detect()
         assert np.array_equal(res[f][0], sort_pairs(want)), f"frame {f}"
         assert res[f][1] == wc
+
+
+def test_scene_refit_one_launch_bit_exact(gpu):
+    """oibvh_scene_refit: every tree refit in one launch equals the oracle's refit."""
+    from oibvh_gb300 import DeviceType, OibvhTree, Scene
+
+    g = load_golden("three_bodies")
+    trees = [OibvhTree(m) for m in g["meshes"]]
+    for t in trees:
+        t.build()
+    sc = Scene()
+    for t in trees:
+        sc.addOibvhTree(t)
+    rng = np.random.default_rng(0)
+    moved = [(m.xyz + rng.normal(scale=1e-3, size=m.xyz.shape)).astype(np.float32) for m in g["meshes"]]
+    for t, x in zip(trees, moved):
+        t.set_positions(x)
+    sc.refit()
+    for t, x in zip(trees, moved):
+        st, _ = t.sorted_faces()
+        assert np.array_equal(t.aabb_tree().view(np.uint32), Port.oibvh_refit(x, st).view(np.uint32))
+    sc.detectCollision(DeviceType.GPU0, 4, 1)
+    want, wc = _oracle_pairs([type(g["meshes"][0])(x, m.tri) for x, m in zip(moved, g["meshes"])])
+    assert np.array_equal(sc.int_tri_pairs(), want) and sc.candidate_count() == wc
