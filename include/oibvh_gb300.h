@@ -133,11 +133,13 @@ int oibvh_scene_set_pairs(oibvh_scene_t s, const uint32_t* pairs, uint32_t n_pai
 /* Scene::detectCollision(deviceType, entryLevel, expandLevels)
  * (src/cuda/scene.cu:157-185,225-446): BVTT broad phase from the cross
  * product of the nodes at entry_level (clamped to each tree's leaf level),
- * each step expanding a pair expand_levels levels down on both sides
- * (1..16 accepted; steps deeper than 3 levels run as 3), with the triangle
- * test fused into the traversal. The pair set does not depend on
- * entry_level or expand_levels: they only shape the work. Blocking:
- * returns once the pair count is known. */
+ * with the triangle test fused into the traversal. The pair set does not
+ * depend on entry_level or expand_levels (they only shape the reference's
+ * work): entry_level sets the initial front as in the reference;
+ * expand_levels is validated (1..16) but this traversal always descends one
+ * level per step and tests each child pair before queueing it, which visits
+ * a subset of the pairs the reference visits. Blocking: returns once the
+ * pair count is known. */
 int oibvh_scene_detect(oibvh_scene_t s, int device_type, uint32_t entry_level, uint32_t expand_levels, void* stream);
 
 /* The two halves of detect (src/cuda/scene.cu:270-311 and :382-423):

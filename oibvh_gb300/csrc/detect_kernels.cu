@@ -6,9 +6,13 @@
 // triangle_intersect_kernel (src/cuda/collide.cu:248-299) with
 // triangleIntersection2 (third/gProximity/cuda_intersect_tritri.h:350-434).
 //
-// The broad phase is one persistent cooperative kernel (k_traverse) that
-// walks the BVTT front level by level with a bounded grid barrier between
-// levels, so the host enqueues one launch and reads counters back once.
+// The broad phase is two kernels: k_init_front tests the cross product of
+// the node pairs at a start level and lists the overlapping ones; in
+// k_traverse every CTA repeatedly takes a chunk of that list and walks it to
+// the leaves level by level with its front in shared memory, so no
+// grid-wide synchronisation is needed; a level that outgrows shared memory
+// spills to a list the next round (another launch) drains. The host enqueues
+// everything and reads counters back once.
 // Appends (next front, candidates, hits) are warp-aggregated: one atomicAdd
 // per warp, positions from ballot/shuffle prefix sums. The narrow phase is
 // fused: overlapping leaf pairs are buffered per warp in shared memory and
@@ -125,50 +129,13 @@ __device__ __forceinline__ void expand_side(const TreeShape& S, uint32_t ia, uin
 }
 
 // ---------------------------------------------------------------------------
-// Grid-wide barrier for the cooperative traversal. Co-residency of every CTA
-// is guaranteed by the cooperative launch; the wait is still bounded: after
-// kSpinLimit polls the CTA raises kFlagTimeout and reports failure, and the
-// kernel returns.
-// ---------------------------------------------------------------------------
-constexpr uint32_t kSpinLimit = 1u << 24;  // polls; with 32 ns sleeps after the first 2048, about a second
-
-__device__ __forceinline__ bool grid_barrier(uint32_t* bar, uint32_t* flags, uint32_t n_blocks, uint32_t* s_ok)
-{
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile uint32_t* vgen = bar + 1;
-        const uint32_t gen = *vgen;
-        __threadfence();
-        const uint32_t arrived = atomicAdd(bar, 1u);
-        uint32_t ok = 1;
-        if (arrived == n_blocks - 1) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            uint32_t spins = 0;
-            while (*vgen == gen) {
-                if (++spins > kSpinLimit) {
-                    atomicOr(flags, (uint32_t)kFlagTimeout);
-                    ok = 0;
-                    break;
-                }
-                if (spins > 2048) __nanosleep(32);
-            }
-        }
-        __threadfence();
-        *s_ok = ok;
-    }
-    __syncthreads();
-    return *s_ok != 0;
-}
-
-// ---------------------------------------------------------------------------
 // Per-warp candidate buffer: leaf pairs whose boxes overlap are queued in
 // shared memory and tested 32 at a time, one per lane, so the 17-axis test
 // runs at full SIMT width however sparse the candidates are.
 // ---------------------------------------------------------------------------
 constexpr int kCandBuf = 64;  // <= 31 left over + 32 added per round
+constexpr uint32_t kFrontCap = 2048;  // per-CTA front in shared memory, per level
+constexpr uint32_t kGrab = 64;        // work-list items a CTA takes at a time
 
 struct WarpCands {
     uint64_t* buf;  // kCandBuf entries
@@ -231,11 +198,14 @@ __device__ __forceinline__ void push_candidate(const DetectArgs& a, WarpCands& w
 // One BVTT pair per lane, one level down on both sides (a leaf stays put):
 // all child boxes are loaded first (independent loads), the up to 4 child
 // pairs are tested, overlapping leaf pairs become candidates and the other
-// overlapping pairs are queued with one warp-aggregated append.
-__device__ __forceinline__ void expand_pair(const DetectArgs& a, WarpCands& wc, bool valid, uint64_t node,
-                                            uint64_t* __restrict__ dst, uint32_t* dst_count, uint32_t lane)
+// overlapping pairs are appended to the next front in shared memory (one
+// shared atomic per warp); what does not fit goes to the global spill list.
+// Returns the number of child pairs tested (lane 0 only, else 0).
+__device__ __forceinline__ uint32_t expand_pair(const DetectArgs& a, WarpCands& wc, bool valid, uint64_t node,
+                                                uint64_t* next, uint32_t* next_cnt, uint64_t* __restrict__ spill,
+                                                uint32_t* spill_cnt, uint32_t lane)
 {
-    uint32_t pair = 0, fa = 0, fb = 0, na = 0, nb = 0, lca = 0, lcb = 0, leaf_a = 0, leaf_b = 0;
+    uint32_t pair = 0, fa = 0, fb = 0, na = 0, nb = 0, leaf_a = 0, leaf_b = 0;
     bool leaves = false;
     Box A0{}, A1{}, B0{}, B1{};
     if (valid) {
@@ -247,8 +217,7 @@ __device__ __forceinline__ void expand_pair(const DetectArgs& a, WarpCands& wc, 
         const uint32_t la = ilog2(ia + 1u), lb = ilog2(ib + 1u);
         expand_side(TA.shape, ia, la, 1, fa, na);
         expand_side(TB.shape, ib, lb, 1, fb, nb);
-        lca = ilog2(fa + 1u);
-        lcb = ilog2(fb + 1u);
+        const uint32_t lca = ilog2(fa + 1u), lcb = ilog2(fb + 1u);
         leaves = lca == TA.shape.L && lcb == TB.shape.L;
         leaf_a = fa - ((1u << lca) - 1u);  // Morton-order leaf index when lca is the leaf level
         leaf_b = fb - ((1u << lcb) - 1u);
@@ -266,7 +235,6 @@ __device__ __forceinline__ void expand_pair(const DetectArgs& a, WarpCands& wc, 
         if (na > 1 && nb > 1) m |= overlap(A1, B1) ? 8u : 0u;
     }
     const uint32_t tested = __reduce_add_sync(0xffffffffu, na * nb);
-    if (lane == 0 && tested) atomicAdd(a.counts + kCountTested, tested);
     // candidates, one bit per round (at most 4 rounds); every lane joins each round
     uint32_t cm = leaves ? m : 0u;
     while (__any_sync(0xffffffffu, cm != 0)) {
@@ -279,7 +247,7 @@ __device__ __forceinline__ void expand_pair(const DetectArgs& a, WarpCands& wc, 
         }
         push_candidate(a, wc, pred, c, lane);
     }
-    // queue the overlapping internal pairs: one atomic per warp
+    // the overlapping internal pairs: reserve slots for the whole warp at once
     const uint32_t cnt = leaves ? 0u : (uint32_t)__popc(m);
     uint32_t incl = cnt;
 #pragma unroll
@@ -288,44 +256,46 @@ __device__ __forceinline__ void expand_pair(const DetectArgs& a, WarpCands& wc, 
         if ((int)lane >= s) incl += y;
     }
     const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    if (total == 0) return;
-    uint32_t wbase = 0;
-    if (lane == 31) wbase = atomicAdd(dst_count, total);
+    if (total == 0) return lane == 0 ? tested : 0u;
+    uint32_t wbase = 0, sbase = 0;
+    if (lane == 31) {
+        wbase = atomicAdd(next_cnt, total);
+        const uint32_t fit = wbase >= kFrontCap ? 0u : min(total, kFrontCap - wbase);
+        if (total > fit) sbase = atomicAdd(spill_cnt, total - fit);
+    }
     wbase = __shfl_sync(0xffffffffu, wbase, 31);
+    sbase = __shfl_sync(0xffffffffu, sbase, 31);
+    const uint32_t spill_from = max(wbase, kFrontCap);  // first front position that spills
     uint32_t pos = wbase + incl - cnt;
     bool overflow = false;
     uint32_t mm = leaves ? 0u : m;
     while (mm) {
         const uint32_t k = __ffs(mm) - 1;
         mm &= mm - 1;
-        if (pos < a.front_cap) dst[pos] = bvtt_pack(pair, fa + (k >> 1), fb + (k & 1));
-        else overflow = true;
+        const uint64_t child = bvtt_pack(pair, fa + (k >> 1), fb + (k & 1));
+        if (pos < kFrontCap) next[pos] = child;
+        else {
+            const uint32_t sp = sbase + (pos - spill_from);
+            if (sp < a.work_cap) spill[sp] = child;
+            else overflow = true;
+        }
         ++pos;
     }
     if (overflow) atomicOr(a.counts + kCountFlags, (uint32_t)kFlagFrontOverflow);
+    return lane == 0 ? tested : 0u;
 }
 
-// The whole broad phase (and, fused, the narrow phase) in one cooperative
-// launch: level-synchronous BVTT front in HBM, one grid barrier per level.
-//   step 0: the initial front, every entry-level node pair of every mesh
-//           pair (Scene::expandBvttNodes), is tested; overlapping pairs are
-//           queued;
-//   step k: every queued pair is expanded, its child pairs tested, the
-//           overlapping ones queued for step k+1 (leaf pairs go to the
-//           candidate buffers).
-// A pair is queued only after its own boxes overlapped, so the front holds
-// exactly the overlapping BVTT nodes of each level.
-__global__ void __launch_bounds__(kDetectThreads) k_traverse(DetectArgs a, uint32_t total0)
+// Initial work list: every start-level node pair of every mesh pair (the
+// reference's Scene::expandBvttNodes cross product, src/cuda/scene.cu:192-223)
+// is tested here; overlapping internal pairs go to work list 0, overlapping
+// leaf pairs straight to the candidates.
+__global__ void __launch_bounds__(kDetectThreads) k_init_front(DetectArgs a, uint32_t total0)
 {
     __shared__ uint64_t s_cand[kDetectThreads / 32][kCandBuf];
-    __shared__ uint32_t s_ok;
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
-    uint32_t* bar = a.counts + kCountBarrier;
     WarpCands wc{s_cand[wib], 0};
-
-    // step 0: initial front (test, queue the overlapping pairs)
     for (uint32_t base = warp * 32; base < total0; base += n_warps * 32) {
         const uint32_t i = base + lane;
         bool ov = false, leafpair = false;
@@ -350,28 +320,63 @@ __global__ void __launch_bounds__(kDetectThreads) k_traverse(DetectArgs a, uint3
         }
         push_candidate(a, wc, leafpair, cval, lane);
         const bool push = ov && !leafpair;
-        const uint32_t pos = warp_append(a.counts + kCountFront0, push, lane);
+        const uint32_t pos = warp_append(a.counts + kCountWork0, push, lane);
         if (push) {
-            if (pos < a.front_cap) a.front[0][pos] = node;
+            if (pos < a.work_cap) a.work[0][pos] = node;
             else atomicOr(a.counts + kCountFlags, (uint32_t)kFlagFrontOverflow);
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.counts + kCountTested, total0);
+    if (a.fuse_narrow && wc.n > 0) test_candidates(a, wc.buf, wc.n, lane);
+}
 
-    for (uint32_t it = 0; it < a.iters; ++it) {
-        if (!grid_barrier(bar, a.counts + kCountFlags, gridDim.x, &s_ok)) return;
-        const uint32_t n = min(*(volatile uint32_t*)(a.counts + kCountFront0 + it), a.front_cap);
-        if (n == 0) break;
-        const uint64_t* __restrict__ src = (it & 1) ? a.front[1] : a.front[0];
-        uint64_t* __restrict__ dst = (it & 1) ? a.front[0] : a.front[1];
-        for (uint32_t base = warp * 32; base < n; base += n_warps * 32) {
-            const uint32_t i = base + lane;
-            const bool valid = i < n;
-            const uint64_t node = valid ? __ldcg(src + i) : 0ull;
-            expand_pair(a, wc, valid, node, dst, a.counts + kCountFront0 + it + 1, lane);
+// Traversal round `round`: CTAs take chunks of the round's work list and walk
+// each chunk down to the leaves level by level with the front in shared
+// memory (__syncthreads between levels only: no grid-wide wait). A level
+// that outgrows shared memory spills the excess to the next round's list.
+__global__ void __launch_bounds__(kDetectThreads) k_traverse(DetectArgs a, uint32_t round)
+{
+    __shared__ uint64_t s_front[2][kFrontCap];
+    __shared__ uint64_t s_cand[kDetectThreads / 32][kCandBuf];
+    __shared__ uint32_t s_cnt[2];
+    __shared__ uint32_t s_grab[2];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    constexpr uint32_t kWarps = kDetectThreads / 32;
+    WarpCands wc{s_cand[wib], 0};
+    const uint64_t* __restrict__ src = (round & 1) ? a.work[1] : a.work[0];
+    uint64_t* __restrict__ spill = (round & 1) ? a.work[0] : a.work[1];
+    uint32_t* spill_cnt = a.counts + kCountWork0 + round + 1;
+    const uint32_t n_src = min(*(volatile uint32_t*)(a.counts + kCountWork0 + round), a.work_cap);
+    uint32_t tested = 0;
+
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const uint32_t g = atomicAdd(a.counts + kCountHead0 + round, kGrab);
+            s_grab[0] = g;
+            s_grab[1] = g < n_src ? min(kGrab, n_src - g) : 0u;
         }
+        __syncthreads();
+        const uint32_t g0 = s_grab[0], gn = s_grab[1];
+        if (gn == 0) break;
+        for (uint32_t i = threadIdx.x; i < gn; i += kDetectThreads) s_front[0][i] = __ldcg(src + g0 + i);
+        uint32_t cur = 0, c = gn;
+        __syncthreads();
+        while (c > 0) {
+            if (threadIdx.x == 0) s_cnt[cur ^ 1] = 0;
+            __syncthreads();
+            for (uint32_t base = wib * 32; base < c; base += kWarps * 32) {
+                const uint32_t i = base + lane;
+                const bool valid = i < c;
+                const uint64_t node = valid ? s_front[cur][i] : 0ull;
+                tested += expand_pair(a, wc, valid, node, s_front[cur ^ 1], &s_cnt[cur ^ 1], spill, spill_cnt, lane);
+            }
+            __syncthreads();
+            c = min(s_cnt[cur ^ 1], kFrontCap);
+            cur ^= 1;
+        }
+        __syncthreads();  // s_grab is rewritten by the next grab
     }
-    // flush the partial candidate buffers
+    if (lane == 0 && tested) atomicAdd(a.counts + kCountTested, tested);
     if (a.fuse_narrow && wc.n > 0) test_candidates(a, wc.buf, wc.n, lane);
 }
 
@@ -406,11 +411,21 @@ __global__ void __launch_bounds__(kDetectThreads) k_narrow(DetectArgs a)
     }
 }
 
-cudaError_t launch_traverse(const DetectArgs& a, uint32_t total0, cudaStream_t s)
+cudaError_t launch_init_front(const DetectArgs& a, uint32_t total0, cudaStream_t s)
 {
-    void* args[] = {(void*)&a, (void*)&total0};
+    uint32_t blocks = (total0 + kDetectThreads - 1) / kDetectThreads;
+    if (blocks > (uint32_t)a.grid) blocks = (uint32_t)a.grid;
+    if (blocks == 0) blocks = 1;
     note_launches(1);
-    return cudaLaunchCooperativeKernel((const void*)k_traverse, dim3(a.grid), dim3(kDetectThreads), args, 0, s);
+    k_init_front<<<blocks, kDetectThreads, 0, s>>>(a, total0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_traverse(const DetectArgs& a, uint32_t round, cudaStream_t s)
+{
+    note_launches(1);
+    k_traverse<<<a.grid, kDetectThreads, 0, s>>>(a, round);
+    return cudaGetLastError();
 }
 
 int traverse_blocks_per_sm()

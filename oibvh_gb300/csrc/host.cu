@@ -317,7 +317,6 @@ namespace {
 struct PassPlan {
     std::vector<PairView> pv;
     uint64_t front0 = 0;
-    uint32_t iters = 1;
 };
 
 void list_pairs(const oibvh_scene_s* s, std::vector<uint32_t>& out)
@@ -335,27 +334,30 @@ void list_pairs(const oibvh_scene_s* s, std::vector<uint32_t>& out)
     }
 }
 
-int plan_pass(const oibvh_scene_s* s, const uint32_t* pr, uint32_t n, uint32_t entry, uint32_t expand, PassPlan& plan)
+// Start level of each pair: the reference's entry level, deepened so that
+// the start cross product holds about 2^18 node pairs over the pass (the
+// pair set does not depend on it; a deeper start gives the traversal enough
+// independent work for every SM).
+int plan_pass(const oibvh_scene_s* s, const uint32_t* pr, uint32_t n, uint32_t entry, PassPlan& plan)
 {
     plan.pv.resize(n);
     plan.front0 = 0;
-    plan.iters = 0;
+    const uint32_t lg = ilog2(std::max(1u, n));
+    const uint32_t auto_level = lg >= 18 ? 0u : (18u - lg) / 2u;
     for (uint32_t p = 0; p < n; ++p) {
         const TreeShape& A = s->trees[pr[2 * p]]->shape;
         const TreeShape& B = s->trees[pr[2 * p + 1]]->shape;
         PairView v{};
         v.a = pr[2 * p];
         v.b = pr[2 * p + 1];
-        v.entry_a = std::min(entry, A.L);
-        v.entry_b = std::min(entry, B.L);
+        const uint32_t start = std::max(entry, auto_level);
+        v.entry_a = std::min(start, A.L);
+        v.entry_b = std::min(start, B.L);
         v.front_cnt_a = A.level_count(v.entry_a);
         v.front_cnt_b = B.level_count(v.entry_b);
         if (plan.front0 > 0x7fffffffull) return fail(OIBVH_ERR_ARG, "initial BVTT front exceeds 2^31 nodes");
         v.front_off = (uint32_t)plan.front0;
         plan.front0 += (uint64_t)v.front_cnt_a * v.front_cnt_b;
-        const uint32_t depth = std::max(A.L - v.entry_a, B.L - v.entry_b);
-        const uint32_t it = (depth + expand - 1) / expand;  // expansion steps after the initial front
-        plan.iters = std::max(plan.iters, it);
         plan.pv[p] = v;
     }
     if (plan.front0 > 0x7fffffffull) return fail(OIBVH_ERR_ARG, "initial BVTT front exceeds 2^31 nodes");
@@ -414,14 +416,14 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
     OK_TRY(upload_views(s, st));
     OK_TRY(s->hits.ensure(s->hit_cap, "cudaMalloc(hits)"));
 
-    const int grid = sm_count(s->device) * std::min(4, traverse_blocks_per_sm());
+    const int grid = sm_count(s->device) * traverse_blocks_per_sm();
+    constexpr uint32_t kRoundsEnqueued = 2;  // rounds launched before the first read-back
     for (uint32_t p0 = 0; p0 < n_pairs; p0 += kMaxPairsPerPass) {
         const uint32_t np = std::min(kMaxPairsPerPass, n_pairs - p0);
         PassPlan plan;
-        OK_TRY(plan_pass(s, pr.data() + 2 * (size_t)p0, np, entry, expand, plan));
-        const uint32_t n_counts = kCountFront0 + plan.iters + 1;
-        OK_TRY(s->counts.ensure(n_counts, "cudaMalloc(counts)"));
-        OK_TRY(s->h_counts.ensure(n_counts, "cudaMallocHost(counts)"));
+        OK_TRY(plan_pass(s, pr.data() + 2 * (size_t)p0, np, entry, plan));
+        OK_TRY(s->counts.ensure(kCountTotal, "cudaMalloc(counts)"));
+        OK_TRY(s->h_counts.ensure(kCountTotal, "cudaMallocHost(counts)"));
         OK_TRY(s->h_pairs.ensure(np, "cudaMallocHost(pairs)"));
         OK_TRY(s->pairv.ensure(np, "cudaMalloc(pairs)"));
         CUDA_TRY(cudaStreamSynchronize(st));
@@ -430,10 +432,10 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
         const uint64_t hits_before = s->hit_count;
         for (int attempt = 0;; ++attempt) {
             if (attempt > 12) return fail(OIBVH_ERR_OVERFLOW, "BVTT queues kept overflowing after regrowing");
-            OK_TRY(s->front0.ensure(s->front_cap, "cudaMalloc(front)"));
-            OK_TRY(s->front1.ensure(s->front_cap, "cudaMalloc(front)"));
+            OK_TRY(s->front0.ensure(s->front_cap, "cudaMalloc(work list)"));
+            OK_TRY(s->front1.ensure(s->front_cap, "cudaMalloc(work list)"));
             if (!narrow) OK_TRY(s->cand.ensure(s->cand_cap, "cudaMalloc(candidates)"));
-            CUDA_TRY(cudaMemsetAsync(s->counts.p, 0, n_counts * sizeof(uint32_t), st));
+            CUDA_TRY(cudaMemsetAsync(s->counts.p, 0, kCountTotal * sizeof(uint32_t), st));
             if (hits_before) {
                 s->h_counts.p[0] = (uint32_t)hits_before;
                 CUDA_TRY(cudaMemcpyAsync(s->counts.p, s->h_counts.p, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
@@ -442,34 +444,42 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
             a.trees = s->views.p;
             a.pairs = s->pairv.p;
             a.n_pairs = np;
-            a.expand_levels = std::min(expand, 3u);
-            a.front[0] = s->front0.p;
-            a.front[1] = s->front1.p;
-            a.front_cap = s->front_cap;
+            a.expand_levels = 1;
+            a.work[0] = s->front0.p;
+            a.work[1] = s->front1.p;
+            a.work_cap = s->front_cap;
             a.cand = narrow ? nullptr : s->cand.p;
             a.cand_cap = narrow ? 0 : s->cand_cap;
             a.hits = s->hits.p;
             a.hit_cap = s->hit_cap;
             a.counts = s->counts.p;
-            a.iters = plan.iters;
             a.fuse_narrow = narrow ? 1u : 0u;
             a.grid = grid;
-            CUDA_TRY(launch_traverse(a, (uint32_t)plan.front0, st));
-            CUDA_TRY(cudaMemcpyAsync(s->h_counts.p, s->counts.p, n_counts * sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                                     st));
-            CUDA_TRY(cudaStreamSynchronize(st));
-            const uint32_t* c = s->h_counts.p;
-            const uint32_t flags = c[kCountFlags];
-            if (flags & kFlagTimeout) return fail(OIBVH_ERR_TIMEOUT, "traversal grid barrier timed out");
-            if (!(flags & kFlagFrontOverflow) && c[kCountFront0 + plan.iters] != 0)
-                return fail(OIBVH_ERR_STATE, "internal: BVTT front not empty after the last level");
-            if (flags) {
-                s->stats.retries++;
-                if (flags & kFlagFrontOverflow) {
-                    uint64_t peak = 0;
-                    for (uint32_t k = 0; k <= plan.iters; ++k) peak = std::max<uint64_t>(peak, c[kCountFront0 + k]);
-                    s->front_cap = grow_cap(peak, s->front_cap);
+            CUDA_TRY(launch_init_front(a, (uint32_t)plan.front0, st));
+            uint32_t rounds = 0;
+            bool overflowed = false;
+            for (;;) {
+                const uint32_t upto = std::min(kMaxRounds, rounds + (rounds ? 1u : kRoundsEnqueued));
+                for (; rounds < upto; ++rounds) CUDA_TRY(launch_traverse(a, rounds, st));
+                CUDA_TRY(cudaMemcpyAsync(s->h_counts.p, s->counts.p, kCountTotal * sizeof(uint32_t),
+                                         cudaMemcpyDeviceToHost, st));
+                CUDA_TRY(cudaStreamSynchronize(st));
+                const uint32_t* c = s->h_counts.p;
+                if (c[kCountFlags]) {
+                    overflowed = true;
+                    break;
                 }
+                if (c[kCountWork0 + rounds] == 0) break;  // nothing spilled past the last round
+                if (rounds >= kMaxRounds) return fail(OIBVH_ERR_OVERFLOW, "BVTT traversal needed too many rounds");
+            }
+            const uint32_t* c = s->h_counts.p;
+            uint64_t peak = 0;
+            for (uint32_t k = 0; k <= rounds; ++k) peak = std::max<uint64_t>(peak, c[kCountWork0 + k]);
+            if (overflowed) {
+                const uint32_t flags = c[kCountFlags];
+                if (flags & kFlagTimeout) return fail(OIBVH_ERR_TIMEOUT, "device wait timed out");
+                s->stats.retries++;
+                if (flags & kFlagFrontOverflow) s->front_cap = grow_cap(peak, s->front_cap);
                 if (flags & kFlagCandOverflow) s->cand_cap = grow_cap(c[kCountCandSlots], s->cand_cap);
                 if (flags & kFlagHitOverflow) {
                     const uint32_t want = grow_cap(c[kCountHits], s->hit_cap);
@@ -478,11 +488,9 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
                 }
                 continue;
             }
-            uint64_t peak = 0;
-            for (uint32_t k = 0; k <= plan.iters; ++k) peak = std::max<uint64_t>(peak, c[kCountFront0 + k]);
             s->stats.nodes_tested += c[kCountTested];
             s->stats.front_peak = std::max(s->stats.front_peak, peak);
-            s->stats.steps = plan.iters + 1;
+            s->stats.steps = rounds;
             s->cand_count += c[kCountCands];
             if (narrow) s->hit_count = c[kCountHits];
             break;
@@ -523,7 +531,7 @@ int narrow_impl(oibvh_scene_s* s, cudaStream_t st)
         a.grid = sm_count(s->device) * 8;
         a.fuse_narrow = 1;
         CUDA_TRY(launch_narrow(a, st));
-        CUDA_TRY(cudaMemcpyAsync(s->h_counts.p, s->counts.p, kCountFront0 * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+        CUDA_TRY(cudaMemcpyAsync(s->h_counts.p, s->counts.p, kCountHead0 * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                                  st));
         CUDA_TRY(cudaStreamSynchronize(st));
         if (s->h_counts.p[kCountFlags] & kFlagHitOverflow) {

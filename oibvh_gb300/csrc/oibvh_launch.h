@@ -47,24 +47,27 @@ struct DetectArgs {
     const PairView* pairs;
     uint32_t n_pairs;
     uint32_t expand_levels;
-    uint64_t* front[2];
-    uint32_t front_cap;
-    uint64_t* cand;
+    uint64_t* work[2];     // traversal work lists (ping-pong between rounds)
+    uint32_t work_cap;
+    uint64_t* cand;        // broad-only mode: candidate leaf pairs
     uint32_t cand_cap;
     uint4* hits;
     uint32_t hit_cap;
-    uint32_t* counts;  // see kCount* below
-    uint32_t iters;    // BVTT steps after the initial front
+    uint32_t* counts;      // see kCount* below
     uint32_t fuse_narrow;  // 1: test candidates in the traversal; 0: store them
-    int grid;          // CTAs (cooperative: all co-resident)
+    int grid;              // CTAs of the grid-stride / persistent kernels
 };
-cudaError_t launch_traverse(const DetectArgs& a, uint32_t total0, cudaStream_t s);
+cudaError_t launch_init_front(const DetectArgs& a, uint32_t total0, cudaStream_t s);
+cudaError_t launch_traverse(const DetectArgs& a, uint32_t round, cudaStream_t s);
 int traverse_blocks_per_sm();
 cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s);
 
 // counts[]: hits, flags, candidates found, candidate slots used (broad-only),
-// nodes tested, grid barrier (2 words), then the front size entering each step.
+// BVTT pairs tested, then per traversal round: the work-list grab head, and
+// the work-list size (round 0: the overlapping start-level pairs; round r+1:
+// what round r spilled).
+constexpr uint32_t kMaxRounds = 16;
 constexpr uint32_t kCountHits = 0, kCountFlags = 1, kCountCands = 2, kCountCandSlots = 3, kCountTested = 4,
-                   kCountBarrier = 5, kCountFront0 = 7;
+                   kCountHead0 = 8, kCountWork0 = kCountHead0 + kMaxRounds, kCountTotal = kCountWork0 + kMaxRounds + 1;
 
 } // namespace oibvh
