@@ -47,7 +47,7 @@ struct DetectArgs {
     const PairView* pairs;
     uint32_t n_pairs;
     uint32_t expand_levels;
-    uint64_t* work[2];     // traversal work lists (ping-pong between rounds)
+    uint64_t* work[2];     // work[0]: the traversal queue (slots hold ~0 when free)
     uint32_t work_cap;
     uint64_t* cand;        // broad-only mode: candidate leaf pairs
     uint32_t cand_cap;
@@ -58,16 +58,14 @@ struct DetectArgs {
     int grid;              // CTAs of the grid-stride / persistent kernels
 };
 cudaError_t launch_init_front(const DetectArgs& a, uint32_t total0, cudaStream_t s);
-cudaError_t launch_traverse(const DetectArgs& a, uint32_t round, cudaStream_t s);
+cudaError_t launch_traverse(const DetectArgs& a, cudaStream_t s);
 int traverse_blocks_per_sm();
 cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s);
 
 // counts[]: hits, flags, candidates found, candidate slots used (broad-only),
-// BVTT pairs tested, then per traversal round: the work-list grab head, and
-// the work-list size (round 0: the overlapping start-level pairs; round r+1:
-// what round r spilled).
-constexpr uint32_t kMaxRounds = 16;
+// BVTT pairs tested, then the traversal queue: reserved tail (= pairs ever
+// queued), taken head, pending work.
 constexpr uint32_t kCountHits = 0, kCountFlags = 1, kCountCands = 2, kCountCandSlots = 3, kCountTested = 4,
-                   kCountHead0 = 8, kCountWork0 = kCountHead0 + kMaxRounds, kCountTotal = kCountWork0 + kMaxRounds + 1;
+                   kCountQTail = 5, kCountQHead = 6, kCountPending = 7, kCountTotal = 8;
 
 } // namespace oibvh
