@@ -7,10 +7,9 @@
 // triangleIntersection2 (third/gProximity/cuda_intersect_tritri.h:350-434).
 //
 // The broad phase is two kernels: k_init_front tests the cross product of
-// the node pairs at a start level and queues the overlapping ones; in
-// k_traverse every CTA repeatedly takes a chunk of the queue and walks it to
-// the leaves level by level with its front in shared memory, publishing
-// surplus pairs back to the queue while other CTAs are idle, so no
+// the node pairs at a start level and lists the overlapping ones; in
+// k_traverse every CTA takes an interleaved share of that list and walks it
+// to the leaves level by level with its front in shared memory, so no
 // grid-wide synchronisation is needed. The host enqueues everything and
 // reads the counters back once.
 // Appends (next front, candidates, hits) are warp-aggregated: one atomicAdd
@@ -135,10 +134,6 @@ __device__ __forceinline__ void expand_side(const TreeShape& S, uint32_t ia, uin
 // ---------------------------------------------------------------------------
 constexpr int kCandBuf = 64;  // <= 31 left over + 32 added per round
 constexpr uint32_t kFrontCap = 2048;  // per-CTA front in shared memory, per level
-constexpr uint32_t kKeep = 256;       // per-CTA front kept while other CTAs starve
-constexpr uint32_t kGrab = 32;        // queue items a CTA takes at a time
-constexpr uint64_t kEmptySlot = ~0ull; // no valid BVTT node has pair 0xffff and index 0xffffff
-constexpr uint32_t kSpinLimit = 1u << 22;
 
 struct WarpCands {
     uint64_t* buf;  // kCandBuf entries
@@ -202,11 +197,12 @@ __device__ __forceinline__ void push_candidate(const DetectArgs& a, WarpCands& w
 // all child boxes are loaded first (independent loads), the up to 4 child
 // pairs are tested, overlapping leaf pairs become candidates and the other
 // overlapping pairs are appended to the CTA's next front in shared memory
-// (one shared atomic per warp). Positions at or past `keep` are published
-// to the global work queue instead, for other CTAs to take.
+// (one shared atomic per warp); what does not fit goes to the spill list
+// of the next round.
 // Returns the number of child pairs tested (lane 0 only, else 0).
 __device__ __forceinline__ uint32_t expand_pair(const DetectArgs& a, WarpCands& wc, bool valid, uint64_t node,
-                                                uint64_t* next, uint32_t* next_cnt, uint32_t keep, uint32_t lane)
+                                                uint64_t* next, uint32_t* next_cnt, uint64_t* __restrict__ spill,
+                                                uint32_t* spill_cnt, uint32_t lane)
 {
     uint32_t pair = 0, fa = 0, fb = 0, na = 0, nb = 0, leaf_a = 0, leaf_b = 0;
     bool leaves = false;
@@ -260,38 +256,31 @@ __device__ __forceinline__ uint32_t expand_pair(const DetectArgs& a, WarpCands& 
     }
     const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
     if (total == 0) return lane == 0 ? tested : 0u;
-    uint32_t wbase = 0, qbase = 0, nq = 0;
+    uint32_t wbase = 0, sbase = 0;
     if (lane == 31) {
         wbase = atomicAdd(next_cnt, total);
-        const uint32_t fit = wbase >= keep ? 0u : min(total, keep - wbase);
-        nq = total - fit;
-        if (nq) {
-            atomicAdd(a.counts + kCountPending, nq);  // before they become visible
-            qbase = atomicAdd(a.counts + kCountQTail, nq);
-            const uint32_t room = qbase >= a.work_cap ? 0u : min(nq, a.work_cap - qbase);
-            if (room < nq) {
-                // the pairs past the end are dropped (the host regrows the queue and reruns)
-                atomicOr(a.counts + kCountFlags, (uint32_t)kFlagFrontOverflow);
-                atomicSub(a.counts + kCountPending, nq - room);
-            }
-        }
+        const uint32_t fit = wbase >= kFrontCap ? 0u : min(total, kFrontCap - wbase);
+        if (total > fit) sbase = atomicAdd(spill_cnt, total - fit);
     }
     wbase = __shfl_sync(0xffffffffu, wbase, 31);
-    qbase = __shfl_sync(0xffffffffu, qbase, 31);
-    const uint32_t q_from = max(wbase, keep);  // first front position that goes to the queue
+    sbase = __shfl_sync(0xffffffffu, sbase, 31);
+    const uint32_t spill_from = max(wbase, kFrontCap);  // first front position that spills
     uint32_t pos = wbase + incl - cnt;
+    bool overflow = false;
     uint32_t mm = leaves ? 0u : m;
     while (mm) {
         const uint32_t k = __ffs(mm) - 1;
         mm &= mm - 1;
         const uint64_t child = bvtt_pack(pair, fa + (k >> 1), fb + (k & 1));
-        if (pos < keep) next[pos] = child;
+        if (pos < kFrontCap) next[pos] = child;
         else {
-            const uint32_t q = qbase + (pos - q_from);
-            if (q < a.work_cap) a.work[0][q] = child;
+            const uint32_t sp = sbase + (pos - spill_from);
+            if (sp < a.work_cap) spill[sp] = child;
+            else overflow = true;
         }
         ++pos;
     }
+    if (overflow) atomicOr(a.counts + kCountFlags, (uint32_t)kFlagFrontOverflow);
     return lane == 0 ? tested : 0u;
 }
 
@@ -330,110 +319,59 @@ __global__ void __launch_bounds__(kDetectThreads) k_init_front(DetectArgs a, uin
         }
         push_candidate(a, wc, leafpair, cval, lane);
         const bool push = ov && !leafpair;
-        const uint32_t pos = warp_append(a.counts + kCountQTail, push, lane);
-        const bool stored = push && pos < a.work_cap;
-        if (stored) a.work[0][pos] = node;
-        else if (push) atomicOr(a.counts + kCountFlags, (uint32_t)kFlagFrontOverflow);
-        const uint32_t ns = __popc(__ballot_sync(0xffffffffu, stored));
-        if (lane == 0 && ns) atomicAdd(a.counts + kCountPending, ns);
+        const uint32_t pos = warp_append(a.counts + kCountWork0, push, lane);
+        if (push) {
+            if (pos < a.work_cap) a.work[0][pos] = node;
+            else atomicOr(a.counts + kCountFlags, (uint32_t)kFlagFrontOverflow);
+        }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.counts + kCountTested, total0);
     if (a.fuse_narrow && wc.n > 0) test_candidates(a, wc.buf, wc.n, lane);
 }
 
-// The traversal proper. CTAs take chunks of the global work queue and walk
-// each chunk to the leaves level by level with the front in shared memory
-// (__syncthreads between levels; no grid-wide wait). While other CTAs starve
-// (few queued items), a CTA keeps at most kKeep pairs per level and publishes
-// the rest to the queue, so heavy regions spread over the whole GPU.
-//
-// Queue protocol: a slot holds kEmptySlot until its item is written;
-// producers add to `pending` before they reserve slots (`qtail`); a CTA takes
-// slots only below qtail (CAS on `qhead`) and waits for them to be written;
-// it subtracts its chunk from `pending` once the chunk's subtree is done, so
-// pending == 0 with qhead == qtail means no work exists anywhere. Every wait
-// is bounded: past kSpinLimit polls the CTA raises kFlagTimeout and stops.
-__global__ void __launch_bounds__(kDetectThreads) k_traverse(DetectArgs a)
+// Traversal round `round`. CTA b takes the round's work-list items b, b+G,
+// b+2G, ... (G = number of CTAs; the list is in spatial order, so the
+// interleave spreads every region of the intersection over all CTAs) and
+// walks them to the leaves level by level with the front in shared memory:
+// __syncthreads between levels, no grid-wide wait, no atomics to take work.
+// A level that outgrows shared memory spills the excess to the next round's
+// list, which the next launch drains the same way.
+__global__ void __launch_bounds__(kDetectThreads) k_traverse(DetectArgs a, uint32_t round)
 {
     __shared__ uint64_t s_front[2][kFrontCap];
     __shared__ uint64_t s_cand[kDetectThreads / 32][kCandBuf];
     __shared__ uint32_t s_cnt[2];
-    __shared__ uint32_t s_grab[2];
-    __shared__ uint32_t s_keep;
-    __shared__ uint32_t s_bad;
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     constexpr uint32_t kWarps = kDetectThreads / 32;
     WarpCands wc{s_cand[wib], 0};
-    volatile uint32_t* qhead = a.counts + kCountQHead;
-    volatile uint32_t* qtail = a.counts + kCountQTail;
-    volatile uint32_t* pending = a.counts + kCountPending;
-    volatile uint64_t* queue = a.work[0];
+    const uint64_t* __restrict__ src = (round & 1) ? a.work[1] : a.work[0];
+    uint64_t* __restrict__ spill = (round & 1) ? a.work[0] : a.work[1];
+    uint32_t* spill_cnt = a.counts + kCountWork0 + round + 1;
+    const uint32_t n_src = min(*(volatile uint32_t*)(a.counts + kCountWork0 + round), a.work_cap);
+    const uint32_t G = gridDim.x;
     uint32_t tested = 0;
 
-    for (;;) {
-        if (threadIdx.x == 0) {
-            uint32_t got = 0, start = 0, spins = 0;
-            for (;;) {
-                const uint32_t h = *qhead, t = min(*qtail, a.work_cap);
-                if (h < t) {
-                    const uint32_t n = min(kGrab, t - h);
-                    if (atomicCAS(a.counts + kCountQHead, h, h + n) == h) {
-                        start = h;
-                        got = n;
-                        break;
-                    }
-                } else if (*pending == 0) {
-                    break;
-                }
-                if (++spins > kSpinLimit) {
-                    atomicOr(a.counts + kCountFlags, (uint32_t)kFlagTimeout);
-                    break;
-                }
-                __nanosleep(100);
-            }
-            s_grab[0] = start;
-            s_grab[1] = got;
-            s_bad = 0;
-        }
+    // items blockIdx.x + k*G, in chunks of at most kFrontCap
+    for (uint32_t k0 = 0;; k0 += kFrontCap) {
+        const uint32_t first = blockIdx.x + k0 * G;
+        if (first >= n_src) break;
+        const uint32_t c0 = min(kFrontCap, (n_src - first + G - 1) / G);
+        for (uint32_t i = threadIdx.x; i < c0; i += kDetectThreads) s_front[0][i] = __ldcg(src + first + i * G);
+        uint32_t cur = 0, c = c0;
         __syncthreads();
-        const uint32_t g0 = s_grab[0], gn = s_grab[1];
-        if (gn == 0) break;
-        for (uint32_t i = threadIdx.x; i < gn; i += kDetectThreads) {
-            uint64_t v = queue[g0 + i];
-            uint32_t spins = 0;
-            while (v == kEmptySlot && ++spins <= kSpinLimit) {
-                __nanosleep(32);
-                v = queue[g0 + i];
-            }
-            if (v == kEmptySlot) {
-                atomicOr(a.counts + kCountFlags, (uint32_t)kFlagTimeout);
-                s_bad = 1;
-            }
-            queue[g0 + i] = kEmptySlot;  // leave the slot clean for the next detect
-            s_front[0][i] = v;
-        }
-        __syncthreads();
-        uint32_t cur = 0, c = s_bad ? 0u : gn;  // a timed-out wait: give up on this chunk
         while (c > 0) {
-            if (threadIdx.x == 0) {
-                s_cnt[cur ^ 1] = 0;
-                const uint32_t queued = *qtail - *qhead;
-                s_keep = queued < gridDim.x ? kKeep : kFrontCap;
-            }
+            if (threadIdx.x == 0) s_cnt[cur ^ 1] = 0;
             __syncthreads();
-            const uint32_t keep = s_keep;
             for (uint32_t base = wib * 32; base < c; base += kWarps * 32) {
                 const uint32_t i = base + lane;
                 const bool valid = i < c;
                 const uint64_t node = valid ? s_front[cur][i] : 0ull;
-                tested += expand_pair(a, wc, valid, node, s_front[cur ^ 1], &s_cnt[cur ^ 1], keep, lane);
+                tested += expand_pair(a, wc, valid, node, s_front[cur ^ 1], &s_cnt[cur ^ 1], spill, spill_cnt, lane);
             }
             __syncthreads();
-            c = min(s_cnt[cur ^ 1], keep);
+            c = min(s_cnt[cur ^ 1], kFrontCap);
             cur ^= 1;
         }
-        if (threadIdx.x == 0) atomicSub(a.counts + kCountPending, gn);
-        __syncthreads();  // s_grab / s_front are rewritten by the next chunk
     }
     if (lane == 0 && tested) atomicAdd(a.counts + kCountTested, tested);
     if (a.fuse_narrow && wc.n > 0) test_candidates(a, wc.buf, wc.n, lane);
@@ -463,10 +401,10 @@ cudaError_t launch_init_front(const DetectArgs& a, uint32_t total0, cudaStream_t
     return cudaGetLastError();
 }
 
-cudaError_t launch_traverse(const DetectArgs& a, cudaStream_t s)
+cudaError_t launch_traverse(const DetectArgs& a, uint32_t round, cudaStream_t s)
 {
     note_launches(1);
-    k_traverse<<<a.grid, kDetectThreads, 0, s>>>(a);
+    k_traverse<<<a.grid, kDetectThreads, 0, s>>>(a, round);
     return cudaGetLastError();
 }
 

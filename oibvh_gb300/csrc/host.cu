@@ -297,7 +297,6 @@ struct oibvh_scene_s {
     uint32_t front_cap = 1u << 20;
     uint32_t cand_cap = 1u << 20;
     uint32_t hit_cap = 1u << 18;
-    bool queue_dirty = true;  // the traversal queue needs its slots reset to empty
 
     // multi-tree refit: job table as last uploaded
     DevBuf<RefitJob> refit_jobs;
@@ -432,13 +431,8 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
         const uint64_t hits_before = s->hit_count;
         for (int attempt = 0;; ++attempt) {
             if (attempt > 12) return fail(OIBVH_ERR_OVERFLOW, "BVTT queues kept overflowing after regrowing");
-            if (s->front0.n < s->front_cap || !s->front0.p) s->queue_dirty = true;
-            OK_TRY(s->front0.ensure(s->front_cap, "cudaMalloc(work queue)"));
-            if (s->queue_dirty) {
-                // every slot of the queue reads "empty" (all ones) until written
-                CUDA_TRY(cudaMemsetAsync(s->front0.p, 0xff, s->front0.n * sizeof(uint64_t), st));
-                s->queue_dirty = false;
-            }
+            OK_TRY(s->front0.ensure(s->front_cap, "cudaMalloc(work list)"));
+            OK_TRY(s->front1.ensure(s->front_cap, "cudaMalloc(work list)"));
             if (!narrow) OK_TRY(s->cand.ensure(s->cand_cap, "cudaMalloc(candidates)"));
             CUDA_TRY(cudaMemsetAsync(s->counts.p, 0, kCountTotal * sizeof(uint32_t), st));
             if (hits_before) {
@@ -451,7 +445,7 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
             a.n_pairs = np;
             a.expand_levels = 1;
             a.work[0] = s->front0.p;
-            a.work[1] = nullptr;
+            a.work[1] = s->front1.p;
             a.work_cap = s->front_cap;
             a.cand = narrow ? nullptr : s->cand.p;
             a.cand_cap = narrow ? 0 : s->cand_cap;
@@ -461,22 +455,25 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
             a.fuse_narrow = narrow ? 1u : 0u;
             a.grid = grid;
             CUDA_TRY(launch_init_front(a, (uint32_t)plan.front0, st));
-            CUDA_TRY(launch_traverse(a, st));
-            CUDA_TRY(cudaMemcpyAsync(s->h_counts.p, s->counts.p, kCountTotal * sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                                     st));
-            CUDA_TRY(cudaStreamSynchronize(st));
+            uint32_t rounds = 0;
+            for (;;) {
+                // two rounds go out with the first read-back; later ones one by one
+                const uint32_t upto = std::min(kMaxRounds, rounds ? rounds + 1 : 2u);
+                for (; rounds < upto; ++rounds) CUDA_TRY(launch_traverse(a, rounds, st));
+                CUDA_TRY(cudaMemcpyAsync(s->h_counts.p, s->counts.p, kCountTotal * sizeof(uint32_t),
+                                         cudaMemcpyDeviceToHost, st));
+                CUDA_TRY(cudaStreamSynchronize(st));
+                const uint32_t* c = s->h_counts.p;
+                if (c[kCountFlags] || c[kCountWork0 + rounds] == 0) break;
+                if (rounds >= kMaxRounds) return fail(OIBVH_ERR_OVERFLOW, "BVTT traversal needed too many rounds");
+            }
             const uint32_t* c = s->h_counts.p;
             const uint32_t flags = c[kCountFlags];
-            if (flags & kFlagTimeout) {
-                s->queue_dirty = true;
-                return fail(OIBVH_ERR_TIMEOUT, "a bounded wait in the traversal gave up");
-            }
+            uint64_t peak = 0;
+            for (uint32_t k = 0; k <= rounds; ++k) peak = std::max<uint64_t>(peak, c[kCountWork0 + k]);
             if (flags) {
                 s->stats.retries++;
-                if (flags & kFlagFrontOverflow) {
-                    s->front_cap = grow_cap(c[kCountQTail], s->front_cap);
-                    s->queue_dirty = true;
-                }
+                if (flags & kFlagFrontOverflow) s->front_cap = grow_cap(peak, s->front_cap);
                 if (flags & kFlagCandOverflow) s->cand_cap = grow_cap(c[kCountCandSlots], s->cand_cap);
                 if (flags & kFlagHitOverflow) {
                     const uint32_t want = grow_cap(c[kCountHits], s->hit_cap);
@@ -485,10 +482,9 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
                 }
                 continue;
             }
-            const uint64_t peak = c[kCountQTail];
             s->stats.nodes_tested += c[kCountTested];
             s->stats.front_peak = std::max(s->stats.front_peak, peak);
-            s->stats.steps = 1;
+            s->stats.steps = rounds;
             s->cand_count += c[kCountCands];
             if (narrow) s->hit_count = c[kCountHits];
             break;
@@ -918,7 +914,7 @@ API int oibvh_scene_set_queue_capacity(oibvh_scene_t s, uint32_t front, uint32_t
     if (front) {
         s->front_cap = front;
         s->front0.release();
-        s->queue_dirty = true;
+        s->front1.release();
     }
     if (candidates) {
         s->cand_cap = candidates;

@@ -47,7 +47,7 @@ struct DetectArgs {
     const PairView* pairs;
     uint32_t n_pairs;
     uint32_t expand_levels;
-    uint64_t* work[2];     // work[0]: the traversal queue (slots hold ~0 when free)
+    uint64_t* work[2];     // traversal work lists (ping-pong between rounds)
     uint32_t work_cap;
     uint64_t* cand;        // broad-only mode: candidate leaf pairs
     uint32_t cand_cap;
@@ -58,14 +58,15 @@ struct DetectArgs {
     int grid;              // CTAs of the grid-stride / persistent kernels
 };
 cudaError_t launch_init_front(const DetectArgs& a, uint32_t total0, cudaStream_t s);
-cudaError_t launch_traverse(const DetectArgs& a, cudaStream_t s);
+cudaError_t launch_traverse(const DetectArgs& a, uint32_t round, cudaStream_t s);
 int traverse_blocks_per_sm();
 cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s);
 
 // counts[]: hits, flags, candidates found, candidate slots used (broad-only),
-// BVTT pairs tested, then the traversal queue: reserved tail (= pairs ever
-// queued), taken head, pending work.
+// BVTT pairs tested, then the work-list size of each traversal round (round
+// 0: the overlapping start pairs; round r+1: what round r spilled).
+constexpr uint32_t kMaxRounds = 16;
 constexpr uint32_t kCountHits = 0, kCountFlags = 1, kCountCands = 2, kCountCandSlots = 3, kCountTested = 4,
-                   kCountQTail = 5, kCountQHead = 6, kCountPending = 7, kCountTotal = 8;
+                   kCountWork0 = 8, kCountTotal = kCountWork0 + kMaxRounds + 1;
 
 } // namespace oibvh
