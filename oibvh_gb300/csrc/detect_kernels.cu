@@ -6,12 +6,12 @@
 // triangle_intersect_kernel (src/cuda/collide.cu:248-299) with
 // triangleIntersection2 (third/gProximity/cuda_intersect_tritri.h:350-434).
 //
-// The broad phase is two kernels: k_init_front tests the cross product of
-// the node pairs at a start level and lists the overlapping ones; in
-// k_traverse every CTA takes an interleaved share of that list and walks it
-// to the leaves level by level with its front in shared memory, so no
-// grid-wide synchronisation is needed. The host enqueues everything and
-// reads the counters back once.
+// The broad phase is three kernels: k_init_front tests the cross product of
+// the node pairs at a start level and lists the overlapping ones; k_top (one
+// CTA) walks the narrow top levels until the front is wide; in k_walk every
+// warp takes an interleaved share of that front and walks it to the leaves
+// with a private front in shared memory, so no grid-wide synchronisation is
+// needed. The host enqueues everything and reads the counters back once.
 // Appends (next front, candidates, hits) are warp-aggregated: one atomicAdd
 // per warp, positions from ballot/shuffle prefix sums. The narrow phase is
 // fused: overlapping leaf pairs are buffered per warp in shared memory and
@@ -133,7 +133,10 @@ __device__ __forceinline__ void expand_side(const TreeShape& S, uint32_t ia, uin
 // runs at full SIMT width however sparse the candidates are.
 // ---------------------------------------------------------------------------
 constexpr int kCandBuf = 64;  // <= 31 left over + 32 added per round
-constexpr uint32_t kFrontCap = 2048;  // per-CTA front in shared memory, per level
+constexpr uint32_t kTopThreads = 1024;  // the single CTA of the top levels
+constexpr uint32_t kTopCap = 8192;      // its front capacity (two buffers: 128 KB)
+constexpr uint32_t kHandoff = 2048;     // front width at which the walkers take over
+constexpr uint32_t kWalkCap = 128;      // per-warp front capacity of the walkers
 
 struct WarpCands {
     uint64_t* buf;  // kCandBuf entries
@@ -201,8 +204,8 @@ __device__ __forceinline__ void push_candidate(const DetectArgs& a, WarpCands& w
 // of the next round.
 // Returns the number of child pairs tested (lane 0 only, else 0).
 __device__ __forceinline__ uint32_t expand_pair(const DetectArgs& a, WarpCands& wc, bool valid, uint64_t node,
-                                                uint64_t* next, uint32_t* next_cnt, uint64_t* __restrict__ spill,
-                                                uint32_t* spill_cnt, uint32_t lane)
+                                                uint64_t* next, uint32_t* next_cnt, uint32_t next_cap,
+                                                uint64_t* __restrict__ spill, uint32_t* spill_cnt, uint32_t lane)
 {
     uint32_t pair = 0, fa = 0, fb = 0, na = 0, nb = 0, leaf_a = 0, leaf_b = 0;
     bool leaves = false;
@@ -259,12 +262,12 @@ __device__ __forceinline__ uint32_t expand_pair(const DetectArgs& a, WarpCands& 
     uint32_t wbase = 0, sbase = 0;
     if (lane == 31) {
         wbase = atomicAdd(next_cnt, total);
-        const uint32_t fit = wbase >= kFrontCap ? 0u : min(total, kFrontCap - wbase);
+        const uint32_t fit = wbase >= next_cap ? 0u : min(total, next_cap - wbase);
         if (total > fit) sbase = atomicAdd(spill_cnt, total - fit);
     }
     wbase = __shfl_sync(0xffffffffu, wbase, 31);
     sbase = __shfl_sync(0xffffffffu, sbase, 31);
-    const uint32_t spill_from = max(wbase, kFrontCap);  // first front position that spills
+    const uint32_t spill_from = max(wbase, next_cap);  // first front position that spills
     uint32_t pos = wbase + incl - cnt;
     bool overflow = false;
     uint32_t mm = leaves ? 0u : m;
@@ -272,7 +275,7 @@ __device__ __forceinline__ uint32_t expand_pair(const DetectArgs& a, WarpCands& 
         const uint32_t k = __ffs(mm) - 1;
         mm &= mm - 1;
         const uint64_t child = bvtt_pack(pair, fa + (k >> 1), fb + (k & 1));
-        if (pos < kFrontCap) next[pos] = child;
+        if (pos < next_cap) next[pos] = child;
         else {
             const uint32_t sp = sbase + (pos - spill_from);
             if (sp < a.work_cap) spill[sp] = child;
@@ -329,47 +332,103 @@ __global__ void __launch_bounds__(kDetectThreads) k_init_front(DetectArgs a, uin
     if (a.fuse_narrow && wc.n > 0) test_candidates(a, wc.buf, wc.n, lane);
 }
 
-// Traversal round `round`. CTA b takes the round's work-list items b, b+G,
-// b+2G, ... (G = number of CTAs; the list is in spatial order, so the
-// interleave spreads every region of the intersection over all CTAs) and
-// walks them to the leaves level by level with the front in shared memory:
-// __syncthreads between levels, no grid-wide wait, no atomics to take work.
-// A level that outgrows shared memory spills the excess to the next round's
-// list, which the next launch drains the same way.
-__global__ void __launch_bounds__(kDetectThreads) k_traverse(DetectArgs a, uint32_t round)
+// The narrow top of the traversal: ONE CTA of kTopThreads walks the start
+// list level by level with its front in shared memory (__syncthreads between
+// levels) until the front holds more than kHandoff pairs; that front becomes
+// the next work list. The first levels hold a few hundred pairs at most, so
+// one CTA covers them with one round of loads per level and no grid-wide
+// synchronisation.
+__global__ void __launch_bounds__(kTopThreads) k_top(DetectArgs a)
 {
-    __shared__ uint64_t s_front[2][kFrontCap];
-    __shared__ uint64_t s_cand[kDetectThreads / 32][kCandBuf];
+    extern __shared__ uint64_t s_dyn[];  // two front buffers of kTopCap
+    __shared__ uint64_t s_cand[kTopThreads / 32][kCandBuf];
     __shared__ uint32_t s_cnt[2];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    constexpr uint32_t kWarps = kDetectThreads / 32;
+    constexpr uint32_t kWarps = kTopThreads / 32;
+    WarpCands wc{s_cand[wib], 0};
+    uint64_t* out = a.work[1];
+    uint32_t* out_cnt = a.counts + kCountWork0 + 1;
+    const uint32_t n0 = min(a.counts[kCountWork0], a.work_cap);
+    uint32_t tested = 0;
+    // the start list fits the front buffer, or goes straight to the walkers
+    if (n0 > kHandoff) {
+        for (uint32_t i = threadIdx.x; i < n0; i += kTopThreads) out[i] = __ldcg(a.work[0] + i);
+        if (threadIdx.x == 0) *out_cnt = n0;
+        return;
+    }
+    for (uint32_t i = threadIdx.x; i < n0; i += kTopThreads) s_dyn[i] = __ldcg(a.work[0] + i);
+    uint32_t cur = 0, c = n0;
+    __syncthreads();
+    while (c > 0) {
+        uint64_t* fc = cur ? s_dyn + kTopCap : s_dyn;
+        uint64_t* fn = cur ? s_dyn : s_dyn + kTopCap;
+        if (c > kHandoff) {
+            // wide enough: hand the front to the walkers
+            for (uint32_t i = threadIdx.x; i < c; i += kTopThreads) out[i] = fc[i];
+            if (threadIdx.x == 0) *out_cnt = c;
+            break;
+        }
+        if (threadIdx.x == 0) s_cnt[cur ^ 1] = 0;
+        __syncthreads();
+        for (uint32_t base = wib * 32; base < c; base += kWarps * 32) {
+            const uint32_t i = base + lane;
+            const bool valid = i < c;
+            const uint64_t node = valid ? fc[i] : 0ull;
+            // what outgrows the buffer goes to the walkers' list directly
+            tested += expand_pair(a, wc, valid, node, fn, &s_cnt[cur ^ 1], kTopCap, out, out_cnt, lane);
+        }
+        __syncthreads();
+        c = min(s_cnt[cur ^ 1], kTopCap);
+        cur ^= 1;
+    }
+    if (lane == 0 && tested) atomicAdd(a.counts + kCountTested, tested);
+    if (a.fuse_narrow && wc.n > 0) test_candidates(a, wc.buf, wc.n, lane);
+}
+
+// The wide bottom of the traversal, round `round` (>= 1): every warp takes
+// the work-list items w, w+W, w+2W, ... (W = warps in the grid; the
+// interleave spreads each region of the intersection over many warps) and
+// walks them to the leaves level by level with a private front in shared
+// memory: warps never wait for each other. A warp whose front outgrows its
+// buffer spills the excess to the next round's list.
+__global__ void __launch_bounds__(kDetectThreads) k_walk(DetectArgs a, uint32_t round)
+{
+    __shared__ uint64_t s_front[kDetectThreads / 32][2][kWalkCap];
+    __shared__ uint64_t s_cand[kDetectThreads / 32][kCandBuf];
+    __shared__ uint32_t s_cnt[kDetectThreads / 32][2];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     WarpCands wc{s_cand[wib], 0};
     const uint64_t* __restrict__ src = (round & 1) ? a.work[1] : a.work[0];
     uint64_t* __restrict__ spill = (round & 1) ? a.work[0] : a.work[1];
     uint32_t* spill_cnt = a.counts + kCountWork0 + round + 1;
     const uint32_t n_src = min(*(volatile uint32_t*)(a.counts + kCountWork0 + round), a.work_cap);
-    const uint32_t G = gridDim.x;
+    const uint32_t W = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint64_t* f0 = s_front[wib][0];
+    uint64_t* f1 = s_front[wib][1];
+    uint32_t* cnt = s_cnt[wib];
     uint32_t tested = 0;
 
-    // items blockIdx.x + k*G, in chunks of at most kFrontCap
-    for (uint32_t k0 = 0;; k0 += kFrontCap) {
-        const uint32_t first = blockIdx.x + k0 * G;
+    for (uint32_t k0 = 0;; k0 += 32) {
+        const uint32_t first = w + k0 * W;
         if (first >= n_src) break;
-        const uint32_t c0 = min(kFrontCap, (n_src - first + G - 1) / G);
-        for (uint32_t i = threadIdx.x; i < c0; i += kDetectThreads) s_front[0][i] = __ldcg(src + first + i * G);
+        const uint32_t c0 = min(32u, (n_src - first + W - 1) / W);
+        if (lane < c0) f0[lane] = __ldcg(src + first + lane * W);
         uint32_t cur = 0, c = c0;
-        __syncthreads();
+        __syncwarp();
         while (c > 0) {
-            if (threadIdx.x == 0) s_cnt[cur ^ 1] = 0;
-            __syncthreads();
-            for (uint32_t base = wib * 32; base < c; base += kWarps * 32) {
+            uint64_t* fc = cur ? f1 : f0;
+            uint64_t* fn = cur ? f0 : f1;
+            if (lane == 0) cnt[cur ^ 1] = 0;
+            __syncwarp();
+            for (uint32_t base = 0; base < c; base += 32) {
                 const uint32_t i = base + lane;
                 const bool valid = i < c;
-                const uint64_t node = valid ? s_front[cur][i] : 0ull;
-                tested += expand_pair(a, wc, valid, node, s_front[cur ^ 1], &s_cnt[cur ^ 1], spill, spill_cnt, lane);
+                const uint64_t node = valid ? fc[i] : 0ull;
+                tested += expand_pair(a, wc, valid, node, fn, &cnt[cur ^ 1], kWalkCap, spill, spill_cnt, lane);
             }
-            __syncthreads();
-            c = min(s_cnt[cur ^ 1], kFrontCap);
+            __syncwarp();
+            c = min(cnt[cur ^ 1], kWalkCap);
             cur ^= 1;
         }
     }
@@ -401,17 +460,33 @@ cudaError_t launch_init_front(const DetectArgs& a, uint32_t total0, cudaStream_t
     return cudaGetLastError();
 }
 
-cudaError_t launch_traverse(const DetectArgs& a, uint32_t round, cudaStream_t s)
+cudaError_t launch_top(const DetectArgs& a, cudaStream_t s)
 {
+    const int smem = (int)(2 * kTopCap * sizeof(uint64_t));
+    static bool configured[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64 || !configured[dev]) {
+        cudaError_t e = cudaFuncSetAttribute(k_top, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        if (dev >= 0 && dev < 64) configured[dev] = true;
+    }
     note_launches(1);
-    k_traverse<<<a.grid, kDetectThreads, 0, s>>>(a, round);
+    k_top<<<1, kTopThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 
-int traverse_blocks_per_sm()
+cudaError_t launch_walk(const DetectArgs& a, uint32_t round, cudaStream_t s)
+{
+    note_launches(1);
+    k_walk<<<a.grid, kDetectThreads, 0, s>>>(a, round);
+    return cudaGetLastError();
+}
+
+int walk_blocks_per_sm()
 {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_traverse, kDetectThreads, 0) != cudaSuccess) return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_walk, kDetectThreads, 0) != cudaSuccess) return 1;
     return n > 0 ? n : 1;
 }
 

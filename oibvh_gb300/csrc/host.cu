@@ -335,7 +335,7 @@ void list_pairs(const oibvh_scene_s* s, std::vector<uint32_t>& out)
 }
 
 // Start level of each pair: the reference's entry level, deepened so that
-// the start cross product holds about 2^18 node pairs over the pass (the
+// the start cross product holds about 2^16 node pairs over the pass (the
 // pair set does not depend on it; a deeper start gives the traversal enough
 // independent work for every SM).
 int plan_pass(const oibvh_scene_s* s, const uint32_t* pr, uint32_t n, uint32_t entry, PassPlan& plan)
@@ -343,7 +343,7 @@ int plan_pass(const oibvh_scene_s* s, const uint32_t* pr, uint32_t n, uint32_t e
     plan.pv.resize(n);
     plan.front0 = 0;
     const uint32_t lg = ilog2(std::max(1u, n));
-    const uint32_t auto_level = lg >= 18 ? 0u : (18u - lg) / 2u;
+    const uint32_t auto_level = lg >= 16 ? 0u : (16u - lg) / 2u;
     for (uint32_t p = 0; p < n; ++p) {
         const TreeShape& A = s->trees[pr[2 * p]]->shape;
         const TreeShape& B = s->trees[pr[2 * p + 1]]->shape;
@@ -416,7 +416,7 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
     OK_TRY(upload_views(s, st));
     OK_TRY(s->hits.ensure(s->hit_cap, "cudaMalloc(hits)"));
 
-    const int grid = sm_count(s->device) * traverse_blocks_per_sm();
+    const int grid = sm_count(s->device) * walk_blocks_per_sm();
     for (uint32_t p0 = 0; p0 < n_pairs; p0 += kMaxPairsPerPass) {
         const uint32_t np = std::min(kMaxPairsPerPass, n_pairs - p0);
         PassPlan plan;
@@ -455,11 +455,12 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
             a.fuse_narrow = narrow ? 1u : 0u;
             a.grid = grid;
             CUDA_TRY(launch_init_front(a, (uint32_t)plan.front0, st));
-            uint32_t rounds = 0;
+            CUDA_TRY(launch_top(a, st));
+            uint32_t rounds = 1;  // list 1 is the first walk round's input
             for (;;) {
-                // two rounds go out with the first read-back; later ones one by one
-                const uint32_t upto = std::min(kMaxRounds, rounds ? rounds + 1 : 2u);
-                for (; rounds < upto; ++rounds) CUDA_TRY(launch_traverse(a, rounds, st));
+                // two walk rounds go out with the first read-back; later ones one by one
+                const uint32_t upto = std::min(kMaxRounds, rounds == 1 ? 3u : rounds + 1);
+                for (; rounds < upto; ++rounds) CUDA_TRY(launch_walk(a, rounds, st));
                 CUDA_TRY(cudaMemcpyAsync(s->h_counts.p, s->counts.p, kCountTotal * sizeof(uint32_t),
                                          cudaMemcpyDeviceToHost, st));
                 CUDA_TRY(cudaStreamSynchronize(st));

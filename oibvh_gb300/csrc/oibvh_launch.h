@@ -58,13 +58,15 @@ struct DetectArgs {
     int grid;              // CTAs of the grid-stride / persistent kernels
 };
 cudaError_t launch_init_front(const DetectArgs& a, uint32_t total0, cudaStream_t s);
-cudaError_t launch_traverse(const DetectArgs& a, uint32_t round, cudaStream_t s);
-int traverse_blocks_per_sm();
+cudaError_t launch_top(const DetectArgs& a, cudaStream_t s);
+cudaError_t launch_walk(const DetectArgs& a, uint32_t round, cudaStream_t s);
+int walk_blocks_per_sm();
 cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s);
 
 // counts[]: hits, flags, candidates found, candidate slots used (broad-only),
-// BVTT pairs tested, then the work-list size of each traversal round (round
-// 0: the overlapping start pairs; round r+1: what round r spilled).
+// BVTT pairs tested, then the work-list size of each traversal round (list
+// 0: the overlapping start pairs; list 1: the front k_top hands over; list
+// r+1: what walk round r spilled).
 constexpr uint32_t kMaxRounds = 16;
 constexpr uint32_t kCountHits = 0, kCountFlags = 1, kCountCands = 2, kCountCandSlots = 3, kCountTested = 4,
                    kCountWork0 = 8, kCountTotal = kCountWork0 + kMaxRounds + 1;
