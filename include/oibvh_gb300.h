@@ -85,18 +85,26 @@ int oibvh_tree_build(oibvh_tree_t t, void* stream);
  * positions already held. Stream-ordered (not blocking). */
 int oibvh_tree_refit(oibvh_tree_t t, const float* xyz, void* stream);
 
-/* Same as oibvh_tree_refit with positions already in device memory. The
- * tree keeps using `d_xyz` (no copy) until the next refit: the caller keeps
- * it alive and unchanged until every detect that uses this tree is done. */
+/* Same as oibvh_tree_refit with the xyz positions already in device memory
+ * (4-byte aligned); they are converted into the tree's own device layout,
+ * stream-ordered, so `d_xyz` may be reused once the stream has passed. */
 int oibvh_tree_refit_device(oibvh_tree_t t, const float* d_xyz, void* stream);
 
-/* Set the positions the next refit (of this tree, or of its scene) uses,
- * without refitting: from a host array (copied, stream-ordered) or from
- * device memory (borrowed, same rules as oibvh_tree_refit_device). The
- * reference moves vertices through Mesh::transform and reads them back in
- * OibvhTree::refit (src/utils/mesh.cpp:187-214, src/cuda/oibvhTree.cu:196-199). */
+/* Set the positions the next refit (of this tree, or of its scene) and the
+ * next detect use, without refitting. The reference moves vertices through
+ * Mesh::transform and reads them back in OibvhTree::refit
+ * (src/utils/mesh.cpp:187-214, src/cuda/oibvhTree.cu:196-199).
+ *   _set_positions:          host xyz, copied (stream-ordered);
+ *   _set_positions_device:   device xyz, converted (stream-ordered);
+ *   _set_positions4_device:  device xyzw, 16 bytes per vertex,
+ *                            16-byte aligned: used in place, no copy; the
+ *                            caller keeps it alive and unchanged until every
+ *                            refit and detect that reads it has finished.
+ * Inside the library every vertex is a 16-byte (x, y, z, unused) record, so
+ * each vertex gather is one vector load. */
 int oibvh_tree_set_positions(oibvh_tree_t t, const float* xyz, void* stream);
-int oibvh_tree_set_positions_device(oibvh_tree_t t, const float* d_xyz);
+int oibvh_tree_set_positions_device(oibvh_tree_t t, const float* d_xyz, void* stream);
+int oibvh_tree_set_positions4_device(oibvh_tree_t t, const float* d_xyzw);
 
 /* OibvhTree::getDepth() (src/cuda/oibvhTree.cu:46-49) = floor(log2(size)). */
 uint32_t oibvh_tree_get_depth(oibvh_tree_t t);

@@ -55,7 +55,8 @@ SIGNATURES = [
     ("oibvh_tree_refit", ctypes.c_int, [_vp, _f32p, _vp]),
     ("oibvh_tree_refit_device", ctypes.c_int, [_vp, _vp, _vp]),
     ("oibvh_tree_set_positions", ctypes.c_int, [_vp, _f32p, _vp]),
-    ("oibvh_tree_set_positions_device", ctypes.c_int, [_vp, _vp]),
+    ("oibvh_tree_set_positions_device", ctypes.c_int, [_vp, _vp, _vp]),
+    ("oibvh_tree_set_positions4_device", ctypes.c_int, [_vp, _vp]),
     ("oibvh_tree_get_depth", _u32, [_vp]),
     ("oibvh_tree_get_prim_count", _u32, [_vp]),
     ("oibvh_tree_get_size", _u32, [_vp]),

@@ -135,10 +135,15 @@ class OibvhTree:
                 "oibvh_tree_set_positions")
         self._keep = x
 
-    def set_positions_device(self, d_xyz_ptr: int) -> None:
-        """Device positions (raw pointer) for the next refit, borrowed, no refit."""
-        N.check(N.lib().oibvh_tree_set_positions_device(self._h, ctypes.c_void_p(int(d_xyz_ptr))),
-                "oibvh_tree_set_positions_device")
+    def set_positions_device(self, d_xyz_ptr: int, stream=None) -> None:
+        """Device xyz positions (raw pointer) for the next refit, converted, no refit."""
+        N.check(N.lib().oibvh_tree_set_positions_device(self._h, ctypes.c_void_p(int(d_xyz_ptr)),
+                                                         _stream_handle(stream)), "oibvh_tree_set_positions_device")
+
+    def set_positions4_device(self, d_xyzw_ptr: int) -> None:
+        """Device xyzw positions (16 B per vertex, 16-B aligned), used in place."""
+        N.check(N.lib().oibvh_tree_set_positions4_device(self._h, ctypes.c_void_p(int(d_xyzw_ptr))),
+                "oibvh_tree_set_positions4_device")
 
     # reference accessors
     def getDepth(self) -> int:

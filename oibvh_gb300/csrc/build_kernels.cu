@@ -35,14 +35,27 @@ __global__ void k_bounds_init(uint32_t* keys)
     }
 }
 
-__global__ void __launch_bounds__(256) k_mesh_bounds(const float* __restrict__ xyz, uint32_t nV, uint32_t* keys)
+// Positions as given (x, y, z) to the device layout (x, y, z, 0): one
+// 16-byte vector load per vertex everywhere else.
+__global__ void __launch_bounds__(256) k_xyz_to_pos4(const float* __restrict__ xyz, uint32_t nV,
+                                                     float4* __restrict__ pos)
+{
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    pos[v] = make_float4(__ldg(xyz + 3 * (size_t)v), __ldg(xyz + 3 * (size_t)v + 1), __ldg(xyz + 3 * (size_t)v + 2),
+                         0.0f);
+}
+
+__global__ void __launch_bounds__(256) k_mesh_bounds(const float4* __restrict__ pos, uint32_t nV, uint32_t* keys)
 {
     uint32_t mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu};
     uint32_t mx[3] = {0u, 0u, 0u};
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
+        const float4 p = __ldg(pos + v);
+        const float c[3] = {p.x, p.y, p.z};
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            const uint32_t o = float_to_ordered(__ldg(xyz + 3 * (size_t)v + k));
+            const uint32_t o = float_to_ordered(c[k]);
             mn[k] = min(mn[k], o);
             mx[k] = max(mx[k], o);
         }
@@ -97,7 +110,7 @@ __device__ __forceinline__ uint32_t quant1024(float u)
     return __float2uint_rz(v);        // NaN -> 0
 }
 
-__global__ void __launch_bounds__(256) k_leaf_morton(const uint32_t* __restrict__ tri, const float* __restrict__ xyz,
+__global__ void __launch_bounds__(256) k_leaf_morton(const uint32_t* __restrict__ tri, const float4* __restrict__ pos,
                                                      uint32_t nT, const uint32_t* __restrict__ bound_keys,
                                                      uint32_t* __restrict__ codes, uint32_t* __restrict__ idx)
 {
@@ -111,11 +124,12 @@ __global__ void __launch_bounds__(256) k_leaf_morton(const uint32_t* __restrict_
     }
     const uint32_t f0 = __ldg(tri + 3 * (size_t)i), f1 = __ldg(tri + 3 * (size_t)i + 1),
                    f2 = __ldg(tri + 3 * (size_t)i + 2);
+    const float4 p0 = __ldg(pos + f0), p1 = __ldg(pos + f1), p2 = __ldg(pos + f2);
+    const float va[3] = {p0.x, p0.y, p0.z}, vb[3] = {p1.x, p1.y, p1.z}, vc[3] = {p2.x, p2.y, p2.z};
     uint32_t q[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const float a = __ldg(xyz + 3 * (size_t)f0 + k), b = __ldg(xyz + 3 * (size_t)f1 + k),
-                    c = __ldg(xyz + 3 * (size_t)f2 + k);
+        const float a = va[k], b = vb[k], c = vc[k];
         const float mn = gmin(gmin(a, b), c), mx = gmax(gmax(a, b), c);
         const float centroid = __fmul_rn(__fadd_rn(mn, mx), 0.5f);
         const float off = __fsub_rn(centroid, bmin[k]);
@@ -274,7 +288,14 @@ size_t radix_sort_scratch_bytes(uint32_t n)
     return (size_t)256 * n_tiles * sizeof(uint32_t) + 256 * sizeof(uint32_t) + 2 * (size_t)n * sizeof(uint32_t);
 }
 
-cudaError_t launch_mesh_bounds(const float* xyz, uint32_t nV, uint32_t* bound_keys, int num_sms, cudaStream_t s)
+cudaError_t launch_xyz_to_pos4(const float* xyz, uint32_t nV, float4* pos, cudaStream_t s)
+{
+    note_launches(1);
+    k_xyz_to_pos4<<<(nV + 255) / 256, 256, 0, s>>>(xyz, nV, pos);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mesh_bounds(const float4* xyz, uint32_t nV, uint32_t* bound_keys, int num_sms, cudaStream_t s)
 {
     note_launches(1);
     k_bounds_init<<<1, 32, 0, s>>>(bound_keys);
@@ -287,7 +308,7 @@ cudaError_t launch_mesh_bounds(const float* xyz, uint32_t nV, uint32_t* bound_ke
     return cudaGetLastError();
 }
 
-cudaError_t launch_leaf_morton(const uint32_t* tri, const float* xyz, uint32_t nT, const uint32_t* bound_keys,
+cudaError_t launch_leaf_morton(const uint32_t* tri, const float4* xyz, uint32_t nT, const uint32_t* bound_keys,
                                uint32_t* codes, uint32_t* idx, cudaStream_t s)
 {
     note_launches(1);

@@ -93,9 +93,10 @@ __device__ __forceinline__ bool tri_intersect_exact(const V3& P1, const V3& P2, 
     return true;
 }
 
-__device__ __forceinline__ V3 load_vertex(const float* __restrict__ xyz, uint32_t v)
+__device__ __forceinline__ V3 load_vertex(const float4* __restrict__ pos, uint32_t v)
 {
-    return V3{__ldg(xyz + 3 * (size_t)v), __ldg(xyz + 3 * (size_t)v + 1), __ldg(xyz + 3 * (size_t)v + 2)};
+    const float4 p = __ldg(pos + v);
+    return V3{p.x, p.y, p.z};
 }
 
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred, uint32_t lane)
@@ -155,8 +156,8 @@ __device__ __forceinline__ void test_candidates(const DetectArgs& a, const uint6
         const TreeView& TB = a.trees[pv.b];
         const uint4 fa = __ldg(TA.face + bvtt_a(c));
         const uint4 fb = __ldg(TB.face + bvtt_b(c));
-        hit = tri_intersect_exact(load_vertex(TA.xyz, fa.x), load_vertex(TA.xyz, fa.y), load_vertex(TA.xyz, fa.z),
-                                  load_vertex(TB.xyz, fb.x), load_vertex(TB.xyz, fb.y), load_vertex(TB.xyz, fb.z));
+        hit = tri_intersect_exact(load_vertex(TA.pos, fa.x), load_vertex(TA.pos, fa.y), load_vertex(TA.pos, fa.z),
+                                  load_vertex(TB.pos, fb.x), load_vertex(TB.pos, fb.y), load_vertex(TB.pos, fb.z));
         rec = make_uint4(pv.a, pv.b, fa.w, fb.w);
     }
     const uint32_t pos = warp_append(a.counts + kCountHits, hit, lane);

@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
 #include <new>
 #include <string>
@@ -181,8 +182,9 @@ struct oibvh_tree_s {
     int device = 0;
     uint32_t nV = 0, nT = 0;
     TreeShape shape{};
-    DevBuf<float> xyz;          // owned positions (3 * nV)
-    const float* cur_xyz = nullptr;  // positions of the last build/refit
+    DevBuf<float> xyz;          // staging for positions given as xyz (3 * nV)
+    DevBuf<float4> pos4;        // owned positions in the device layout (x, y, z, 0)
+    const float4* cur_pos = nullptr;  // positions the next refit / detect use (owned or borrowed)
     DevBuf<uint32_t> tri;       // faces as given (3 * nT)
     DevBuf<uint4> face;         // Morton-ordered faces (v0, v1, v2, original index)
     DevBuf<float4> box;         // 2 * (size - nT): internal nodes only
@@ -194,7 +196,7 @@ struct oibvh_tree_s {
         RefitJob j{};
         j.box = box.p;
         j.face = face.p;
-        j.xyz = cur_xyz;
+        j.pos = cur_pos;
         j.shape = shape;
         j.block_begin = 0;
         j.n_blocks = refit_blocks_for(nT);
@@ -206,6 +208,7 @@ struct oibvh_tree_s {
 static int tree_alloc(oibvh_tree_t t)
 {
     OK_TRY(t->xyz.ensure(3 * (size_t)t->nV, "cudaMalloc(positions)"));
+    OK_TRY(t->pos4.ensure((size_t)t->nV, "cudaMalloc(positions)"));
     OK_TRY(t->tri.ensure(3 * (size_t)t->nT, "cudaMalloc(faces)"));
     OK_TRY(t->face.ensure(t->nT, "cudaMalloc(sorted faces)"));
     OK_TRY(t->box.ensure(2 * (size_t)std::max(1u, t->shape.size - t->nT), "cudaMalloc(tree)"));
@@ -240,13 +243,15 @@ static int tree_create_impl(const float* xyz, uint32_t nV, const uint32_t* tri, 
     if (st == OIBVH_OK) {
         cudaError_t e = cudaMemcpy(t->xyz.p, xyz, 3 * (size_t)nV * sizeof(float), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemcpy(t->tri.p, tri, 3 * (size_t)nT * sizeof(uint32_t), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = launch_xyz_to_pos4(t->xyz.p, nV, t->pos4.p, 0);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(0);
         if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpy(mesh)");
     }
     if (st != OIBVH_OK) {
         delete t;
         return st;
     }
-    t->cur_xyz = t->xyz.p;
+    t->cur_pos = t->pos4.p;
     *out = t;
     return OIBVH_OK;
 }
@@ -265,9 +270,8 @@ static int tree_build_impl(oibvh_tree_t t, cudaStream_t s)
     uint32_t* keys6 = (uint32_t*)scratch.p;
     uint32_t* codes = (uint32_t*)(scratch.p + codes_off);
     uint32_t* idx = (uint32_t*)(scratch.p + idx_off);
-    t->cur_xyz = t->xyz.p;
-    CUDA_TRY(launch_mesh_bounds(t->xyz.p, t->nV, keys6, sm_count(t->device), s));
-    CUDA_TRY(launch_leaf_morton(t->tri.p, t->xyz.p, nT, keys6, codes, idx, s));
+    CUDA_TRY(launch_mesh_bounds(t->cur_pos, t->nV, keys6, sm_count(t->device), s));
+    CUDA_TRY(launch_leaf_morton(t->tri.p, t->cur_pos, nT, keys6, codes, idx, s));
     CUDA_TRY(launch_radix_sort(codes, idx, nT, 30, scratch.p + sort_off, s));
     CUDA_TRY(launch_gather_faces(t->tri.p, idx, nT, t->face.p, s));
     CUDA_TRY(launch_refit_one(t->job(), s));
@@ -382,7 +386,7 @@ int upload_views(oibvh_scene_s* s, cudaStream_t st)
         TreeView v{};
         v.box = t->box.p;
         v.face = t->face.p;
-        v.xyz = t->cur_xyz;
+        v.pos = t->cur_pos;
         v.shape = t->shape;
         v.nV = t->nV;
         s->h_views.p[i] = v;
@@ -606,6 +610,8 @@ API int oibvh_tree_create_copy(oibvh_tree_t other, const float* xyz, uint32_t n_
     int st = tree_alloc(t);
     if (st == OIBVH_OK) {
         cudaError_t e = cudaMemcpy(t->xyz.p, xyz, 3 * (size_t)t->nV * sizeof(float), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = launch_xyz_to_pos4(t->xyz.p, t->nV, t->pos4.p, 0);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(0);
         if (e == cudaSuccess)
             e = cudaMemcpy(t->tri.p, other->tri.p, 3 * (size_t)t->nT * sizeof(uint32_t), cudaMemcpyDeviceToDevice);
         if (e == cudaSuccess)
@@ -619,7 +625,7 @@ API int oibvh_tree_create_copy(oibvh_tree_t other, const float* xyz, uint32_t n_
         delete t;
         return st;
     }
-    t->cur_xyz = t->xyz.p;
+    t->cur_pos = t->pos4.p;
     t->built = true;  // the copied boxes describe `other`'s positions until refit
     *out = t;
     return OIBVH_OK;
@@ -633,6 +639,29 @@ API int oibvh_tree_build(oibvh_tree_t t, void* stream)
     GUARD_END
 }
 
+// Positions as given (xyz, host or device) into the tree's own device layout.
+static int stage_xyz(oibvh_tree_t t, const float* xyz, bool on_device, cudaStream_t s)
+{
+    const float* src = xyz;
+    if (!on_device) {
+        CUDA_TRY(cudaMemcpyAsync(t->xyz.p, xyz, 3 * (size_t)t->nV * sizeof(float), cudaMemcpyHostToDevice, s));
+        src = t->xyz.p;
+    }
+    CUDA_TRY(launch_xyz_to_pos4(src, t->nV, t->pos4.p, s));
+    t->cur_pos = t->pos4.p;
+    return OIBVH_OK;
+}
+
+static int check_device_ptr(const void* p, size_t align)
+{
+    cudaPointerAttributes attr{};
+    CUDA_TRY(cudaPointerGetAttributes(&attr, p));
+    if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
+        return fail(OIBVH_ERR_ARG, "pointer is not device memory");
+    if (((uintptr_t)p) % align) return fail(OIBVH_ERR_ARG, "pointer is not aligned to " + std::to_string(align));
+    return OIBVH_OK;
+}
+
 API int oibvh_tree_refit(oibvh_tree_t t, const float* xyz, void* stream)
 {
     GUARD_BEGIN
@@ -640,9 +669,7 @@ API int oibvh_tree_refit(oibvh_tree_t t, const float* xyz, void* stream)
     if (!t->built) return fail(OIBVH_ERR_STATE, "refit before build");
     DeviceGuard g(t->device);
     cudaStream_t s = (cudaStream_t)stream;
-    if (xyz)
-        CUDA_TRY(cudaMemcpyAsync(t->xyz.p, xyz, 3 * (size_t)t->nV * sizeof(float), cudaMemcpyHostToDevice, s));
-    t->cur_xyz = t->xyz.p;
+    if (xyz) OK_TRY(stage_xyz(t, xyz, false, s));
     CUDA_TRY(launch_refit_one(t->job(), s));
     return OIBVH_OK;
     GUARD_END
@@ -654,11 +681,8 @@ API int oibvh_tree_refit_device(oibvh_tree_t t, const float* d_xyz, void* stream
     if (!t || !d_xyz) return fail(OIBVH_ERR_ARG, "tree or d_xyz is NULL");
     if (!t->built) return fail(OIBVH_ERR_STATE, "refit before build");
     DeviceGuard g(t->device);
-    cudaPointerAttributes attr{};
-    CUDA_TRY(cudaPointerGetAttributes(&attr, d_xyz));
-    if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
-        return fail(OIBVH_ERR_ARG, "d_xyz is not device memory");
-    t->cur_xyz = d_xyz;
+    OK_TRY(check_device_ptr(d_xyz, 4));
+    OK_TRY(stage_xyz(t, d_xyz, true, (cudaStream_t)stream));
     CUDA_TRY(launch_refit_one(t->job(), (cudaStream_t)stream));
     return OIBVH_OK;
     GUARD_END
@@ -669,23 +693,27 @@ API int oibvh_tree_set_positions(oibvh_tree_t t, const float* xyz, void* stream)
     GUARD_BEGIN
     if (!t || !xyz) return fail(OIBVH_ERR_ARG, "tree or xyz is NULL");
     DeviceGuard g(t->device);
-    CUDA_TRY(cudaMemcpyAsync(t->xyz.p, xyz, 3 * (size_t)t->nV * sizeof(float), cudaMemcpyHostToDevice,
-                             (cudaStream_t)stream));
-    t->cur_xyz = t->xyz.p;
-    return OIBVH_OK;
+    return stage_xyz(t, xyz, false, (cudaStream_t)stream);
     GUARD_END
 }
 
-API int oibvh_tree_set_positions_device(oibvh_tree_t t, const float* d_xyz)
+API int oibvh_tree_set_positions_device(oibvh_tree_t t, const float* d_xyz, void* stream)
 {
     GUARD_BEGIN
     if (!t || !d_xyz) return fail(OIBVH_ERR_ARG, "tree or d_xyz is NULL");
     DeviceGuard g(t->device);
-    cudaPointerAttributes attr{};
-    CUDA_TRY(cudaPointerGetAttributes(&attr, d_xyz));
-    if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
-        return fail(OIBVH_ERR_ARG, "d_xyz is not device memory");
-    t->cur_xyz = d_xyz;
+    OK_TRY(check_device_ptr(d_xyz, 4));
+    return stage_xyz(t, d_xyz, true, (cudaStream_t)stream);
+    GUARD_END
+}
+
+API int oibvh_tree_set_positions4_device(oibvh_tree_t t, const float* d_xyzw)
+{
+    GUARD_BEGIN
+    if (!t || !d_xyzw) return fail(OIBVH_ERR_ARG, "tree or d_xyzw is NULL");
+    DeviceGuard g(t->device);
+    OK_TRY(check_device_ptr(d_xyzw, 16));
+    t->cur_pos = (const float4*)d_xyzw;
     return OIBVH_OK;
     GUARD_END
 }
@@ -710,7 +738,7 @@ API int oibvh_tree_get_aabbs(oibvh_tree_t t, float* out6, uint64_t cap_nodes)
         // leaves are not stored: rebuild them from the faces and positions
         DevBuf<float4> leaves;
         OK_TRY(leaves.ensure(2 * (size_t)t->nT, "cudaMalloc(leaf boxes)"));
-        CUDA_TRY(launch_leaf_boxes(t->face.p, t->cur_xyz, t->nT, leaves.p, 0));
+        CUDA_TRY(launch_leaf_boxes(t->face.p, t->cur_pos, t->nT, leaves.p, 0));
         CUDA_TRY(cudaMemcpy(tmp.data() + 2 * internal, leaves.p, 2 * (size_t)t->nT * sizeof(float4),
                             cudaMemcpyDeviceToHost));
     }

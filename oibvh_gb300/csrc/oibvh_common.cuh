@@ -108,7 +108,7 @@ struct TreeShape {
 struct TreeView {
     float4* box;        // 2*(size-nT) float4: level-ordered real internal nodes
     const uint4* face;  // Morton-sorted faces: (v0, v1, v2, original face index)
-    const float* xyz;   // 3 floats per vertex
+    const float4* pos;  // vertex positions, (x, y, z, unused) per vertex
     TreeShape shape;
     uint32_t nV;
     uint32_t pad0;
@@ -150,24 +150,20 @@ __device__ __forceinline__ Box merge(const Box& l, const Box& r)
 }
 
 // Box of one face (v0, v1, v2, .): glm::min(glm::min(v0, v1), v2) and the
-// max likewise, as calculate_aabb_kernel (src/cuda/oibvh.cu:24-40).
-__device__ __forceinline__ Box leaf_box(const float* __restrict__ xyz, uint4 f)
+// max likewise, as calculate_aabb_kernel (src/cuda/oibvh.cu:24-40); one
+// 16-byte load per vertex.
+__device__ __forceinline__ Box leaf_box(const float4* __restrict__ pos, uint4 f)
 {
-    const float ax = __ldg(xyz + 3 * (size_t)f.x), ay = __ldg(xyz + 3 * (size_t)f.x + 1),
-                az = __ldg(xyz + 3 * (size_t)f.x + 2);
-    const float bx = __ldg(xyz + 3 * (size_t)f.y), by = __ldg(xyz + 3 * (size_t)f.y + 1),
-                bz = __ldg(xyz + 3 * (size_t)f.y + 2);
-    const float cx = __ldg(xyz + 3 * (size_t)f.z), cy = __ldg(xyz + 3 * (size_t)f.z + 1),
-                cz = __ldg(xyz + 3 * (size_t)f.z + 2);
-    return Box{gmin(gmin(ax, bx), cx), gmin(gmin(ay, by), cy), gmin(gmin(az, bz), cz),
-               gmax(gmax(ax, bx), cx), gmax(gmax(ay, by), cy), gmax(gmax(az, bz), cz)};
+    const float4 a = __ldg(pos + f.x), b = __ldg(pos + f.y), c = __ldg(pos + f.z);
+    return Box{gmin(gmin(a.x, b.x), c.x), gmin(gmin(a.y, b.y), c.y), gmin(gmin(a.z, b.z), c.z),
+               gmax(gmax(a.x, b.x), c.x), gmax(gmax(a.y, b.y), c.y), gmax(gmax(a.z, b.z), c.z)};
 }
 
 // Box of a node given by implicit index and level: internal nodes are read
 // from the tree (32 B, two float4), leaves are rebuilt from their face.
 __device__ __forceinline__ Box node_box(const TreeView& T, uint32_t implicit, uint32_t level)
 {
-    if (level == T.shape.L) return leaf_box(T.xyz, __ldg(T.face + implicit - ((1u << level) - 1u)));
+    if (level == T.shape.L) return leaf_box(T.pos, __ldg(T.face + implicit - ((1u << level) - 1u)));
     const float4* p = T.box + 2 * (size_t)T.shape.real_index(implicit);
     const float4 a = __ldg(p), b = __ldg(p + 1);
     return Box{a.x, a.y, a.z, b.x, b.y, b.z};

@@ -16,7 +16,7 @@ void note_launches(uint64_t n);
 struct RefitJob {
     float4* box;           // internal nodes
     const uint4* face;
-    const float* xyz;
+    const float4* pos;
     TreeShape shape;
     uint32_t block_begin;  // first CTA of this tree in the launch
     uint32_t n_blocks;
@@ -26,8 +26,9 @@ struct RefitJob {
 
 // build_kernels.cu
 size_t radix_sort_scratch_bytes(uint32_t n);
-cudaError_t launch_mesh_bounds(const float* xyz, uint32_t nV, uint32_t* bound_keys, int num_sms, cudaStream_t s);
-cudaError_t launch_leaf_morton(const uint32_t* tri, const float* xyz, uint32_t nT, const uint32_t* bound_keys,
+cudaError_t launch_xyz_to_pos4(const float* xyz, uint32_t nV, float4* pos, cudaStream_t s);
+cudaError_t launch_mesh_bounds(const float4* pos, uint32_t nV, uint32_t* bound_keys, int num_sms, cudaStream_t s);
+cudaError_t launch_leaf_morton(const uint32_t* tri, const float4* pos, uint32_t nT, const uint32_t* bound_keys,
                                uint32_t* codes, uint32_t* idx, cudaStream_t s);
 cudaError_t launch_radix_sort(uint32_t* keys, uint32_t* vals, uint32_t n, int key_bits, void* scratch,
                               cudaStream_t s);
@@ -37,7 +38,7 @@ cudaError_t launch_gather_faces(const uint32_t* tri, const uint32_t* perm, uint3
 uint32_t refit_blocks_for(uint32_t nT);
 uint32_t refit_counters_per_tree();
 cudaError_t launch_refit_one(const RefitJob& job, cudaStream_t s);
-cudaError_t launch_leaf_boxes(const uint4* face, const float* xyz, uint32_t nT, float4* out, cudaStream_t s);
+cudaError_t launch_leaf_boxes(const uint4* face, const float4* pos, uint32_t nT, float4* out, cudaStream_t s);
 cudaError_t launch_refit(const RefitJob* d_jobs, uint32_t n_jobs, uint32_t total_blocks, uint32_t* d_counters,
                          size_t n_counters, cudaStream_t s);
 

@@ -126,7 +126,7 @@ __device__ __forceinline__ void reduce_block(Box v[4], const TreeShape& S, float
 }
 
 // `jobs` == nullptr: a single tree passed by value in `one`.
-__global__ void __launch_bounds__(kRefitThreads) k_refit(const RefitJob* __restrict__ jobs, uint32_t n_jobs,
+__global__ void __launch_bounds__(kRefitThreads, 5) k_refit(const RefitJob* __restrict__ jobs, uint32_t n_jobs,
                                                          const RefitJob one)
 {
     __shared__ Box sm8[8];
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(kRefitThreads) k_refit(const RefitJob* __restr
     for (int k = 0; k < 4; ++k) f[k] = (leaf0 + k < S.nT) ? __ldg(job.face + leaf0 + k) : make_uint4(0, 0, 0, 0);
     Box v[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) v[k] = leaf_box(job.xyz, f[k]);
+    for (int k = 0; k < 4; ++k) v[k] = leaf_box(job.pos, f[k]);
 
     uint32_t levels = min((uint32_t)kRefitLog, S.L);
     reduce_block(v, S, job.box, S.L, chunk << kRefitLog, levels, sm8);
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(kRefitThreads) k_refit(const RefitJob* __restr
 }
 
 // Leaf boxes of one tree as float4 pairs (for oibvh_tree_get_aabbs).
-__global__ void __launch_bounds__(256) k_leaf_boxes(const uint4* __restrict__ face, const float* __restrict__ xyz,
+__global__ void __launch_bounds__(256) k_leaf_boxes(const uint4* __restrict__ face, const float4* __restrict__ xyz,
                                                     uint32_t nT, float4* __restrict__ out)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -225,7 +225,7 @@ cudaError_t launch_refit(const RefitJob* d_jobs, uint32_t n_jobs, uint32_t total
     return cudaGetLastError();
 }
 
-cudaError_t launch_leaf_boxes(const uint4* face, const float* xyz, uint32_t nT, float4* out, cudaStream_t s)
+cudaError_t launch_leaf_boxes(const uint4* face, const float4* xyz, uint32_t nT, float4* out, cudaStream_t s)
 {
     note_launches(1);
     k_leaf_boxes<<<(nT + 255) / 256, 256, 0, s>>>(face, xyz, nT, out);

@@ -144,3 +144,25 @@ def test_stream_argument(gpu):
     s = torch.cuda.Stream()
     sc.detectCollision(DeviceType.GPU0, 4, 3, stream=s)
     assert np.array_equal(sc.int_tri_pairs(), g["hits"][0])
+
+
+def test_positions_xyzw_in_place(gpu):
+    """oibvh_tree_set_positions4_device: 16-byte (x, y, z, w) records used in place."""
+    import torch
+
+    from oibvh_gb300 import DeviceType
+
+    g = load_golden("deforming")
+    sc, trees = _scene(g["meshes"])
+    fr = g["frames"][0]
+    dev = [torch.nn.functional.pad(torch.from_numpy(np.ascontiguousarray(x)), (0, 1)).contiguous().cuda() for x in fr]
+    for t, d in zip(trees, dev):
+        t.set_positions4_device(d.data_ptr())
+    sc.refit()
+    sc.detectCollision(DeviceType.GPU0, 4, 3)
+    assert np.array_equal(sc.int_tri_pairs(), g["hits"][1])
+    # misaligned pointer is refused
+    from oibvh_gb300 import OibvhError
+
+    with pytest.raises(OibvhError):
+        trees[0].set_positions4_device(dev[0].data_ptr() + 4)
