@@ -9,9 +9,8 @@
 //     per thread: it loads the four 16-byte face records and the twelve
 //     vertices with independent loads, builds the leaf boxes in registers,
 //     reduces two levels inside the thread, five across the warp (shuffles)
-//     and three across the CTA (eight boxes through shared memory), staging
-//     the 1023 nodes it produces in shared memory and writing them to HBM
-//     level by level with contiguous float4 stores;
+//     and three across the CTA (eight boxes through shared memory), writing
+//     every internal node it produces;
 //   * the CTA finishing last among a group of 1024 sibling subtree roots
 //     (one atomic counter per group, threadfence-reduction pattern) loads
 //     the group and climbs the next 10 levels the same way, up to the root.
@@ -38,6 +37,12 @@ __device__ __forceinline__ Box shfl_down(const Box& b, int d)
                __shfl_down_sync(0xffffffffu, b.xy, d), __shfl_down_sync(0xffffffffu, b.xz, d)};
 }
 
+__device__ __forceinline__ void store_node(float4* box, uint32_t real, const Box& b)
+{
+    box[2 * (size_t)real] = make_float4(b.nx, b.ny, b.nz, 0.0f);
+    box[2 * (size_t)real + 1] = make_float4(b.xx, b.xy, b.xz, 0.0f);
+}
+
 __device__ __forceinline__ Box load_node_cg(const float4* box, uint32_t real)
 {
     const float4 a = __ldcg(box + 2 * (size_t)real);
@@ -45,63 +50,58 @@ __device__ __forceinline__ Box load_node_cg(const float4* box, uint32_t real)
     return Box{a.x, a.y, a.z, c.x, c.y, c.z};
 }
 
-// Shared-memory staging of the nodes one CTA produces: the k-th level above
-// the block (k = 1..10) holds 1024 >> k nodes at entries [1024 - (2048 >> k),
-// ...), two float4 each. The block's nodes are written to HBM afterwards,
-// one level at a time, with contiguous float4 stores (full 32-byte sectors).
-__device__ __forceinline__ void stage_node(float4* st, uint32_t k, uint32_t j, const Box& b)
-{
-    const uint32_t o = (1024u - (2048u >> k)) + j;
-    st[2 * o] = make_float4(b.nx, b.ny, b.nz, 0.0f);
-    st[2 * o + 1] = make_float4(b.xx, b.xy, b.xz, 0.0f);
-}
-
 // Reduce the 1024-node block whose four nodes per thread are v[0..3] (level
 // `lvl`, global indices base + 4*tid + k, real when < level_count(lvl)) by
-// `levels` levels into the staging buffer: two levels inside the thread,
-// five across the warp (shuffles), three across the CTA.
-__device__ __forceinline__ void reduce_block(Box v[4], const TreeShape& S, uint32_t lvl, uint32_t base,
-                                             uint32_t levels, Box* sm8, float4* st)
+// `levels` levels, writing each produced node. Thread 0 ends holding the
+// block root (level lvl - levels, index base >> levels).
+__device__ __forceinline__ void reduce_block(Box v[4], const TreeShape& S, float4* box, uint32_t lvl, uint32_t base,
+                                             uint32_t levels, Box* sm8)
 {
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     uint32_t cnt = S.level_count(lvl);
     uint32_t idx = base + 4 * tid;  // index of v[0]
-    uint32_t k = 0;                 // levels done
-    if (k < levels) {
+    uint32_t done = 0;
+    // two levels inside the thread
+    if (done < levels) {
+        const uint32_t off = S.level_offset(lvl - 1);
         const Box n0 = (idx + 1 < cnt) ? merge(v[0], v[1]) : v[0];
         const Box n1 = (idx + 3 < cnt) ? merge(v[2], v[3]) : v[2];
-        ++k;
-        stage_node(st, k, 2 * tid, n0);
-        stage_node(st, k, 2 * tid + 1, n1);
+        if (idx < cnt) store_node(box, off + (idx >> 1), n0);
+        if (idx + 2 < cnt) store_node(box, off + (idx >> 1) + 1, n1);
         v[0] = n0;
         v[1] = n1;
         cnt = (cnt + 1) >> 1;
         idx >>= 1;
+        --lvl;
+        ++done;
     }
-    if (k < levels) {
+    if (done < levels) {
+        const uint32_t off = S.level_offset(lvl - 1);
         const Box n0 = (idx + 1 < cnt) ? merge(v[0], v[1]) : v[0];
-        ++k;
-        stage_node(st, k, tid, n0);
+        if (idx < cnt) store_node(box, off + (idx >> 1), n0);
         v[0] = n0;
         cnt = (cnt + 1) >> 1;
+        --lvl;
+        ++done;
     }
     // five levels across the warp: lane holds node idx0 + lane (idx0 = base/4 + 32*warp)
     const uint32_t idx0 = (base >> 2) + 32 * warp;
 #pragma unroll
     for (int s = 0; s < 5; ++s) {
-        if (k < levels) {  // uniform over the CTA
+        if (done < levels) {  // uniform over the CTA
             const Box r = shfl_down(v[0], 1 << s);
             const uint32_t j = (idx0 + lane) >> s;  // this lane's node (when lane % 2^(s+1) == 0)
-            ++k;
             if ((lane & ((2u << s) - 1u)) == 0) {
                 if (j + 1 < cnt) v[0] = merge(v[0], r);
-                stage_node(st, k, (j >> 1) - (base >> k), v[0]);
+                if (j < cnt) store_node(box, S.level_offset(lvl - 1) + (j >> 1), v[0]);
             }
             cnt = (cnt + 1) >> 1;
+            --lvl;
+            ++done;
         }
     }
     // three levels across the CTA: the 8 warp roots
-    if (k < levels) {
+    if (done < levels) {
         if (lane == 0) sm8[warp] = v[0];
         __syncthreads();
         if (warp == 0) {
@@ -109,33 +109,19 @@ __device__ __forceinline__ void reduce_block(Box v[4], const TreeShape& S, uint3
             const uint32_t b0 = base >> 7;  // index of warp 0's root
 #pragma unroll
             for (int s = 0; s < 3; ++s) {
-                if (k < levels) {
+                if (done < levels) {
                     const Box r = shfl_down(v[0], 1 << s);
                     const uint32_t j = (b0 + lane) >> s;
-                    ++k;
                     if (lane < 8 && (lane & ((2u << s) - 1u)) == 0) {
                         if (j + 1 < cnt) v[0] = merge(v[0], r);
-                        stage_node(st, k, (j >> 1) - (base >> k), v[0]);
+                        if (j < cnt) store_node(box, S.level_offset(lvl - 1) + (j >> 1), v[0]);
                     }
                     cnt = (cnt + 1) >> 1;
+                    --lvl;
+                    ++done;
                 }
             }
         }
-    }
-}
-
-// Write the staged nodes of the block (levels lvl-1 .. lvl-levels) to HBM.
-__device__ __forceinline__ void flush_block(const float4* st, float4* box, const TreeShape& S, uint32_t lvl,
-                                            uint32_t base, uint32_t levels)
-{
-    for (uint32_t k = 1; k <= levels; ++k) {
-        const uint32_t l = lvl - k;
-        const uint32_t first = base >> k, lc = S.level_count(l);
-        if (first >= lc) break;
-        const uint32_t n = min(1024u >> k, lc - first);
-        const float4* src = st + 2 * (1024u - (2048u >> k));
-        float4* dst = box + 2 * (size_t)(S.level_offset(l) + first);
-        for (uint32_t i = threadIdx.x; i < 2 * n; i += kRefitThreads) dst[i] = src[i];
     }
 }
 
@@ -145,7 +131,6 @@ __global__ void __launch_bounds__(kRefitThreads, 5) k_refit(const RefitJob* __re
 {
     __shared__ Box sm8[8];
     __shared__ uint32_t s_last;
-    __shared__ float4 st[2 * 1023];
 
     RefitJob job = one;
     if (jobs != nullptr) {
@@ -171,9 +156,7 @@ __global__ void __launch_bounds__(kRefitThreads, 5) k_refit(const RefitJob* __re
     for (int k = 0; k < 4; ++k) v[k] = leaf_box(job.pos, f[k]);
 
     uint32_t levels = min((uint32_t)kRefitLog, S.L);
-    reduce_block(v, S, S.L, chunk << kRefitLog, levels, sm8, st);
-    __syncthreads();
-    flush_block(st, job.box, S, S.L, chunk << kRefitLog, levels);
+    reduce_block(v, S, job.box, S.L, chunk << kRefitLog, levels, sm8);
     uint32_t lvl = S.L - levels;
     if (lvl == 0) return;
 
@@ -182,9 +165,8 @@ __global__ void __launch_bounds__(kRefitThreads, 5) k_refit(const RefitJob* __re
     for (int stage = 0;; ++stage) {
         const uint32_t g = idx >> kRefitLog;
         const uint32_t gcnt = min((uint32_t)kRefitChunk, S.level_count(lvl) - (g << kRefitLog));
-        __threadfence();  // every thread: its flushed nodes are visible before the arrival
-        __syncthreads();
         if (threadIdx.x == 0) {
+            __threadfence();
             const uint32_t old = atomicAdd(job.counters + stage * kStageCounters + g, 1u);
             s_last = (old == gcnt - 1) ? 1u : 0u;
         }
@@ -200,9 +182,7 @@ __global__ void __launch_bounds__(kRefitThreads, 5) k_refit(const RefitJob* __re
             v[k] = (j < cnt) ? load_node_cg(job.box, off + j) : Box{0, 0, 0, 0, 0, 0};
         }
         levels = min((uint32_t)kRefitLog, lvl);
-        reduce_block(v, S, lvl, base, levels, sm8, st);
-        __syncthreads();
-        flush_block(st, job.box, S, lvl, base, levels);
+        reduce_block(v, S, job.box, lvl, base, levels, sm8);
         lvl -= levels;
         if (lvl == 0) return;
         idx = g;
