@@ -199,6 +199,38 @@ int oibvh_scene_get_stats(oibvh_scene_t s, oibvh_detect_stats* out);
 
 int oibvh_scene_destroy(oibvh_scene_t s);
 
+/* ------------------------------------------------------- no allocation */
+
+/* Collision detection for ONE mesh pair (tree a against tree b) that
+ * allocates nothing: no device memory, no pinned host memory. This entry
+ * point has no counterpart in the reference; it exists for callers that must
+ * not allocate while they run: a frame loop with a hard budget (cudaMalloc
+ * synchronises the whole device), an application whose device memory belongs
+ * to an outside pool allocator, or work issued while a CUDA graph capture in
+ * global mode is under way on another stream (cudaMalloc is illegal then).
+ *
+ * The traversal runs the same kernels as oibvh_scene_detect over a fixed
+ * scratch area compiled into the library: about 4 MB of device memory held on
+ * every GPU that loads the library until the process exits, with room for
+ * 262,144 queued node pairs per work list. A pair that needs more returns
+ * OIBVH_ERR_OVERFLOW (use oibvh_scene_detect, which grows its queues); an
+ * entry_level whose starting cross product exceeds 64 x 262,144 node pairs is
+ * rejected with OIBVH_ERR_ARG.
+ *
+ * Inputs: two built trees on the same device (created beforehand). Output:
+ * up to out_cap records {0, 1, triA, triB} (original face indices; 0 and 1
+ * name a and b) written to the DEVICE buffer d_out4; *n_hits receives the
+ * number of colliding pairs, also when it exceeds out_cap (then the call
+ * returns OIBVH_ERR_OVERFLOW). Blocking.
+ *
+ * The first call on a device resolves the scratch address (cudaGetSymbolAddress
+ * with that device current) and caches it: make that first call before any
+ * stream capture. All calls share the one scratch area and overwrite it;
+ * calls whose GPU work overlaps (different host threads or streams) race and
+ * must be serialised by the caller. */
+int oibvh_pair_detect_noalloc(oibvh_tree_t a, oibvh_tree_t b, uint32_t entry_level, uint32_t* d_out4,
+                              uint32_t out_cap, uint32_t* n_hits, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

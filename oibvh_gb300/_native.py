@@ -77,6 +77,7 @@ SIGNATURES = [
     ("oibvh_scene_set_queue_capacity", ctypes.c_int, [_vp, _u32, _u32, _u32]),
     ("oibvh_scene_get_stats", ctypes.c_int, [_vp, ctypes.POINTER(DetectStats)]),
     ("oibvh_scene_destroy", ctypes.c_int, [_vp]),
+    ("oibvh_pair_detect_noalloc", ctypes.c_int, [_vp, _vp, _u32, _vp, _u32, _u32p, _vp]),
 ]
 
 _lib = None

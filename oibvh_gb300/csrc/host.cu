@@ -974,3 +974,26 @@ API int oibvh_scene_destroy(oibvh_scene_t s)
     }
     return OIBVH_OK;
 }
+
+// ============================================================================
+// Used by oibvh_pair_detect_noalloc (noalloc.cu)
+// ============================================================================
+namespace oibvh {
+
+int tree_device_view(oibvh_tree_t t, TreeView* out, int* device, bool* built)
+{
+    TreeView v{};
+    v.box = t->box.p;
+    v.face = t->face.p;
+    v.pos = t->cur_pos;
+    v.shape = t->shape;
+    v.nV = t->nV;
+    *out = v;
+    *device = t->device;
+    *built = t->built;
+    return OIBVH_OK;
+}
+
+int noalloc_fail(int code, const std::string& msg) { return fail(code, msg); }
+
+}  // namespace oibvh
