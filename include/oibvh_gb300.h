@@ -184,6 +184,52 @@ int oibvh_scene_get_candidates(oibvh_scene_t s, uint32_t* out4, uint64_t cap, ui
  * reruns), so this only trades memory against reruns. 0 keeps a value. */
 int oibvh_scene_set_queue_capacity(oibvh_scene_t s, uint32_t front, uint32_t candidates, uint32_t hits);
 
+/* Build every tree of the scene with one launch per build stage, whatever
+ * the number of trees (bounds, Morton codes, one stable sort by code and then
+ * by tree, gather, one refit for all): the batched form of
+ * OibvhTree::build() (src/cuda/oibvhTree.cu:237-388). Trees may be added
+ * unbuilt for this. Blocking. */
+int oibvh_scene_build(oibvh_scene_t s, void* stream);
+
+/* Rigid transforms of every tree on the device, one launch (the reference
+ * transforms on the host and round-trips through Transform::transformVec4,
+ * src/cuda/transform.cu:18-41, src/utils/mesh.cpp:187-214): tree i's
+ * positions become M_i * rest_i, with d_rest_xyzw the rest positions of all
+ * trees packed in tree order (16 B per vertex, 16-byte aligned) and d_mats
+ * 12 floats per tree (row-major 3x4; x' = ((m0 x + m1 y) + m2 z) + m3, each
+ * operation rounded on its own). Stream-ordered; follow with oibvh_scene_refit. */
+int oibvh_scene_transform(oibvh_scene_t s, const float* d_rest_xyzw, const float* d_mats, void* stream);
+
+/* Traversal tuning (also chosen by oibvh_scene_autotune). */
+typedef struct oibvh_tuning {
+    uint32_t start_pairs_log2;    /* start cross product ~ 2^this node pairs per pass (8..24, default 16) */
+    uint32_t handoff;             /* front width at which one CTA hands the walk to all warps (32..8192, 2048) */
+    uint32_t walk_blocks_per_sm;  /* walker CTAs per SM, 0 = as many as fit */
+    uint32_t front_capacity;      /* starting work-list capacity (entries), 0 = keep */
+    uint32_t hit_capacity;        /* starting hit-queue capacity (records), 0 = keep */
+} oibvh_tuning;
+int oibvh_scene_set_tuning(oibvh_scene_t s, const oibvh_tuning* t);
+int oibvh_scene_get_tuning(oibvh_scene_t s, oibvh_tuning* t);
+/* Project-written autotuner: times `reps` detects of the scene's current
+ * state for each setting of a small grid (start size x handoff x walker
+ * CTAs), keeps the fastest, and sizes the queues from the observed peaks
+ * with 2x headroom. Blocking; *chosen may be NULL. */
+int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t reps, oibvh_tuning* chosen);
+
+/* A whole frame as one CUDA graph: [oibvh_scene_transform(d_rest, d_mats)]
+ * + [oibvh_scene_refit] (when refit != 0) + the detect of every pair (at most
+ * 65536 pairs, fixed number of traversal rounds, results to pinned memory).
+ * capture_frame runs one ordinary frame first (it sizes the queues with 2x
+ * headroom and uploads the tables), then captures. launch_frame replays the
+ * graph (re-capturing first if the scene or tuning changed); finish_frame
+ * waits for it and validates: if a queue overflowed, it reruns the detect the
+ * synchronous way and marks the graph for re-capture, so results are always
+ * complete. Matrix contents at d_mats may change between launches. */
+int oibvh_scene_capture_frame(oibvh_scene_t s, uint32_t entry_level, uint32_t expand_levels, int refit,
+                              const float* d_rest_xyzw, const float* d_mats, void* stream);
+int oibvh_scene_launch_frame(oibvh_scene_t s, void* stream);
+int oibvh_scene_finish_frame(oibvh_scene_t s, void* stream);
+
 /* Per-detect diagnostics: passes, BVTT steps, queue regrowths, nodes tested. */
 typedef struct oibvh_detect_stats {
     uint32_t passes;         /* pair batches */

@@ -43,6 +43,16 @@ class DetectStats(ctypes.Structure):
     ]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [
+        ("start_pairs_log2", ctypes.c_uint32),
+        ("handoff", ctypes.c_uint32),
+        ("walk_blocks_per_sm", ctypes.c_uint32),
+        ("front_capacity", ctypes.c_uint32),
+        ("hit_capacity", ctypes.c_uint32),
+    ]
+
+
 # (name, restype, argtypes) for every symbol of include/oibvh_gb300.h
 SIGNATURES = [
     ("oibvh_status_string", ctypes.c_char_p, [ctypes.c_int]),
@@ -70,6 +80,14 @@ SIGNATURES = [
     ("oibvh_scene_broad", ctypes.c_int, [_vp, ctypes.c_int, _u32, _u32, _vp]),
     ("oibvh_scene_narrow", ctypes.c_int, [_vp, _vp]),
     ("oibvh_scene_refit", ctypes.c_int, [_vp, _vp]),
+    ("oibvh_scene_build", ctypes.c_int, [_vp, _vp]),
+    ("oibvh_scene_transform", ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    ("oibvh_scene_set_tuning", ctypes.c_int, [_vp, ctypes.POINTER(Tuning)]),
+    ("oibvh_scene_get_tuning", ctypes.c_int, [_vp, ctypes.POINTER(Tuning)]),
+    ("oibvh_scene_autotune", ctypes.c_int, [_vp, _u32, _u32, ctypes.POINTER(Tuning)]),
+    ("oibvh_scene_capture_frame", ctypes.c_int, [_vp, _u32, _u32, ctypes.c_int, _vp, _vp, _vp]),
+    ("oibvh_scene_launch_frame", ctypes.c_int, [_vp, _vp]),
+    ("oibvh_scene_finish_frame", ctypes.c_int, [_vp, _vp]),
     ("oibvh_scene_get_int_tri_pair_count", _u32, [_vp]),
     ("oibvh_scene_get_candidate_count", _u64, [_vp]),
     ("oibvh_scene_get_int_tri_pairs", ctypes.c_int, [_vp, _u32p, _u64, ctypes.POINTER(_u64)]),

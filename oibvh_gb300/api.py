@@ -231,6 +231,47 @@ class Scene:
         """Refit every tree of the scene in one launch (to the positions set last)."""
         N.check(N.lib().oibvh_scene_refit(self._h, _stream_handle(stream)), "oibvh_scene_refit")
 
+    def build(self, stream=None) -> None:
+        """Build every tree of the scene, one launch per build stage."""
+        N.check(N.lib().oibvh_scene_build(self._h, _stream_handle(stream)), "oibvh_scene_build")
+
+    def transform(self, d_rest_xyzw_ptr: int, d_mats_ptr: int, stream=None) -> None:
+        """Tree i's positions = M_i * rest_i (packed xyzw rest positions, 12 floats per matrix)."""
+        N.check(N.lib().oibvh_scene_transform(self._h, ctypes.c_void_p(int(d_rest_xyzw_ptr)),
+                                              ctypes.c_void_p(int(d_mats_ptr)), _stream_handle(stream)),
+                "oibvh_scene_transform")
+
+    def set_tuning(self, **kw) -> None:
+        t = N.Tuning()
+        N.check(N.lib().oibvh_scene_get_tuning(self._h, ctypes.byref(t)), "oibvh_scene_get_tuning")
+        for k, v in kw.items():
+            setattr(t, k, int(v))
+        N.check(N.lib().oibvh_scene_set_tuning(self._h, ctypes.byref(t)), "oibvh_scene_set_tuning")
+
+    def tuning(self) -> dict:
+        t = N.Tuning()
+        N.check(N.lib().oibvh_scene_get_tuning(self._h, ctypes.byref(t)), "oibvh_scene_get_tuning")
+        return {k: int(getattr(t, k)) for k, _ in N.Tuning._fields_}
+
+    def autotune(self, entryLevel: int = 0, reps: int = 3) -> dict:
+        t = N.Tuning()
+        N.check(N.lib().oibvh_scene_autotune(self._h, int(entryLevel), int(reps), ctypes.byref(t)),
+                "oibvh_scene_autotune")
+        return {k: int(getattr(t, k)) for k, _ in N.Tuning._fields_}
+
+    def capture_frame(self, entryLevel: int = 0, expandLevels: int = 1, refit: bool = True,
+                      d_rest_xyzw_ptr: int | None = None, d_mats_ptr: int | None = None, stream=None) -> None:
+        r = ctypes.c_void_p(int(d_rest_xyzw_ptr)) if d_rest_xyzw_ptr else ctypes.c_void_p(None)
+        m = ctypes.c_void_p(int(d_mats_ptr)) if d_mats_ptr else ctypes.c_void_p(None)
+        N.check(N.lib().oibvh_scene_capture_frame(self._h, int(entryLevel), int(expandLevels), int(bool(refit)), r, m,
+                                                  _stream_handle(stream)), "oibvh_scene_capture_frame")
+
+    def launch_frame(self, stream=None) -> None:
+        N.check(N.lib().oibvh_scene_launch_frame(self._h, _stream_handle(stream)), "oibvh_scene_launch_frame")
+
+    def finish_frame(self, stream=None) -> None:
+        N.check(N.lib().oibvh_scene_finish_frame(self._h, _stream_handle(stream)), "oibvh_scene_finish_frame")
+
     def getIntTriPairCount(self) -> int:
         return int(N.lib().oibvh_scene_get_int_tri_pair_count(self._h))
 

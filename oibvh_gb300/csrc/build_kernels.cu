@@ -352,4 +352,174 @@ cudaError_t launch_gather_faces(const uint32_t* tri, const uint32_t* perm, uint3
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Multi-tree build: every stage is one launch for all trees of a scene. A CTA
+// finds its tree with a binary search over the jobs' first-CTA numbers.
+// Faces of all trees are numbered globally (tree t owns [face_off, +nT)); one
+// stable sort by Morton code followed by one stable sort by tree id gives,
+// per tree, the order of the single-tree build: (code, original index).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t find_job(const BuildJob* jobs, uint32_t n, uint32_t block, bool faces)
+{
+    uint32_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        const uint32_t b = faces ? jobs[mid].fblock_begin : jobs[mid].vblock_begin;
+        if (b <= block) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_bounds_init_multi(const BuildJob* __restrict__ jobs, uint32_t n_jobs)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_jobs) return;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        jobs[j].bound_keys[k] = 0xffffffffu;
+        jobs[j].bound_keys[3 + k] = 0u;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_mesh_bounds_multi(const BuildJob* __restrict__ jobs, uint32_t n_jobs)
+{
+    const uint32_t j = find_job(jobs, n_jobs, blockIdx.x, false);
+    const BuildJob job = jobs[j];
+    const uint32_t v = (blockIdx.x - job.vblock_begin) * blockDim.x + threadIdx.x;
+    uint32_t mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu};
+    uint32_t mx[3] = {0u, 0u, 0u};
+    if (v < job.nV) {
+        const float4 p = __ldg(job.pos + v);
+        const float c[3] = {p.x, p.y, p.z};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) mn[k] = mx[k] = float_to_ordered(c[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        for (int s = 16; s > 0; s >>= 1) {
+            mn[k] = min(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], s));
+            mx[k] = max(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], s));
+        }
+    }
+    if ((threadIdx.x & 31) == 0 && (v - (threadIdx.x & 31)) < job.nV) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            atomicMin(job.bound_keys + k, mn[k]);
+            atomicMax(job.bound_keys + 3 + k, mx[k]);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_leaf_morton_multi(const BuildJob* __restrict__ jobs, uint32_t n_jobs,
+                                                           uint32_t* __restrict__ codes, uint32_t* __restrict__ idx,
+                                                           uint32_t* __restrict__ tree_of)
+{
+    const uint32_t j = find_job(jobs, n_jobs, blockIdx.x, true);
+    const BuildJob job = jobs[j];
+    const uint32_t i = (blockIdx.x - job.fblock_begin) * blockDim.x + threadIdx.x;
+    if (i >= job.nT) return;
+    float bmin[3], bmax[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        bmin[k] = ordered_to_float(job.bound_keys[k]);
+        bmax[k] = ordered_to_float(job.bound_keys[3 + k]);
+    }
+    const uint32_t f0 = __ldg(job.tri + 3 * (size_t)i), f1 = __ldg(job.tri + 3 * (size_t)i + 1),
+                   f2 = __ldg(job.tri + 3 * (size_t)i + 2);
+    const float4 p0 = __ldg(job.pos + f0), p1 = __ldg(job.pos + f1), p2 = __ldg(job.pos + f2);
+    const float va[3] = {p0.x, p0.y, p0.z}, vb[3] = {p1.x, p1.y, p1.z}, vc[3] = {p2.x, p2.y, p2.z};
+    uint32_t q[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float mn = gmin(gmin(va[k], vb[k]), vc[k]), mx = gmax(gmax(va[k], vb[k]), vc[k]);
+        const float centroid = __fmul_rn(__fadd_rn(mn, mx), 0.5f);
+        q[k] = quant1024(__fdiv_rn(__fsub_rn(centroid, bmin[k]), __fsub_rn(bmax[k], bmin[k])));
+    }
+    const uint32_t g = job.face_off + i;
+    codes[g] = (stretch3(q[0]) << 2) | (stretch3(q[1]) << 1) | stretch3(q[2]);
+    idx[g] = g;
+    tree_of[g] = j;
+}
+
+__global__ void __launch_bounds__(256) k_gather_u32(const uint32_t* __restrict__ src, const uint32_t* __restrict__ idx,
+                                                    uint32_t n, uint32_t* __restrict__ dst)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = __ldg(src + __ldg(idx + i));
+}
+
+// Sorted position i (grouped by tree, trees in job order) -> that tree's face records.
+__global__ void __launch_bounds__(256) k_gather_faces_multi(const BuildJob* __restrict__ jobs, uint32_t n_jobs,
+                                                            const uint32_t* __restrict__ idx,
+                                                            const uint32_t* __restrict__ tree_of, uint32_t n)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t g = __ldg(idx + i);
+    const BuildJob& job = jobs[__ldg(tree_of + g)];
+    const uint32_t o = g - job.face_off;
+    job.face_out[i - job.face_off] =
+        make_uint4(__ldg(job.tri + 3 * (size_t)o), __ldg(job.tri + 3 * (size_t)o + 1), __ldg(job.tri + 3 * (size_t)o + 2), o);
+}
+
+// Rigid transforms of every tree: pos = M * rest, M a row-major 3x4 matrix per
+// tree, each product and sum rounded on its own: x' = ((m0 x + m1 y) + m2 z) + m3.
+__global__ void __launch_bounds__(256) k_transform_multi(const BuildJob* __restrict__ jobs, uint32_t n_jobs,
+                                                         const float4* __restrict__ rest,
+                                                         const float* __restrict__ mats)
+{
+    const uint32_t j = find_job(jobs, n_jobs, blockIdx.x, false);
+    const BuildJob& job = jobs[j];
+    const uint32_t v = (blockIdx.x - job.vblock_begin) * blockDim.x + threadIdx.x;
+    if (v >= job.nV) return;
+    const float4 p = __ldg(rest + job.vert_off + v);
+    const float* m = mats + 12 * (size_t)j;
+    float o[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+        o[r] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(__ldg(m + 4 * r), p.x), __fmul_rn(__ldg(m + 4 * r + 1), p.y)),
+                                   __fmul_rn(__ldg(m + 4 * r + 2), p.z)),
+                         __ldg(m + 4 * r + 3));
+    job.pos_out[v] = make_float4(o[0], o[1], o[2], 0.0f);
+}
+
+cudaError_t launch_build_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, uint32_t f_blocks,
+                               uint32_t n_faces, uint32_t tree_bits, void* scratch, cudaStream_t s)
+{
+    // scratch: codes, idx, tree_of, keys2 (4 x n_faces u32), then the sort scratch
+    uint32_t* codes = (uint32_t*)scratch;
+    uint32_t* idx = codes + n_faces;
+    uint32_t* tree_of = idx + n_faces;
+    uint32_t* keys2 = tree_of + n_faces;
+    void* sort_scratch = keys2 + n_faces;
+    note_launches(4);
+    k_bounds_init_multi<<<(n_jobs + 255) / 256, 256, 0, s>>>(d_jobs, n_jobs);
+    k_mesh_bounds_multi<<<v_blocks, 256, 0, s>>>(d_jobs, n_jobs);
+    k_leaf_morton_multi<<<f_blocks, 256, 0, s>>>(d_jobs, n_jobs, codes, idx, tree_of);
+    cudaError_t e = launch_radix_sort(codes, idx, n_faces, 30, sort_scratch, s);
+    if (e != cudaSuccess) return e;
+    k_gather_u32<<<(n_faces + 255) / 256, 256, 0, s>>>(tree_of, idx, n_faces, keys2);
+    if (tree_bits > 0) {
+        e = launch_radix_sort(keys2, idx, n_faces, (int)tree_bits, sort_scratch, s);
+        if (e != cudaSuccess) return e;
+    }
+    note_launches(1);
+    k_gather_faces_multi<<<(n_faces + 255) / 256, 256, 0, s>>>(d_jobs, n_jobs, idx, tree_of, n_faces);
+    return cudaGetLastError();
+}
+
+size_t build_multi_scratch_bytes(uint32_t n_faces)
+{
+    return 4 * (size_t)n_faces * sizeof(uint32_t) + radix_sort_scratch_bytes(n_faces);
+}
+
+cudaError_t launch_transform_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, const float4* rest,
+                                   const float* mats, cudaStream_t s)
+{
+    note_launches(1);
+    k_transform_multi<<<v_blocks, 256, 0, s>>>(d_jobs, n_jobs, rest, mats);
+    return cudaGetLastError();
+}
+
 } // namespace oibvh

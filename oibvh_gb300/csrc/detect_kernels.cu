@@ -352,7 +352,8 @@ __global__ void __launch_bounds__(kTopThreads) k_top(DetectArgs a)
     const uint32_t n0 = min(a.counts[kCountWork0], a.work_cap);
     uint32_t tested = 0;
     // the start list fits the front buffer, or goes straight to the walkers
-    if (n0 > kHandoff) {
+    const uint32_t handoff = a.handoff ? min(a.handoff, kTopCap) : kHandoff;
+    if (n0 > handoff) {
         for (uint32_t i = threadIdx.x; i < n0; i += kTopThreads) out[i] = __ldcg(a.work[0] + i);
         if (threadIdx.x == 0) *out_cnt = n0;
         return;
@@ -363,7 +364,7 @@ __global__ void __launch_bounds__(kTopThreads) k_top(DetectArgs a)
     while (c > 0) {
         uint64_t* fc = cur ? s_dyn + kTopCap : s_dyn;
         uint64_t* fn = cur ? s_dyn : s_dyn + kTopCap;
-        if (c > kHandoff) {
+        if (c > handoff) {
             // wide enough: hand the front to the walkers
             for (uint32_t i = threadIdx.x; i < c; i += kTopThreads) out[i] = fc[i];
             if (threadIdx.x == 0) *out_cnt = c;

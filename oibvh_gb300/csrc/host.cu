@@ -309,11 +309,36 @@ struct oibvh_scene_s {
     std::vector<RefitJob> refit_cache;
     uint32_t refit_blocks = 0;
 
+    // multi-tree build / transform: job table for the current tree list
+    DevBuf<BuildJob> build_jobs;
+    DevBuf<uint32_t> bound_keys;
+    std::vector<BuildJob> build_cache;
+    uint32_t v_blocks = 0, f_blocks = 0, n_faces = 0, n_verts = 0;
+
+    // tuning (oibvh_scene_set_tuning / oibvh_scene_autotune)
+    uint32_t tune_start_log2 = 16;  // start cross product ~ 2^this node pairs per pass
+    uint32_t tune_handoff = 2048;   // front width at which k_top hands over to the walkers
+    uint32_t tune_walk_per_sm = 0;  // walker CTAs per SM, 0 = as many as fit
+
+    // captured frame (CUDA graph): [transform] + refit + detect
+    cudaGraphExec_t frame_exec = nullptr;
+    bool frame_stale = true;
+    uint32_t frame_entry = 0, frame_expand = 1, frame_rounds = 3, frame_kernels = 0;
+    bool frame_refit = true;
+    const float4* frame_rest = nullptr;
+    const float* frame_mats = nullptr;
+    PinnedBuf<uint32_t> h_frame_counts;
+
     uint64_t hit_count = 0;
     uint64_t cand_count = 0;
     bool cands_valid = false;    // candidates of a single pass are on the device
     std::vector<PairView> last_pairs;
     oibvh_detect_stats stats{};
+
+    ~oibvh_scene_s()
+    {
+        if (frame_exec) cudaGraphExecDestroy(frame_exec);
+    }
 };
 
 namespace {
@@ -339,7 +364,8 @@ void list_pairs(const oibvh_scene_s* s, std::vector<uint32_t>& out)
 }
 
 // Start level of each pair: the reference's entry level, deepened so that
-// the start cross product holds about 2^16 node pairs over the pass (the
+// the start cross product holds about 2^tune_start_log2 (default 2^16) node
+// pairs over the pass (the
 // pair set does not depend on it; a deeper start gives the traversal enough
 // independent work for every SM).
 int plan_pass(const oibvh_scene_s* s, const uint32_t* pr, uint32_t n, uint32_t entry, PassPlan& plan)
@@ -347,7 +373,8 @@ int plan_pass(const oibvh_scene_s* s, const uint32_t* pr, uint32_t n, uint32_t e
     plan.pv.resize(n);
     plan.front0 = 0;
     const uint32_t lg = ilog2(std::max(1u, n));
-    const uint32_t auto_level = lg >= 16 ? 0u : (16u - lg) / 2u;
+    const uint32_t target = s->tune_start_log2;
+    const uint32_t auto_level = lg >= target ? 0u : (target - lg) / 2u;
     for (uint32_t p = 0; p < n; ++p) {
         const TreeShape& A = s->trees[pr[2 * p]]->shape;
         const TreeShape& B = s->trees[pr[2 * p + 1]]->shape;
@@ -395,6 +422,13 @@ int upload_views(oibvh_scene_s* s, cudaStream_t st)
     return OIBVH_OK;
 }
 
+int walk_grid(const oibvh_scene_s* s)
+{
+    const int fit = walk_blocks_per_sm();
+    const int per = s->tune_walk_per_sm ? std::min<int>(fit, (int)s->tune_walk_per_sm) : fit;
+    return sm_count(s->device) * std::max(1, per);
+}
+
 // Broad phase (+ narrow phase when `narrow`) over every pair, pass by pass.
 int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expand, bool narrow, cudaStream_t st)
 {
@@ -406,6 +440,20 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
     for (auto t : s->trees)
         if (!t->built) return fail(OIBVH_ERR_STATE, "every tree must be built before detect");
     DeviceGuard g(s->device);
+    struct StaleIfMoved {
+        oibvh_scene_s* s;
+        const void* p[6];
+        explicit StaleIfMoved(oibvh_scene_s* sc)
+            : s(sc), p{sc->front0.p, sc->front1.p, sc->hits.p, sc->counts.p, sc->pairv.p, sc->views.p}
+        {
+        }
+        ~StaleIfMoved()
+        {
+            const void* q[6] = {s->front0.p, s->front1.p, s->hits.p, s->counts.p, s->pairv.p, s->views.p};
+            for (int i = 0; i < 6; ++i)
+                if (p[i] != q[i]) s->frame_stale = true;
+        }
+    } stale_guard(s);
     s->stats = oibvh_detect_stats{};
     s->hit_count = 0;
     s->cand_count = 0;
@@ -420,7 +468,7 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
     OK_TRY(upload_views(s, st));
     OK_TRY(s->hits.ensure(s->hit_cap, "cudaMalloc(hits)"));
 
-    const int grid = sm_count(s->device) * walk_blocks_per_sm();
+    const int grid = walk_grid(s);
     for (uint32_t p0 = 0; p0 < n_pairs; p0 += kMaxPairsPerPass) {
         const uint32_t np = std::min(kMaxPairsPerPass, n_pairs - p0);
         PassPlan plan;
@@ -458,6 +506,7 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
             a.counts = s->counts.p;
             a.fuse_narrow = narrow ? 1u : 0u;
             a.grid = grid;
+            a.handoff = s->tune_handoff;
             CUDA_TRY(launch_init_front(a, (uint32_t)plan.front0, st));
             CUDA_TRY(launch_top(a, st));
             uint32_t rounds = 1;  // list 1 is the first walk round's input
@@ -806,8 +855,10 @@ API int oibvh_scene_add_tree(oibvh_scene_t s, oibvh_tree_t t, uint32_t* id)
     GUARD_BEGIN
     if (!s || !t) return fail(OIBVH_ERR_ARG, "scene or tree is NULL");
     if (t->device != s->device) return fail(OIBVH_ERR_ARG, "tree lives on another device");
-    if (!t->built) return fail(OIBVH_ERR_STATE, "addOibvhTree needs a built tree (src/cuda/scene.cu:97)");
+    // the reference asserts a built tree (src/cuda/scene.cu:97); here a tree may
+    // also be added unbuilt and built with the others by oibvh_scene_build
     s->trees.push_back(t);
+    s->frame_stale = true;
     if (id) *id = (uint32_t)(s->trees.size() - 1);
     return OIBVH_OK;
     GUARD_END
@@ -820,6 +871,7 @@ API int oibvh_scene_set_pairs(oibvh_scene_t s, const uint32_t* pairs, uint32_t n
     if (!pairs) {
         s->all_pairs = true;
         s->pairs.clear();
+        s->frame_stale = true;
         return OIBVH_OK;
     }
     for (uint32_t i = 0; i < n_pairs; ++i)
@@ -827,6 +879,7 @@ API int oibvh_scene_set_pairs(oibvh_scene_t s, const uint32_t* pairs, uint32_t n
             return fail(OIBVH_ERR_ARG, "pair " + std::to_string(i) + " is not two distinct trees of this scene");
     s->all_pairs = false;
     s->pairs.assign(pairs, pairs + 2 * (size_t)n_pairs);
+    s->frame_stale = true;
     return OIBVH_OK;
     GUARD_END
 }
@@ -955,6 +1008,7 @@ API int oibvh_scene_set_queue_capacity(oibvh_scene_t s, uint32_t front, uint32_t
         s->hits.release();
         s->hit_count = 0;
     }
+    s->frame_stale = true;  // a captured frame points at the released buffers
     return OIBVH_OK;
 }
 
@@ -997,3 +1051,351 @@ int tree_device_view(oibvh_tree_t t, TreeView* out, int* device, bool* built)
 int noalloc_fail(int code, const std::string& msg) { return fail(code, msg); }
 
 }  // namespace oibvh
+
+// ============================================================================
+// Multi-tree build, transforms, tuning and the captured frame
+// ============================================================================
+namespace {
+
+// (Re)build the job table of the multi-tree build / transform launches.
+int ensure_build_jobs(oibvh_scene_s* s, cudaStream_t st)
+{
+    const size_t n = s->trees.size();
+    std::vector<BuildJob> jobs(n);
+    uint32_t vb = 0, fb = 0, fo = 0, vo = 0;
+    OK_TRY(s->bound_keys.ensure(6 * std::max<size_t>(n, 1), "cudaMalloc(bounds)"));
+    for (size_t i = 0; i < n; ++i) {
+        const oibvh_tree_t t = s->trees[i];
+        BuildJob j{};
+        j.pos = t->cur_pos;
+        j.tri = t->tri.p;
+        j.face_out = t->face.p;
+        j.bound_keys = s->bound_keys.p + 6 * i;
+        j.pos_out = t->pos4.p;
+        j.nV = t->nV;
+        j.nT = t->nT;
+        j.vblock_begin = vb;
+        j.fblock_begin = fb;
+        j.face_off = fo;
+        j.vert_off = vo;
+        vb += (t->nV + 255) / 256;
+        fb += (t->nT + 255) / 256;
+        if ((uint64_t)fo + t->nT > 0xffffffffull || (uint64_t)vo + t->nV > 0xffffffffull)
+            return fail(OIBVH_ERR_ARG, "the scene holds more than 2^32 faces or vertices");
+        fo += t->nT;
+        vo += t->nV;
+        jobs[i] = j;
+    }
+    s->v_blocks = vb;
+    s->f_blocks = fb;
+    s->n_faces = fo;
+    s->n_verts = vo;
+    bool same = s->build_cache.size() == n && s->build_jobs.p;
+    for (size_t i = 0; same && i < n; ++i) same = std::memcmp(&jobs[i], &s->build_cache[i], sizeof(BuildJob)) == 0;
+    if (!same) {
+        OK_TRY(s->build_jobs.ensure(std::max<size_t>(n, 1), "cudaMalloc(build jobs)"));
+        CUDA_TRY(cudaMemcpyAsync(s->build_jobs.p, jobs.data(), n * sizeof(BuildJob), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaStreamSynchronize(st));  // jobs is a pageable host vector
+        s->build_cache = jobs;
+    }
+    return OIBVH_OK;
+}
+
+}  // namespace
+
+API int oibvh_scene_build(oibvh_scene_t s, void* stream)
+{
+    GUARD_BEGIN
+    if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
+    if (s->trees.empty()) return OIBVH_OK;
+    DeviceGuard g(s->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    OK_TRY(ensure_build_jobs(s, st));
+    DevBuf<uint8_t> scratch;
+    OK_TRY(scratch.ensure(build_multi_scratch_bytes(s->n_faces), "cudaMalloc(build scratch)"));
+    const uint32_t n = (uint32_t)s->trees.size();
+    const uint32_t tree_bits = n <= 1 ? 0u : ilog2(next_pow2(n));
+    CUDA_TRY(launch_build_multi(s->build_jobs.p, n, s->v_blocks, s->f_blocks, s->n_faces, tree_bits, scratch.p, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    for (auto t : s->trees) t->built = true;
+    const int r = oibvh_scene_refit(s, stream);
+    if (r != OIBVH_OK) return r;
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return OIBVH_OK;
+    GUARD_END
+}
+
+API int oibvh_scene_transform(oibvh_scene_t s, const float* d_rest_xyzw, const float* d_mats, void* stream)
+{
+    GUARD_BEGIN
+    if (!s || !d_rest_xyzw || !d_mats) return fail(OIBVH_ERR_ARG, "scene, rest or mats is NULL");
+    if (s->trees.empty()) return OIBVH_OK;
+    if (((uintptr_t)d_rest_xyzw) % 16) return fail(OIBVH_ERR_ARG, "rest positions must be 16-byte aligned");
+    DeviceGuard g(s->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    for (auto t : s->trees) t->cur_pos = t->pos4.p;  // the transform writes each tree's own positions
+    OK_TRY(ensure_build_jobs(s, st));
+    CUDA_TRY(launch_transform_multi(s->build_jobs.p, (uint32_t)s->trees.size(), s->v_blocks,
+                                    (const float4*)d_rest_xyzw, d_mats, st));
+    return OIBVH_OK;
+    GUARD_END
+}
+
+API int oibvh_scene_set_tuning(oibvh_scene_t s, const oibvh_tuning* t)
+{
+    if (!s || !t) return fail(OIBVH_ERR_ARG, "scene or tuning is NULL");
+    if (t->start_pairs_log2 < 8 || t->start_pairs_log2 > 24) return fail(OIBVH_ERR_ARG, "start_pairs_log2 in 8..24");
+    if (t->handoff < 32 || t->handoff > 8192) return fail(OIBVH_ERR_ARG, "handoff in 32..8192");
+    s->tune_start_log2 = t->start_pairs_log2;
+    s->tune_handoff = t->handoff;
+    s->tune_walk_per_sm = t->walk_blocks_per_sm;
+    if (t->front_capacity) s->front_cap = std::min<uint32_t>(t->front_capacity, 0x7fffffffu);
+    if (t->hit_capacity) s->hit_cap = std::min<uint32_t>(t->hit_capacity, 0x7fffffffu);
+    s->frame_stale = true;
+    return OIBVH_OK;
+}
+
+API int oibvh_scene_get_tuning(oibvh_scene_t s, oibvh_tuning* t)
+{
+    if (!s || !t) return fail(OIBVH_ERR_ARG, "scene or tuning is NULL");
+    t->start_pairs_log2 = s->tune_start_log2;
+    t->handoff = s->tune_handoff;
+    t->walk_blocks_per_sm = s->tune_walk_per_sm;
+    t->front_capacity = s->front_cap;
+    t->hit_capacity = s->hit_cap;
+    return OIBVH_OK;
+}
+
+// Times `reps` detects per candidate setting with CUDA events and keeps the
+// fastest; queue capacities are set from the observed peaks with headroom so
+// that timed frames never regrow.
+API int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t reps, oibvh_tuning* chosen)
+{
+    GUARD_BEGIN
+    if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
+    if (reps == 0) reps = 3;
+    DeviceGuard g(s->device);
+    const uint32_t starts[] = {12, 14, 16, 18, 20};
+    const uint32_t handoffs[] = {512, 2048, 8192};
+    const int fit = walk_blocks_per_sm();
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    float best = 1e30f;
+    oibvh_tuning bt{};
+    int st = OIBVH_OK;
+    // warm-up sizes the queues
+    st = detect_impl(s, s->device, entry_level, 1, true, 0);
+    for (uint32_t sl : starts) {
+        for (uint32_t h : handoffs) {
+            for (int per = std::max(1, fit / 2); per <= fit && st == OIBVH_OK; per += std::max(1, fit / 2)) {
+                s->tune_start_log2 = sl;
+                s->tune_handoff = h;
+                s->tune_walk_per_sm = (uint32_t)per;
+                st = detect_impl(s, s->device, entry_level, 1, true, 0);
+                if (st != OIBVH_OK) break;
+                float tot = 0.0f;
+                for (uint32_t r = 0; r < reps && st == OIBVH_OK; ++r) {
+                    cudaEventRecord(e0, 0);
+                    st = detect_impl(s, s->device, entry_level, 1, true, 0);
+                    cudaEventRecord(e1, 0);
+                    cudaEventSynchronize(e1);
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    tot += ms;
+                }
+                if (st == OIBVH_OK && tot < best) {
+                    best = tot;
+                    bt.start_pairs_log2 = sl;
+                    bt.handoff = h;
+                    bt.walk_blocks_per_sm = (uint32_t)per;
+                }
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != OIBVH_OK) return st;
+    s->tune_start_log2 = bt.start_pairs_log2;
+    s->tune_handoff = bt.handoff;
+    s->tune_walk_per_sm = bt.walk_blocks_per_sm;
+    // capacities: the largest work list and hit count seen, doubled
+    st = detect_impl(s, s->device, entry_level, 1, true, 0);
+    if (st != OIBVH_OK) return st;
+    s->front_cap = grow_cap(2 * s->stats.front_peak, s->front_cap);
+    if (s->hit_count * 2 > s->hit_cap) {
+        const uint32_t want = grow_cap(2 * s->hit_count, s->hit_cap);
+        OK_TRY(s->hits.ensure(want, "cudaMalloc(hits)"));
+        s->hit_cap = want;
+    }
+    bt.front_capacity = s->front_cap;
+    bt.hit_capacity = s->hit_cap;
+    s->frame_stale = true;
+    if (chosen) *chosen = bt;
+    return OIBVH_OK;
+    GUARD_END
+}
+
+namespace {
+
+// Capture [transform] + refit + detect of every pair (one pass) into a graph.
+int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
+{
+    if (s->frame_exec) {
+        cudaGraphExecDestroy(s->frame_exec);
+        s->frame_exec = nullptr;
+    }
+    std::vector<uint32_t> pr;
+    list_pairs(s, pr);
+    const uint32_t np = (uint32_t)(pr.size() / 2);
+    if (np == 0) return fail(OIBVH_ERR_STATE, "no pairs to detect");
+    if (np > kMaxPairsPerPass) return fail(OIBVH_ERR_UNSUPPORTED, "a captured frame handles at most 65536 pairs");
+    // warm-up frame outside the capture: sizes every buffer and uploads the tables
+    if (s->frame_rest) OK_TRY(oibvh_scene_transform(s, (const float*)s->frame_rest, s->frame_mats, st));
+    if (s->frame_refit) OK_TRY(oibvh_scene_refit(s, st));
+    OK_TRY(detect_impl(s, s->device, s->frame_entry, s->frame_expand, true, st));
+    // headroom, then the exact tables the graph will read
+    s->front_cap = std::max(s->front_cap, grow_cap(2 * s->stats.front_peak, s->front_cap));
+    OK_TRY(s->front0.ensure(s->front_cap, "cudaMalloc(work list)"));
+    OK_TRY(s->front1.ensure(s->front_cap, "cudaMalloc(work list)"));
+    if (s->hit_count * 2 > s->hit_cap) {
+        const uint32_t want = grow_cap(2 * s->hit_count, s->hit_cap);
+        OK_TRY(s->hits.ensure(want, "cudaMalloc(hits)"));
+        s->hit_cap = want;
+    }
+    OK_TRY(s->h_frame_counts.ensure(kCountTotal, "cudaMallocHost(frame counts)"));
+    PassPlan plan;
+    OK_TRY(plan_pass(s, pr.data(), np, s->frame_entry, plan));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    std::memcpy(s->h_pairs.p, plan.pv.data(), np * sizeof(PairView));
+    CUDA_TRY(cudaMemcpyAsync(s->pairv.p, s->h_pairs.p, np * sizeof(PairView), cudaMemcpyHostToDevice, st));
+    OK_TRY(upload_views(s, st));
+    if (s->frame_rest) OK_TRY(ensure_build_jobs(s, st));
+    if (s->frame_refit) OK_TRY(oibvh_scene_refit(s, st));  // refreshes the refit job table
+    CUDA_TRY(cudaStreamSynchronize(st));
+
+    DetectArgs a{};
+    a.trees = s->views.p;
+    a.pairs = s->pairv.p;
+    a.n_pairs = np;
+    a.expand_levels = 1;
+    a.work[0] = s->front0.p;
+    a.work[1] = s->front1.p;
+    a.work_cap = s->front_cap;
+    a.hits = s->hits.p;
+    a.hit_cap = s->hit_cap;
+    a.counts = s->counts.p;
+    a.fuse_narrow = 1;
+    a.grid = walk_grid(s);
+    a.handoff = s->tune_handoff;
+
+    const uint64_t launches0 = 0;
+    (void)launches0;
+    cudaGraph_t graph = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    uint32_t kernels = 0;
+    cudaError_t e = cudaSuccess;
+    if (s->frame_rest && e == cudaSuccess) {
+        e = launch_transform_multi(s->build_jobs.p, (uint32_t)s->trees.size(), s->v_blocks, s->frame_rest,
+                                   s->frame_mats, st);
+        ++kernels;
+    }
+    if (s->frame_refit && e == cudaSuccess) {
+        e = launch_refit(s->refit_jobs.p, (uint32_t)s->trees.size(), s->refit_blocks, s->refit_counters.p,
+                         refit_counters_per_tree() * s->trees.size(), st);
+        ++kernels;
+    }
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->counts.p, 0, kCountTotal * sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = launch_init_front(a, (uint32_t)plan.front0, st);
+    if (e == cudaSuccess) e = launch_top(a, st);
+    kernels += 2;
+    for (uint32_t r = 1; r <= s->frame_rounds && e == cudaSuccess; ++r) {
+        e = launch_walk(a, r, st);
+        ++kernels;
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s->h_frame_counts.p, s->counts.p, kCountTotal * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                            st);
+    const cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+    if (e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return cuda_fail(e, "capturing the frame");
+    }
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&s->frame_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        s->frame_exec = nullptr;
+        return cuda_fail(e, "cudaGraphInstantiate");
+    }
+    s->frame_kernels = kernels;
+    s->frame_stale = false;
+    s->last_pairs = plan.pv;
+    return OIBVH_OK;
+}
+
+}  // namespace
+
+API int oibvh_scene_capture_frame(oibvh_scene_t s, uint32_t entry_level, uint32_t expand_levels, int refit,
+                                  const float* d_rest_xyzw, const float* d_mats, void* stream)
+{
+    GUARD_BEGIN
+    if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
+    if (expand_levels < 1 || expand_levels > 16) return fail(OIBVH_ERR_ARG, "expand_levels must be in 1..16");
+    if ((d_rest_xyzw == nullptr) != (d_mats == nullptr)) return fail(OIBVH_ERR_ARG, "give both rest and mats, or neither");
+    for (auto t : s->trees)
+        if (!t->built) return fail(OIBVH_ERR_STATE, "every tree must be built before a frame is captured");
+    DeviceGuard g(s->device);
+    s->frame_entry = entry_level;
+    s->frame_expand = expand_levels;
+    s->frame_refit = refit != 0;
+    s->frame_rest = (const float4*)d_rest_xyzw;
+    s->frame_mats = d_mats;
+    return capture_frame_impl(s, (cudaStream_t)stream);
+    GUARD_END
+}
+
+API int oibvh_scene_launch_frame(oibvh_scene_t s, void* stream)
+{
+    GUARD_BEGIN
+    if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
+    DeviceGuard g(s->device);
+    if (s->frame_stale || !s->frame_exec) OK_TRY(capture_frame_impl(s, (cudaStream_t)stream));
+    CUDA_TRY(cudaGraphLaunch(s->frame_exec, (cudaStream_t)stream));
+    note_launches(s->frame_kernels);
+    return OIBVH_OK;
+    GUARD_END
+}
+
+API int oibvh_scene_finish_frame(oibvh_scene_t s, void* stream)
+{
+    GUARD_BEGIN
+    if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
+    DeviceGuard g(s->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_TRY(cudaStreamSynchronize(st));
+    const uint32_t* c = s->h_frame_counts.p;
+    if (!c) return fail(OIBVH_ERR_STATE, "no frame was launched");
+    if (c[kCountFlags] || c[kCountWork0 + s->frame_rounds + 1] != 0) {
+        // the captured queues were too small for this frame: redo the detect the
+        // synchronous way (the refit already ran) and capture again next frame
+        s->frame_stale = true;
+        OK_TRY(detect_impl(s, s->device, s->frame_entry, s->frame_expand, true, st));
+        s->stats.retries++;
+        return OIBVH_OK;
+    }
+    s->stats = oibvh_detect_stats{};
+    s->stats.passes = 1;
+    s->stats.steps = s->frame_rounds;
+    s->stats.nodes_tested = c[kCountTested];
+    uint64_t peak = 0;
+    for (uint32_t k = 0; k <= s->frame_rounds + 1; ++k) peak = std::max<uint64_t>(peak, c[kCountWork0 + k]);
+    s->stats.front_peak = peak;
+    s->hit_count = c[kCountHits];
+    s->cand_count = c[kCountCands];
+    s->stats.candidates = s->cand_count;
+    s->stats.hits = s->hit_count;
+    s->cands_valid = false;
+    return OIBVH_OK;
+    GUARD_END
+}

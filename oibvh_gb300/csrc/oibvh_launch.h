@@ -24,8 +24,27 @@ struct RefitJob {
     uint32_t pad0;
 };
 
+// One tree of a multi-tree build / transform launch.
+struct BuildJob {
+    const float4* pos;      // positions to build from
+    const uint32_t* tri;    // faces as given (3 * nT)
+    uint4* face_out;        // Morton-ordered face records
+    uint32_t* bound_keys;   // 6 words of scratch (mesh bounds)
+    float4* pos_out;        // transform target (the tree's own positions)
+    uint32_t nV, nT;
+    uint32_t vblock_begin;  // first CTA of this tree in vertex-chunk launches (256 vertices per CTA)
+    uint32_t fblock_begin;  // first CTA of this tree in face-chunk launches (256 faces per CTA)
+    uint32_t face_off;      // first face of this tree in the global face numbering
+    uint32_t vert_off;      // first vertex of this tree in packed rest positions
+};
+
 // build_kernels.cu
 size_t radix_sort_scratch_bytes(uint32_t n);
+size_t build_multi_scratch_bytes(uint32_t n_faces);
+cudaError_t launch_build_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, uint32_t f_blocks,
+                               uint32_t n_faces, uint32_t tree_bits, void* scratch, cudaStream_t s);
+cudaError_t launch_transform_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, const float4* rest,
+                                   const float* mats, cudaStream_t s);
 cudaError_t launch_xyz_to_pos4(const float* xyz, uint32_t nV, float4* pos, cudaStream_t s);
 cudaError_t launch_mesh_bounds(const float4* pos, uint32_t nV, uint32_t* bound_keys, int num_sms, cudaStream_t s);
 cudaError_t launch_leaf_morton(const uint32_t* tri, const float4* pos, uint32_t nT, const uint32_t* bound_keys,
@@ -57,6 +76,7 @@ struct DetectArgs {
     uint32_t* counts;      // see kCount* below
     uint32_t fuse_narrow;  // 1: test candidates in the traversal; 0: store them
     int grid;              // CTAs of the grid-stride / persistent kernels
+    uint32_t handoff;      // front width at which k_top hands over to the walkers (<= 8192)
 };
 cudaError_t launch_init_front(const DetectArgs& a, uint32_t total0, cudaStream_t s);
 cudaError_t launch_top(const DetectArgs& a, cudaStream_t s);

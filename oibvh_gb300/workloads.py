@@ -95,33 +95,112 @@ def _subdiv_probs(lo: float = 1e3, hi: float = 1e6) -> np.ndarray:
     return w / w.sum()
 
 
-def batched(n_pairs: int = 512, seed: int = 77, noise: float = 0.05, frac_lo: float = 0.3,
-            frac_hi: float = 0.7, sigma: float = 1e-3) -> PairWorkload:
+@dataclass
+class BatchWorkload:
+    """Mesh pairs placed by rigid transforms: meshes[2p] = A (identity),
+    meshes[2p+1] = B. `rest` are the untransformed meshes and `base[i]` the
+    3x4 placement of mesh i (float64); frame f rotates every B about its own
+    centre by f * spin_deg degrees around a seeded axis."""
+
+    name: str
+    rest: list
+    base: list
+    pairs: list
+    centers: list
+    axes: list
+    spin_deg: float = 0.5
+    info: dict = field(default_factory=dict)
+
+    def matrices(self, frame: int) -> np.ndarray:
+        """float32[n_meshes, 12]: row-major 3x4 transforms of every mesh at `frame`."""
+        out = np.empty((len(self.rest), 12), dtype=np.float64)
+        for i, M in enumerate(self.base):
+            if i % 2 == 1 and frame:
+                ang = math.radians(self.spin_deg * frame)
+                R = _axis_angle(self.axes[i], ang)
+                c = self.centers[i]
+                # x -> Rf (M x - c) + c, composed in float64
+                Rm = R @ M[:, :3]
+                t = R @ (M[:, 3] - c) + c
+                M = np.concatenate([Rm, t[:, None]], 1)
+            out[i] = M.reshape(-1)
+        return out.astype(np.float32)
+
+    def positions(self, frame: int) -> list:
+        """Transformed float32 positions, computed as the device does:
+        x' = ((m0 x + m1 y) + m2 z) + m3 with float32 rounding at each step."""
+        mats = self.matrices(frame)
+        res = []
+        for m, M in zip(self.rest, mats):
+            x, y, z = (m.xyz[:, k] for k in range(3))
+            rows = []
+            for r in range(3):
+                a = (M[4 * r] * x + M[4 * r + 1] * y) + M[4 * r + 2] * z
+                rows.append((a + M[4 * r + 3]).astype(np.float32))
+            res.append(np.stack(rows, 1))
+        return res
+
+    def packed_rest_xyzw(self) -> np.ndarray:
+        return np.concatenate([np.pad(m.xyz, ((0, 0), (0, 1))) for m in self.rest], 0).astype(np.float32)
+
+
+def _axis_angle(axis, ang):
+    x, y, z = axis
+    c, s = math.cos(ang), math.sin(ang)
+    C = 1 - c
+    return np.array([[c + x * x * C, x * y * C - z * s, x * z * C + y * s],
+                     [y * x * C + z * s, c + y * y * C, y * z * C - x * s],
+                     [z * x * C - y * s, z * y * C + x * s, c + z * z * C]], dtype=np.float64)
+
+
+def batched(n_pairs: int = 512, seed: int = 77, noise: float = 0.05, frac_lo: float = 0.3, frac_hi: float = 0.7,
+            subdivs=_BATCH_SUBDIVS, variants: int = 4) -> BatchWorkload:
+    """`n_pairs` pairs of noise-displaced icospheres, subdivision drawn so that
+    triangle counts are log-uniform over 1k..1M (s = 3..7); B has radius
+    U(0.6, 1) and sits where 30..70% of its surface lies inside A.
+    (`variants` noise fields per subdivision are generated and reused.)"""
     rng = np.random.Generator(np.random.PCG64(seed))
     probs = _subdiv_probs()
+    if tuple(subdivs) != _BATCH_SUBDIVS:
+        probs = np.ones(len(subdivs)) / len(subdivs)
     cache = {}
 
-    def sphere(s):
-        if s not in cache:
-            cache[s] = M.icosphere(s)
-        return cache[s]
+    def mesh(s, k):
+        if (s, k) not in cache:
+            cache[(s, k)] = noise_displace_mesh(s, noise, seed * 1000 + 10 * s + k)
+        return cache[(s, k)]
 
-    meshes, pairs, fracs = [], [], []
+    rest, base, pairs, centers, axes, fracs = [], [], [], [], [], []
     for p in range(n_pairs):
-        sa, sb = (int(x) for x in rng.choice(_BATCH_SUBDIVS, size=2, p=probs))
+        sa, sb = (int(x) for x in rng.choice(subdivs, size=2, p=probs))
+        ka, kb = (int(x) for x in rng.integers(0, variants, 2))
         rb = float(rng.uniform(0.6, 1.0))
         frac = float(rng.uniform(frac_lo, frac_hi))
-        a = M.noise_displace(sphere(sa), noise, seed=seed * 100000 + 2 * p)
-        b0 = M.noise_displace(sphere(sb), noise * rb, seed=seed * 100000 + 2 * p + 1)
-        b0 = M.Mesh((b0.xyz.astype(np.float64) * rb).astype(np.float32), b0.tri)
+        a = mesh(sa, ka)
+        b0 = mesh(sb, kb)
+        b = M.Mesh((b0.xyz.astype(np.float64) * rb).astype(np.float32), b0.tri)
         d = distance_for_overlap(1.0, rb, frac)
-        b = M.rigid_transform(b0, M.random_rotation(rng), _unit_vector(rng) * d)
-        meshes += [a, b]
+        R = M.random_rotation(rng)
+        t = _unit_vector(rng) * d
+        rest += [a, b]
+        base += [np.concatenate([np.eye(3), np.zeros((3, 1))], 1), np.concatenate([R, t[:, None]], 1)]
+        centers += [np.zeros(3), t.copy()]
+        axes += [np.array([0.0, 0.0, 1.0]), _unit_vector(rng)]
         pairs.append((2 * p, 2 * p + 1))
         fracs.append(frac)
-    w = PairWorkload(f"batched: {n_pairs} pairs of noise icospheres, T log-uniform 1k-1M, 30-70% overlap",
-                     meshes, pairs, jitter_sigma=sigma, seed=seed)
-    tri = np.array([m.n_triangles for m in meshes])
-    w.info = {"n_pairs": n_pairs, "triangles_total": int(tri.sum()), "triangles_min": int(tri.min()),
-              "triangles_max": int(tri.max()), "overlap_mean": float(np.mean(fracs))}
+    tri = np.array([m.n_triangles for m in rest])
+    w = BatchWorkload(f"batched: {n_pairs} pairs of noise icospheres, T log-uniform 1k-1M, 30-70% overlap",
+                      rest, base, pairs, centers, axes)
+    w.info = {"n_pairs": n_pairs, "meshes": len(rest), "triangles_total": int(tri.sum()),
+              "triangles_min": int(tri.min()), "triangles_max": int(tri.max()),
+              "vertices_total": int(sum(m.n_vertices for m in rest)), "overlap_mean": float(np.mean(fracs))}
     return w
+
+
+_ICO_CACHE = {}
+
+
+def noise_displace_mesh(subdiv: int, amplitude: float, seed: int) -> "M.Mesh":
+    if subdiv not in _ICO_CACHE:
+        _ICO_CACHE[subdiv] = M.icosphere(subdiv)
+    return M.noise_displace(_ICO_CACHE[subdiv], amplitude, seed=seed)

@@ -1,0 +1,123 @@
+"""Batched path on the GPU: one-launch-per-stage scene build, device rigid
+transforms, many pairs per detect, the captured frame graph and the autotuner,
+each checked bit-exact against the oracle port."""
+import numpy as np
+import pytest
+
+from oracle.oracle import Port, sort_pairs
+
+pytestmark = pytest.mark.gpu
+
+
+def _workload(n_pairs=10, subdivs=(2, 3, 4), seed=5):
+    from oibvh_gb300 import workloads as W
+
+    return W.batched(n_pairs, seed=seed, subdivs=subdivs, variants=2)
+
+
+def _oracle(meshes_xyz, tris, pairs):
+    p = Port()
+    for x, t in zip(meshes_xyz, tris):
+        p.add_mesh(x, t)
+    h, c = p.detect(np.asarray(pairs, dtype=np.uint32))
+    return sort_pairs(h), c
+
+
+def _scene_from(w, build_with_scene=True):
+    from oibvh_gb300 import OibvhTree, Scene
+
+    trees = [OibvhTree(m) for m in w.rest]
+    sc = Scene()
+    for t in trees:
+        sc.addOibvhTree(t)
+    if build_with_scene:
+        sc.build()
+    else:
+        for t in trees:
+            t.build()
+    sc.set_pairs(w.pairs)
+    return sc, trees
+
+
+def test_scene_build_equals_per_tree_build(gpu):
+    w = _workload(12, subdivs=(1, 2, 3, 4))
+    sc, trees = _scene_from(w)
+    for t, m in zip(trees, w.rest):
+        aabbs, st, perm = Port.oibvh_build(m.xyz, m.tri)
+        f, p = t.sorted_faces()
+        assert np.array_equal(p, perm) and np.array_equal(f, st)
+        assert np.array_equal(t.aabb_tree().view(np.uint32), aabbs.view(np.uint32))
+
+
+def test_transform_refit_detect_vs_oracle(gpu):
+    import torch
+
+    from oibvh_gb300 import DeviceType
+
+    w = _workload(10)
+    sc, trees = _scene_from(w)
+    rest = torch.from_numpy(w.packed_rest_xyzw()).cuda()
+    for frame in (0, 3):
+        mats = torch.from_numpy(w.matrices(frame)).cuda()
+        sc.transform(rest.data_ptr(), mats.data_ptr())
+        sc.refit()
+        sc.detectCollision(DeviceType.GPU0, 0, 1)
+        pos = w.positions(frame)
+        # transform arithmetic is the documented float32 formula: leaf boxes match bit for bit
+        for t, x in zip(trees[:4], pos[:4]):
+            st, _ = t.sorted_faces()
+            assert np.array_equal(t.aabb_tree().view(np.uint32), Port.oibvh_refit(x, st).view(np.uint32))
+        want, wc = _oracle(pos, [m.tri for m in w.rest], w.pairs)
+        assert np.array_equal(sc.int_tri_pairs(), want), f"frame {frame}"
+        assert sc.candidate_count() == wc
+
+
+def test_captured_frame_graph_vs_oracle(gpu):
+    import torch
+
+    w = _workload(8, seed=9)
+    sc, trees = _scene_from(w)
+    rest = torch.from_numpy(w.packed_rest_xyzw()).cuda()
+    mats = torch.from_numpy(w.matrices(0)).cuda()
+    sc.capture_frame(0, 1, True, rest.data_ptr(), mats.data_ptr())
+    for frame in (1, 2, 5):
+        mats.copy_(torch.from_numpy(w.matrices(frame)))
+        sc.launch_frame()
+        sc.finish_frame()
+        want, wc = _oracle(w.positions(frame), [m.tri for m in w.rest], w.pairs)
+        assert np.array_equal(sc.int_tri_pairs(), want), f"frame {frame}"
+        assert sc.candidate_count() == wc
+
+
+def test_frame_graph_recovers_from_small_queues(gpu):
+    """A frame whose queues are too small is redone synchronously, never truncated."""
+    import torch
+
+    w = _workload(6, seed=11)
+    sc, trees = _scene_from(w)
+    rest = torch.from_numpy(w.packed_rest_xyzw()).cuda()
+    mats = torch.from_numpy(w.matrices(0)).cuda()
+    sc.capture_frame(0, 1, True, rest.data_ptr(), mats.data_ptr())
+    sc.set_queue_capacity(front=16, hits=8)  # invalidates the captured buffers: re-capture on launch
+    mats.copy_(torch.from_numpy(w.matrices(4)))
+    sc.launch_frame()
+    sc.finish_frame()
+    want, _ = _oracle(w.positions(4), [m.tri for m in w.rest], w.pairs)
+    assert np.array_equal(sc.int_tri_pairs(), want)
+
+
+def test_autotune_keeps_the_pair_set(gpu):
+    from oibvh_gb300 import DeviceType
+
+    w = _workload(10, seed=13)
+    sc, trees = _scene_from(w, build_with_scene=False)
+    for t, x in zip(trees, w.positions(0)):
+        t.refit(x)
+    sc.detectCollision(DeviceType.GPU0, 0, 1)
+    before = sc.int_tri_pairs()
+    chosen = sc.autotune(0, 2)
+    assert chosen["handoff"] in (512, 2048, 8192)
+    sc.detectCollision(DeviceType.GPU0, 0, 1)
+    assert np.array_equal(sc.int_tri_pairs(), before)
+    want, _ = _oracle(w.positions(0), [m.tri for m in w.rest], w.pairs)
+    assert np.array_equal(before, want)
