@@ -328,6 +328,7 @@ struct oibvh_scene_s {
     const float4* frame_rest = nullptr;
     const float* frame_mats = nullptr;
     PinnedBuf<uint32_t> h_frame_counts;
+    cudaStream_t capture_stream = nullptr;  // private stream the frame is captured on
 
     uint64_t hit_count = 0;
     uint64_t cand_count = 0;
@@ -338,6 +339,7 @@ struct oibvh_scene_s {
     ~oibvh_scene_s()
     {
         if (frame_exec) cudaGraphExecDestroy(frame_exec);
+        if (capture_stream) cudaStreamDestroy(capture_stream);
     }
 };
 
@@ -1289,8 +1291,10 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
     a.grid = walk_grid(s);
     a.handoff = s->tune_handoff;
 
-    const uint64_t launches0 = 0;
-    (void)launches0;
+    // capture on a private non-blocking stream (the legacy default stream
+    // cannot be captured); the graph is launched on the caller's stream
+    if (!s->capture_stream) CUDA_TRY(cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking));
+    st = s->capture_stream;
     cudaGraph_t graph = nullptr;
     CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     uint32_t kernels = 0;

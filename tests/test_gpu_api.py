@@ -46,8 +46,11 @@ def test_bad_arguments(gpu):
     with pytest.raises(OibvhError):
         sc.set_pairs([(0, 5)])
     unbuilt = OibvhTree(g["meshes"][0])
+    other = Scene()
+    other.addOibvhTree(unbuilt)  # allowed: oibvh_scene_build builds scene trees together
+    other.addOibvhTree(trees[0])
     with pytest.raises(OibvhError) as e:
-        Scene().addOibvhTree(unbuilt)
+        other.detectCollision(DeviceType.GPU0, 0, 1)
     assert e.value.status == 5
     with pytest.raises(OibvhError):
         unbuilt.refit()
