@@ -235,7 +235,7 @@ typedef struct oibvh_detect_stats {
     uint32_t passes;         /* pair batches */
     uint32_t steps;          /* BVTT steps of the last pass */
     uint32_t retries;        /* queue regrowths */
-    uint32_t pad0;
+    uint32_t frame_redos;    /* captured frames redone synchronously, since the scene was created */
     uint64_t nodes_tested;   /* BVTT nodes tested, all passes */
     uint64_t candidates;
     uint64_t hits;

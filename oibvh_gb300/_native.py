@@ -35,7 +35,7 @@ class DetectStats(ctypes.Structure):
         ("passes", ctypes.c_uint32),
         ("steps", ctypes.c_uint32),
         ("retries", ctypes.c_uint32),
-        ("pad0", ctypes.c_uint32),
+        ("frame_redos", ctypes.c_uint32),
         ("nodes_tested", ctypes.c_uint64),
         ("candidates", ctypes.c_uint64),
         ("hits", ctypes.c_uint64),

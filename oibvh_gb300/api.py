@@ -305,4 +305,4 @@ class Scene:
     def stats(self) -> dict:
         st = N.DetectStats()
         N.check(N.lib().oibvh_scene_get_stats(self._h, ctypes.byref(st)), "oibvh_scene_get_stats")
-        return {k: int(getattr(st, k)) for k, _ in N.DetectStats._fields_ if k != "pad0"}
+        return {k: int(getattr(st, k)) for k, _ in N.DetectStats._fields_}

@@ -323,7 +323,7 @@ struct oibvh_scene_s {
     // captured frame (CUDA graph): [transform] + refit + detect
     cudaGraphExec_t frame_exec = nullptr;
     bool frame_stale = true;
-    uint32_t frame_entry = 0, frame_expand = 1, frame_rounds = 3, frame_kernels = 0;
+    uint32_t frame_entry = 0, frame_expand = 1, frame_rounds = 3, frame_kernels = 0, frame_redos = 0;
     bool frame_refit = true;
     const float4* frame_rest = nullptr;
     const float* frame_mats = nullptr;
@@ -1018,6 +1018,7 @@ API int oibvh_scene_get_stats(oibvh_scene_t s, oibvh_detect_stats* out)
 {
     if (!s || !out) return fail(OIBVH_ERR_ARG, "scene or out is NULL");
     *out = s->stats;
+    out->frame_redos = s->frame_redos;
     return OIBVH_OK;
 }
 
@@ -1256,6 +1257,9 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
     if (s->frame_rest) OK_TRY(oibvh_scene_transform(s, (const float*)s->frame_rest, s->frame_mats, st));
     if (s->frame_refit) OK_TRY(oibvh_scene_refit(s, st));
     OK_TRY(detect_impl(s, s->device, s->frame_entry, s->frame_expand, true, st));
+    // walk rounds: the warm-up frame used steps - 1 of them; two more for headroom
+    // (a round with an empty input list returns at once)
+    s->frame_rounds = std::min(kMaxRounds - 1, std::max(3u, s->stats.steps + 1));
     // headroom, then the exact tables the graph will read
     s->front_cap = std::max(s->front_cap, grow_cap(2 * s->stats.front_peak, s->front_cap));
     OK_TRY(s->front0.ensure(s->front_cap, "cudaMalloc(work list)"));
@@ -1384,6 +1388,7 @@ API int oibvh_scene_finish_frame(oibvh_scene_t s, void* stream)
         // the captured queues were too small for this frame: redo the detect the
         // synchronous way (the refit already ran) and capture again next frame
         s->frame_stale = true;
+        s->frame_redos++;
         OK_TRY(detect_impl(s, s->device, s->frame_entry, s->frame_expand, true, st));
         s->stats.retries++;
         return OIBVH_OK;

@@ -126,12 +126,15 @@ class BatchWorkload:
             out[i] = M.reshape(-1)
         return out.astype(np.float32)
 
-    def positions(self, frame: int) -> list:
-        """Transformed float32 positions, computed as the device does:
+    def positions(self, frame: int, which=None) -> list:
+        """Transformed float32 positions of every mesh (or of the meshes listed
+        in `which`), computed as the device does:
         x' = ((m0 x + m1 y) + m2 z) + m3 with float32 rounding at each step."""
         mats = self.matrices(frame)
+        idx = range(len(self.rest)) if which is None else which
         res = []
-        for m, M in zip(self.rest, mats):
+        for i in idx:
+            m, M = self.rest[i], mats[i]
             x, y, z = (m.xyz[:, k] for k in range(3))
             rows = []
             for r in range(3):
