@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["batched", "deforming", "plain"], default="batched")
+    ap.add_argument("--workload", choices=["batched", "precision", "deforming", "plain"], default="batched")
     ap.add_argument("--pairs", type=int, default=512, help="mesh pairs of the batched workload")
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -110,17 +110,59 @@ def jitter_frames(w, n_frames, seed=5):
 
 # --------------------------------------------------------------------------- clocks
 class ClockSampler:
+    """SM clock and clock-event reasons sampled every 5 ms through NVML (read
+    only), in a thread, while the timed region runs; nvidia-smi (200 ms) when
+    the NVML library cannot be loaded."""
+
+    # nvmlClocksEventReasons bits (nvml.h)
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index):
-        self.index = index
+    def __init__(self, cuda_index):
+        self.index = self._nvml_index(cuda_index)
         self.rows = []
         self.proc = None
         self.thread = None
+        self.stop_flag = threading.Event()
+        self.nvml = None
+        self.source = None
+
+    @staticmethod
+    def _nvml_index(cuda_index):
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        ids = [v.strip() for v in vis.split(",") if v.strip()]
+        if ids and cuda_index < len(ids) and ids[cuda_index].isdigit():
+            return int(ids[cuda_index])
+        return cuda_index
+
+    def _open_nvml(self):
+        import ctypes as C
+
+        try:
+            lib = C.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return None
+            h = C.c_void_p()
+            if lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self.index), C.byref(h)) != 0:
+                return None
+            reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                lib.nvmlDeviceGetCurrentClocksThrottleReasons
+            mx = C.c_uint()
+            lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx))  # NVML_CLOCK_SM
+            return lib, h, reasons, mx.value
+        except (OSError, AttributeError):
+            return None
 
     def start(self):
+        self.nvml = self._open_nvml()
+        if self.nvml is not None:
+            self.source = "nvml 5 ms"
+            self.thread = threading.Thread(target=self._poll_nvml, daemon=True)
+            self.thread.start()
+            return
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
@@ -128,36 +170,56 @@ class ClockSampler:
         except Exception:
             self.proc = None
             return
+        self.source = "nvidia-smi 200 ms"
         self.thread = threading.Thread(target=self._read, daemon=True)
         self.thread.start()
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.rows.append([x.strip() for x in line.split(",")])
+    def _poll_nvml(self):
+        import ctypes as C
 
-    def stop(self):
-        if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except Exception:
-            self.proc.kill()
-        if self.thread:
-            self.thread.join(timeout=2)
-        sm, smax, reasons = [], [], set()
+        lib, h, reasons, mx = self.nvml
+        clk, r = C.c_uint(), C.c_ulonglong()
+        while not self.stop_flag.is_set():
+            if lib.nvmlDeviceGetClockInfo(h, 1, C.byref(clk)) == 0 and reasons(h, C.byref(r)) == 0:
+                self.rows.append((float(clk.value), float(mx), int(r.value)))
+            time.sleep(0.005)
+
+    def _read(self):
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in self.rows:
+        bits = {v: k for k, v in self.REASONS.items()}
+        for line in self.proc.stdout:
+            r = [x.strip() for x in line.split(",")]
             try:
-                sm.append(float(r[0]))
-                smax.append(float(r[1]))
+                mask = 0
+                for k, n in enumerate(names):
+                    if len(r) > 4 + k and r[4 + k].lower().startswith("active"):
+                        mask |= bits[n]
+                self.rows.append((float(r[0]), float(r[1]), mask))
             except (ValueError, IndexError):
                 continue
-            for k, n in enumerate(names):
-                if len(r) > 4 + k and r[4 + k].lower().startswith("active"):
-                    reasons.add(n)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+
+    def stop(self):
+        if self.source is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clock sampling unavailable"]}
+        self.stop_flag.set()
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        if self.nvml is not None:
+            try:
+                self.nvml[0].nvmlShutdown()
+            except Exception:
+                pass
+        rows = list(self.rows)
+        sm = [r[0] for r in rows]
+        reasons = sorted({n for r in rows for b, n in self.REASONS.items() if r[2] & b})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(r[1] for r in rows) if rows else None,
+                "sm_min_mhz": min(sm) if sm else None, "reasons": reasons, "samples": len(sm), "source": self.source}
 
 
 # --------------------------------------------------------------------------- our arm
@@ -768,13 +830,265 @@ def run_reference_batched(args, rank, world):
     }
 
 
+# --------------------------------------------------------------------------- precision workload
+def _pctl(xs, q):
+    xs = sorted(xs)
+    if not xs:
+        return None
+    k = min(len(xs) - 1, max(0, int(round(q / 100.0 * (len(xs) - 1)))))
+    return xs[k]
+
+
+def run_ours_precision(args, rank, world, local):
+    """64 pairs of 256x256-quad sine sheets, 10% of B's triangles coplanar
+    with A's or within 1e-7: every frame (identity rigid transforms uploaded,
+    transform + refit + detect as one captured CUDA graph) runs the
+    FP64-filtered triangle test. Reported beside it: the same frame with the
+    reference's float test, the float/FP64 disagreement count, frame latency
+    percentiles, and the plain path (one pair per call) with its per-query
+    latency percentiles."""
+    import ctypes as C
+
+    import torch
+
+    from oibvh_gb300 import DeviceType, OibvhTree, Scene, _native
+    from oibvh_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    dev = local
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    w = W.sheets(args.pairs if args.pairs != 512 else 64, 256)
+    n_pairs = len(w.pairs)
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    L = _native.lib()
+    trees = [OibvhTree(m, device=dev) for m in w.meshes]
+    sc = Scene(dev)
+    for t in trees:
+        sc.addOibvhTree(t)
+    sc.set_pairs(w.pairs)
+    rest = torch.from_numpy(np.concatenate([np.pad(m.xyz, ((0, 0), (0, 1))) for m in w.meshes], 0)).to(f"cuda:{dev}")
+    ident = np.tile(np.array([1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], dtype=np.float32), (len(w.meshes), 1))
+    mats = torch.from_numpy(ident).to(f"cuda:{dev}")
+    mats_pinned = torch.from_numpy(ident).pin_memory()
+    sc.build(stream=sh)
+    sc.transform(rest.data_ptr(), mats.data_ptr(), stream=sh)
+    sc.refit(stream=sh)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+    hit_buf = torch.empty((1 << 24, 4), dtype=torch.int32).pin_memory()
+
+    def measure(mode, steps, e2e=False):
+        sc.set_precision(mode)
+        sc.capture_frame(ENTRY_LEVEL, EXPAND_LEVELS, True, rest.data_ptr(), mats.data_ptr(), stream=sh)
+        d2h = 0
+        for _ in range(args.warmup):
+            sc.launch_frame(stream=sh)
+            sc.finish_frame(stream=sh)
+        barrier()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        lat = []
+        l0 = L.oibvh_get_launch_count()
+        for k in range(steps):
+            flush.fill_(k & 255)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            starts[k].record(stream)
+            if e2e:
+                mats.copy_(mats_pinned, non_blocking=True)
+            sc.launch_frame(stream=sh)
+            sc.finish_frame(stream=sh)
+            if e2e:
+                n = sc.getIntTriPairCount()
+                got = C.c_uint64()
+                cap = min(n, hit_buf.shape[0])
+                _native.check(L.oibvh_scene_get_int_tri_pairs(
+                    sc.handle, C.cast(C.c_void_p(hit_buf.data_ptr()), _native._u32p), cap, C.byref(got)),
+                    "oibvh_scene_get_int_tri_pairs")
+                d2h += 16 * cap
+            ends[k].record(stream)
+            lat.append(1e3 * (time.perf_counter() - t0))
+        barrier()
+        ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends))
+        return ms, lat, L.oibvh_get_launch_count() - l0, sc.stats(), d2h
+
+    sampler = ClockSampler(dev) if rank == 0 else None
+    if sampler:
+        sampler.start()
+    ms_f, lat_f, launches, st_f, _ = measure(_native.PRECISION_FP64_FILTERED, args.steps)
+    hits = sc.getIntTriPairCount()
+    ms_e2e, lat_e2e, _, _, d2h = measure(_native.PRECISION_FP64_FILTERED, args.steps, e2e=True)
+    clocks = sampler.stop() if sampler else None
+    got_f = sc.int_tri_pairs() if not args.no_cpu_baseline else None
+    ms_32, lat_32, _, st_32, _ = measure(_native.PRECISION_FP32, max(3, args.steps // 2))
+    hits32 = sc.getIntTriPairCount()
+
+    # the plain path: one pair per call (refit both trees + detect), each query alone
+    plain = []
+    for a, b in w.pairs:
+        ps = Scene(dev)
+        ps.addOibvhTree(trees[a])
+        ps.addOibvhTree(trees[b])
+        ps.set_precision(_native.PRECISION_FP64_FILTERED)
+        plain.append(ps)
+    for ps in plain:
+        ps.refit(stream=sh)
+        ps.detectCollision(DeviceType(dev), ENTRY_LEVEL, EXPAND_LEVELS, stream=sh)
+    barrier()
+    q_lat = []
+    tp0 = time.perf_counter()
+    for rep in range(3):
+        for ps in plain:
+            t0 = time.perf_counter()
+            ps.refit(stream=sh)
+            ps.detectCollision(DeviceType(dev), ENTRY_LEVEL, EXPAND_LEVELS, stream=sh)
+            ps.getIntTriPairCount()
+            q_lat.append(1e3 * (time.perf_counter() - t0))
+    plain_s = (time.perf_counter() - tp0) / 3
+    plain_hits = sum(ps.getIntTriPairCount() for ps in plain)
+
+    t_dev = torch.tensor([ms_f, ms_e2e], dtype=torch.float64, device=f"cuda:{dev}")
+    if dist is not None:
+        dist.all_reduce(t_dev, op=dist.ReduceOp.MAX)
+        dist.destroy_process_group()
+    ms_f, ms_e2e = float(t_dev[0]), float(t_dev[1])
+    if rank != 0:
+        return None
+    K = args.steps
+    value = K * n_pairs * world / (ms_f / 1e3)
+    line = {
+        "metric": "collision queries/s (mesh pairs through refit + broad + narrow), FP64-filtered triangle test",
+        "value": round(value, 1), "unit": "queries/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
+        "ms_per_step": round(ms_f / K, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 + f64 (filtered)", "data": "synthetic (seeded sine sheets)",
+        "config": {"workload": w.name, **w.info, "entry_level": ENTRY_LEVEL, "expand_levels": EXPAND_LEVELS,
+                   "frame": "one captured CUDA graph: identity transforms + refit all sheets + detect all pairs",
+                   "l2": "flushed between steps (256 MiB write, outside the timed events)",
+                   "parallelism": f"replicas{world}"},
+        "frame_latency_ms": {"p50": round(_pctl(lat_f, 50), 4), "p99": round(_pctl(lat_f, 99), 4),
+                             "max": round(max(lat_f), 4), "how": "host wall clock, launch to results on the host; "
+                             "every query of a frame completes with it"},
+        "fp64_filter": {"candidates": st_f["candidates"], "fp64_candidates": st_f["fp64_candidates"],
+                        "fp64_axes": st_f["fp64_axes"], "fp32_disagreements": st_f["fp32_disagreements"],
+                        "hits_fp64": hits, "hits_fp32": hits32},
+        "fp32_frame": {"queries_per_s": round(max(3, K // 2) * n_pairs / (ms_32 / 1e3), 1),
+                       "ms_per_frame": round(ms_32 / max(3, K // 2), 4),
+                       "latency_p99_ms": round(_pctl(lat_32, 99), 4)},
+        "plain_single_pair": {"queries_per_s": round(n_pairs / plain_s, 1),
+                              "latency_ms": {"p50": round(_pctl(q_lat, 50), 4), "p99": round(_pctl(q_lat, 99), 4)},
+                              "how": "each pair its own scene: refit both trees + detect, synchronous, FP64-filtered",
+                              "hits": plain_hits},
+        "batched_over_plain": round(value / (n_pairs / plain_s), 2),
+        "e2e": {"value": round(K * n_pairs * world / (ms_e2e / 1e3), 1), "unit": "queries/s",
+                "h2d_bytes_per_step": int(mats_pinned.numel() * 4), "d2h_bytes_per_step": int(d2h / max(1, K)),
+                "latency_ms": {"p50": round(_pctl(lat_e2e, 50), 4), "p99": round(_pctl(lat_e2e, 99), 4)}},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_precision(w, got_f, args.cpu_seconds)
+    return line
+
+
+def cpu_baseline_precision(w, got, seconds):
+    """The FP64 oracle on this host (1 core) over a sample of the pairs, each
+    pair set compared with the GPU's filtered result for that pair."""
+    from oracle.oracle import Port
+
+    t0 = time.perf_counter()
+    n = 0
+    mismatches = 0
+    checked = []
+    for p in _sample_pairs(w, len(w.pairs)):
+        a, b = w.pairs[p]
+        port = Port()
+        port.add_mesh(w.meshes[a].xyz, w.meshes[a].tri)
+        port.add_mesh(w.meshes[b].xyz, w.meshes[b].tri)
+        h64, _ = port.detect(fp64=True)
+        n += 1
+        mine = got[(got[:, 0] == a) & (got[:, 1] == b)][:, 2:]
+        want = {tuple(r) for r in h64[:, 2:].tolist()}
+        have = {tuple(r) for r in mine.tolist()}
+        mismatches += len(want ^ have)
+        checked.append(p)
+        if time.perf_counter() - t0 > seconds:
+            break
+    el = time.perf_counter() - t0
+    return {"value": round(n / el, 3), "unit": "queries/s", "cores": 1, "kind": "port",
+            "sample": f"{n} pair queries (build both + FP64 detect) of the {len(w.pairs)} pairs, {el:.1f} s",
+            "fp64_oracle_mismatches": mismatches, "pairs_checked": len(checked)}
+
+
+def run_reference_precision(args, rank, world):
+    """The reference CPU path over the sheets (oracle port; FP32 test, the
+    reference's arithmetic) on every host core, 1 pair per thread per step."""
+    if rank != 0:
+        return None
+    from oracle.oracle import Port
+    from oibvh_gb300 import workloads as W
+
+    w = W.sheets(64, 256)
+    threads = os.cpu_count() or 1
+    sample = _sample_pairs(w, min(len(w.pairs), threads))
+    ports = []
+    for p in sample:
+        a, b = w.pairs[p]
+        port = Port()
+        port.add_mesh(w.meshes[a].xyz, w.meshes[a].tri)
+        port.add_mesh(w.meshes[b].xyz, w.meshes[b].tri)
+        ports.append((port, a, b))
+
+    def one_step():
+        def work(k):
+            port, a, b = ports[k]
+            port.set_positions(0, w.meshes[a].xyz)
+            port.set_positions(1, w.meshes[b].xyz)
+            port.detect()
+
+        tt = [threading.Thread(target=work, args=(k,)) for k in range(len(ports))]
+        for t in tt:
+            t.start()
+        for t in tt:
+            t.join()
+
+    for _ in range(args.warmup):
+        one_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        one_step()
+    el = time.perf_counter() - t0
+    q = args.steps * len(ports)
+    value = q / el
+    return {"metric": "collision queries/s (mesh pairs through refit + broad + narrow), FP64-filtered triangle test",
+            "value": round(value, 3), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1e3 * el / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded sine sheets)",
+            "config": {"workload": w.name, **w.info, "parallelism": f"{len(ports)} host threads, 1 pair each"},
+            "impl": "reference",
+            "cpu_baseline": {"value": round(value, 3), "unit": "queries/s", "cores": len(ports), "kind": "port",
+                             "sample": f"{q} pair queries (refit both + detect, float test) over {len(ports)} pairs"},
+            "e2e": {"value": round(value, 3), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
-        line = (run_reference_batched if args.workload == "batched" else run_reference)(args, rank, world)
+        line = {"batched": run_reference_batched, "precision": run_reference_precision}.get(
+            args.workload, run_reference)(args, rank, world)
     else:
-        line = (run_ours_batched if args.workload == "batched" else run_ours)(args, rank, world, local)
+        line = {"batched": run_ours_batched, "precision": run_ours_precision}.get(
+            args.workload, run_ours)(args, rank, world, local)
     if line is not None:
         print(json.dumps(line), flush=True)
 

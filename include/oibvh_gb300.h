@@ -230,6 +230,23 @@ int oibvh_scene_capture_frame(oibvh_scene_t s, uint32_t entry_level, uint32_t ex
 int oibvh_scene_launch_frame(oibvh_scene_t s, void* stream);
 int oibvh_scene_finish_frame(oibvh_scene_t s, void* stream);
 
+/* Arithmetic of the triangle test. OIBVH_PRECISION_FP32 (the default) is
+ * the reference's float test, operation for operation (src/utils/utils.cpp:71-169):
+ * the pair set is the reference's bit for bit. OIBVH_PRECISION_FP64_FILTERED
+ * has no counterpart in the reference: every axis test is evaluated in float
+ * with a forward error bound on its two margins, and an axis whose margins
+ * lie within the bound of zero is evaluated again in FP64; the pair set then
+ * equals that of the same 17-axis test evaluated entirely in FP64 over the
+ * same float inputs. In that mode the stats also count the FP64 work and the
+ * candidates on which the float test and the FP64 test disagree. Takes
+ * effect at the next detect (a captured frame is re-captured). */
+enum {
+    OIBVH_PRECISION_FP32 = 0,
+    OIBVH_PRECISION_FP64_FILTERED = 1,
+};
+int oibvh_scene_set_precision(oibvh_scene_t s, int mode);
+int oibvh_scene_get_precision(oibvh_scene_t s);
+
 /* Per-detect diagnostics: passes, BVTT steps, queue regrowths, nodes tested. */
 typedef struct oibvh_detect_stats {
     uint32_t passes;         /* pair batches */
@@ -240,6 +257,9 @@ typedef struct oibvh_detect_stats {
     uint64_t candidates;
     uint64_t hits;
     uint64_t front_peak;     /* largest front */
+    uint64_t fp64_axes;      /* precision mode: axis tests evaluated again in FP64 */
+    uint64_t fp64_candidates;     /* precision mode: candidates with at least one such axis */
+    uint64_t fp32_disagreements;  /* precision mode: candidates where float and FP64 answers differ */
 } oibvh_detect_stats;
 int oibvh_scene_get_stats(oibvh_scene_t s, oibvh_detect_stats* out);
 

@@ -26,6 +26,8 @@ ERR_OVERFLOW = 4
 ERR_STATE = 5
 ERR_UNSUPPORTED = 6
 ERR_TIMEOUT = 7
+PRECISION_FP32 = 0
+PRECISION_FP64_FILTERED = 1
 
 DEVICE_CPU = -1
 
@@ -40,6 +42,9 @@ class DetectStats(ctypes.Structure):
         ("candidates", ctypes.c_uint64),
         ("hits", ctypes.c_uint64),
         ("front_peak", ctypes.c_uint64),
+        ("fp64_axes", ctypes.c_uint64),
+        ("fp64_candidates", ctypes.c_uint64),
+        ("fp32_disagreements", ctypes.c_uint64),
     ]
 
 
@@ -93,6 +98,8 @@ SIGNATURES = [
     ("oibvh_scene_get_int_tri_pairs", ctypes.c_int, [_vp, _u32p, _u64, ctypes.POINTER(_u64)]),
     ("oibvh_scene_get_candidates", ctypes.c_int, [_vp, _u32p, _u64, ctypes.POINTER(_u64)]),
     ("oibvh_scene_set_queue_capacity", ctypes.c_int, [_vp, _u32, _u32, _u32]),
+    ("oibvh_scene_set_precision", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("oibvh_scene_get_precision", ctypes.c_int, [_vp]),
     ("oibvh_scene_get_stats", ctypes.c_int, [_vp, ctypes.POINTER(DetectStats)]),
     ("oibvh_scene_destroy", ctypes.c_int, [_vp]),
     ("oibvh_pair_detect_noalloc", ctypes.c_int, [_vp, _vp, _u32, _vp, _u32, _u32p, _vp]),

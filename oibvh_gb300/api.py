@@ -302,6 +302,14 @@ class Scene:
         N.check(N.lib().oibvh_scene_set_queue_capacity(self._h, int(front), int(candidates), int(hits)),
                 "oibvh_scene_set_queue_capacity")
 
+    def set_precision(self, mode: int) -> None:
+        """N.PRECISION_FP32 (the reference's float test) or
+        N.PRECISION_FP64_FILTERED (float test, undecided axes again in FP64)."""
+        N.check(N.lib().oibvh_scene_set_precision(self._h, int(mode)), "oibvh_scene_set_precision")
+
+    def precision(self) -> int:
+        return int(N.lib().oibvh_scene_get_precision(self._h))
+
     def stats(self) -> dict:
         st = N.DetectStats()
         N.check(N.lib().oibvh_scene_get_stats(self._h, ctypes.byref(st)), "oibvh_scene_get_stats")

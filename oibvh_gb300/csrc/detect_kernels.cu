@@ -93,6 +93,244 @@ __device__ __forceinline__ bool tri_intersect_exact(const V3& P1, const V3& P2, 
     return true;
 }
 
+// ---------------------------------------------------------------------------
+// Precision mode: the same 17 tests with an FP64 filter.
+//
+// Each axis test compares two margins, d1 = mn1 - mx2 and d2 = mn2 - mx1
+// (the axis separates when either is > 0). Every float quantity of the test
+// carries a running forward error bound against its exact value over the
+// same float inputs (u = 2^-24; c = fl(a - b): e_c = e_a + e_b + u|c|;
+// c = fl(a b): e_c = |a| e_b + |b| e_a + e_a e_b + u|c| + 2^-149), so each projection
+// P has a bound e_P and each margin the bound E = max e_P + max e_Q. The
+// FP64 formula obeys the same recurrences with u = 2^-53, so its margin lies
+// within 2^-29 E (plus second-order terms) of the exact one. A margin with
+// |d| > 2E therefore has the same sign in float, exact and FP64 arithmetic.
+//
+// The test runs in two passes. Pass 1 evaluates all 17 axes in float: an
+// axis whose margin is > 2E separates in every arithmetic and ends the
+// test; an axis with both margins < -2E separates in none; the rest are
+// undecided. Pass 2 evaluates only the undecided axes again in FP64, with
+// the FP64 formula's own operations in its own order (no contraction),
+// until one separates. The pair set then equals the all-FP64 pair set by
+// construction, while the float answer (the reference arithmetic) is known
+// for every candidate, so the disagreements between the two are counted.
+//
+// Shortcut: two triangles that share a vertex (equal coordinates) are never
+// separated by this test in any arithmetic: the shared vertex gives the same
+// projection in both triangles' sets, so mn1 <= s <= mx2 and mn2 <= s <= mx1
+// on every axis. Relative extents outside [2^-20, 2^20] and non-finite
+// inputs take the full FP64 test (the bounds could under- or overflow).
+// ---------------------------------------------------------------------------
+struct D3 {
+    double x, y, z;
+};
+__device__ __forceinline__ D3 to_d(const V3& v) { return D3{(double)v.x, (double)v.y, (double)v.z}; }
+__device__ __forceinline__ D3 dsub(const D3& a, const D3& b)
+{
+    return D3{__dsub_rn(a.x, b.x), __dsub_rn(a.y, b.y), __dsub_rn(a.z, b.z)};
+}
+__device__ __forceinline__ D3 dcross(const D3& x, const D3& y)
+{
+    return D3{__dsub_rn(__dmul_rn(x.y, y.z), __dmul_rn(y.y, x.z)), __dsub_rn(__dmul_rn(x.z, y.x), __dmul_rn(y.z, x.x)),
+              __dsub_rn(__dmul_rn(x.x, y.y), __dmul_rn(y.x, x.y))};
+}
+__device__ __forceinline__ double ddot(const D3& a, const D3& b)
+{
+    return __dadd_rn(__dadd_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)), __dmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ bool project6_d(const D3& ax, const D3& p1, const D3& p2, const D3& p3, const D3& q1,
+                                           const D3& q2, const D3& q3)
+{
+    const double P1 = ddot(ax, p1), P2 = ddot(ax, p2), P3 = ddot(ax, p3);
+    const double Q1 = ddot(ax, q1), Q2 = ddot(ax, q2), Q3 = ddot(ax, q3);
+    const double mx1 = fmax(fmax(P1, P2), P3), mn1 = fmin(fmin(P1, P2), P3);
+    const double mx2 = fmax(fmax(Q1, Q2), Q3), mn2 = fmin(fmin(Q1, Q2), Q3);
+    if (mn1 > mx2) return false;
+    if (mn2 > mx1) return false;
+    return true;
+}
+__device__ __forceinline__ const D3& pick3(uint32_t i, const D3& a, const D3& b, const D3& c)
+{
+    return i == 0 ? a : (i == 1 ? b : c);
+}
+
+// Relative vertices of the FP64 formula: p_i = P_i - P1, q_j = Q_j - P1.
+struct D6 {
+    D3 p2, p3, q1, q2, q3;
+};
+__device__ __forceinline__ D6 fp64_relative(const V3& P1, const V3& P2, const V3& P3, const V3& Q1, const V3& Q2,
+                                            const V3& Q3)
+{
+    const D3 dP1 = to_d(P1);
+    return D6{dsub(to_d(P2), dP1), dsub(to_d(P3), dP1), dsub(to_d(Q1), dP1), dsub(to_d(Q2), dP1), dsub(to_d(Q3), dP1)};
+}
+
+// Axis k of the 17 (0: n1, 1: m1, 2 + 3i + j: e_i x f_j, 11 + i: e_i x n1,
+// 14 + j: f_j x m1) in FP64: true when it does NOT separate the triangles.
+// Edges as the FP64 formula forms them: e1 = p2 - p1, e2 = p3 - p2,
+// e3 = p1 - p3, f1 = q2 - q1, f2 = q3 - q2, f3 = q1 - q3 (p1 = 0).
+__device__ __forceinline__ bool axis_overlaps_fp64(uint32_t k, const D6& r)
+{
+    const D3 p1{0.0, 0.0, 0.0};
+    const D3 e1 = dsub(r.p2, p1), e2 = dsub(r.p3, r.p2), e3 = dsub(p1, r.p3);
+    const D3 f1 = dsub(r.q2, r.q1), f2 = dsub(r.q3, r.q2), f3 = dsub(r.q1, r.q3);
+    D3 ax;
+    if (k == 0) ax = dcross(e1, e2);
+    else if (k == 1) ax = dcross(f1, f2);
+    else if (k < 11) ax = dcross(pick3((k - 2) / 3, e1, e2, e3), pick3((k - 2) % 3, f1, f2, f3));
+    else if (k < 14) ax = dcross(pick3(k - 11, e1, e2, e3), dcross(e1, e2));
+    else ax = dcross(pick3(k - 14, f1, f2, f3), dcross(f1, f2));
+    return project6_d(ax, p1, r.p2, r.p3, r.q1, r.q2, r.q3);
+}
+
+// FP64 tests of the axes in `mask`, in order, until one separates.
+__device__ __noinline__ bool fp64_axes_separate(uint32_t mask, V3 P1, V3 P2, V3 P3, V3 Q1, V3 Q2, V3 Q3,
+                                                uint32_t& evaluated)
+{
+    const D6 r = fp64_relative(P1, P2, P3, Q1, Q2, Q3);
+    while (mask) {
+        const uint32_t k = __ffs(mask) - 1;
+        mask &= mask - 1;
+        ++evaluated;
+        if (!axis_overlaps_fp64(k, r)) return true;
+    }
+    return false;
+}
+
+// A float vector with a componentwise bound on its error.
+struct EV3 {
+    V3 v, e;
+};
+constexpr float kU = 0x1p-24f;
+constexpr float kEta = 0x1p-149f;  // a product that underflows is off by up to half the smallest subnormal
+// (a sum or difference whose result is subnormal is exact)
+__device__ __forceinline__ float err_sub(float c, float ea, float eb) { return ea + eb + kU * fabsf(c); }
+__device__ __forceinline__ float err_mul(float a, float b, float c, float ea, float eb)
+{
+    return fabsf(a) * eb + fabsf(b) * ea + ea * eb + kU * fabsf(c) + kEta;
+}
+__device__ __forceinline__ EV3 esub(const EV3& a, const EV3& b)
+{
+    const V3 c = vsub(a.v, b.v);
+    return EV3{c, V3{err_sub(c.x, a.e.x, b.e.x), err_sub(c.y, a.e.y, b.e.y), err_sub(c.z, a.e.z, b.e.z)}};
+}
+// glm::cross with bounds: c = fl(fl(a b) - fl(d g)) per component
+__device__ __forceinline__ float ecross1(float a, float b, float d, float g, float ea, float eb, float ed, float eg,
+                                         float& err)
+{
+    const float m1 = __fmul_rn(a, b), m2 = __fmul_rn(d, g), c = __fsub_rn(m1, m2);
+    err = err_sub(c, err_mul(a, b, m1, ea, eb), err_mul(d, g, m2, ed, eg));
+    return c;
+}
+__device__ __forceinline__ EV3 ecross(const EV3& x, const EV3& y)
+{
+    EV3 r;
+    r.v.x = ecross1(x.v.y, y.v.z, y.v.y, x.v.z, x.e.y, y.e.z, y.e.y, x.e.z, r.e.x);
+    r.v.y = ecross1(x.v.z, y.v.x, y.v.z, x.v.x, x.e.z, y.e.x, y.e.z, x.e.x, r.e.y);
+    r.v.z = ecross1(x.v.x, y.v.y, y.v.x, x.v.y, x.e.x, y.e.y, y.e.x, x.e.y, r.e.z);
+    return r;
+}
+// glm::dot with a bound: fl(fl(fl(ax px) + fl(ay py)) + fl(az pz))
+__device__ __forceinline__ float edot(const EV3& a, const EV3& p, float& err)
+{
+    const float t0 = __fmul_rn(a.v.x, p.v.x), t1 = __fmul_rn(a.v.y, p.v.y), t2 = __fmul_rn(a.v.z, p.v.z);
+    const float s = __fadd_rn(t0, t1), r = __fadd_rn(s, t2);
+    const float e0 = err_mul(a.v.x, p.v.x, t0, a.e.x, p.e.x);
+    const float e1 = err_mul(a.v.y, p.v.y, t1, a.e.y, p.e.y);
+    const float e2 = err_mul(a.v.z, p.v.z, t2, a.e.z, p.e.z);
+    err = err_sub(r, err_sub(s, e0, e1), e2);
+    return r;
+}
+// One float axis test with bounds: 0 = separates in every arithmetic,
+// 1 = separates in none, 2 = undecided; `sep32` is the plain float answer.
+__device__ __forceinline__ uint32_t project6_bounded(const EV3& ax, const EV3& p1, const EV3& p2, const EV3& p3,
+                                                     const EV3& q1, const EV3& q2, const EV3& q3, bool& sep32)
+{
+    float eP1, eP2, eP3, eQ1, eQ2, eQ3;
+    const float P1 = edot(ax, p1, eP1), P2 = edot(ax, p2, eP2), P3 = edot(ax, p3, eP3);
+    const float Q1 = edot(ax, q1, eQ1), Q2 = edot(ax, q2, eQ2), Q3 = edot(ax, q3, eQ3);
+    const float mx1 = fmaxf(fmaxf(P1, P2), P3), mn1 = fminf(fminf(P1, P2), P3);
+    const float mx2 = fmaxf(fmaxf(Q1, Q2), Q3), mn2 = fminf(fminf(Q1, Q2), Q3);
+    sep32 = mn1 > mx2 || mn2 > mx1;
+    // 2 E: covers the FP64 error (2^-29 E), second-order terms and the
+    // rounding of the margins and of the bound itself
+    const float tau = 2.0f * (fmaxf(fmaxf(eP1, eP2), eP3) + fmaxf(fmaxf(eQ1, eQ2), eQ3));
+    const float d1 = __fsub_rn(mn1, mx2), d2 = __fsub_rn(mn2, mx1);
+    if (d1 > tau || d2 > tau) return 0u;
+    if (d1 < -tau && d2 < -tau) return 1u;
+    return 2u;
+}
+
+__device__ __forceinline__ bool veq(const V3& a, const V3& b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+
+enum : uint32_t { kPass1Separated = 0, kPass1Hit = 1, kPass1Undecided = 2 };
+
+// Pass 1 of the filtered test: every axis in float with error bounds.
+// Returns kPass1Separated / kPass1Hit when the float and FP64 answers are
+// known to agree, else kPass1Undecided with the axes to settle in FP64 in
+// `mask` and the plain float answer in `hit32`.
+__device__ __forceinline__ uint32_t tri_pass1(const V3& P1, const V3& P2, const V3& P3, const V3& Q1, const V3& Q2,
+                                              const V3& Q3, uint32_t& mask, bool& hit32)
+{
+    const EV3 p1{V3{0.0f, 0.0f, 0.0f}, V3{0.0f, 0.0f, 0.0f}};
+    const V3 p2v = vsub(P2, P1), p3v = vsub(P3, P1);
+    const V3 q1v = vsub(Q1, P1), q2v = vsub(Q2, P1), q3v = vsub(Q3, P1);
+    float A = fmaxf(fmaxf(fmaxf(fabsf(p2v.x), fabsf(p2v.y)), fmaxf(fabsf(p2v.z), fabsf(p3v.x))),
+                    fmaxf(fmaxf(fabsf(p3v.y), fabsf(p3v.z)), fmaxf(fabsf(q1v.x), fabsf(q1v.y))));
+    A = fmaxf(A, fmaxf(fmaxf(fabsf(q1v.z), fabsf(q2v.x)), fmaxf(fabsf(q2v.y), fabsf(q2v.z))));
+    A = fmaxf(A, fmaxf(fmaxf(fabsf(q3v.x), fabsf(q3v.y)), fabsf(q3v.z)));
+    if (!(A >= 0x1p-20f && A <= 0x1p20f)) {
+        // the bounds could under- or overflow: every axis in FP64
+        hit32 = tri_intersect_exact(P1, P2, P3, Q1, Q2, Q3);
+        mask = (1u << 17) - 1u;
+        return kPass1Undecided;
+    }
+    if (veq(P1, Q1) || veq(P1, Q2) || veq(P1, Q3) || veq(P2, Q1) || veq(P2, Q2) || veq(P2, Q3) || veq(P3, Q1) ||
+        veq(P3, Q2) || veq(P3, Q3))
+        return kPass1Hit;  // a shared vertex: never separated
+    // relative vertices: one rounding each
+    const EV3 p2{p2v, V3{kU * fabsf(p2v.x), kU * fabsf(p2v.y), kU * fabsf(p2v.z)}};
+    const EV3 p3{p3v, V3{kU * fabsf(p3v.x), kU * fabsf(p3v.y), kU * fabsf(p3v.z)}};
+    const EV3 q1{q1v, V3{kU * fabsf(q1v.x), kU * fabsf(q1v.y), kU * fabsf(q1v.z)}};
+    const EV3 q2{q2v, V3{kU * fabsf(q2v.x), kU * fabsf(q2v.y), kU * fabsf(q2v.z)}};
+    const EV3 q3{q3v, V3{kU * fabsf(q3v.x), kU * fabsf(q3v.y), kU * fabsf(q3v.z)}};
+    const EV3 e1 = esub(p2, p1), e2 = esub(p3, p2), e3 = esub(p1, p3);
+    const EV3 f1 = esub(q2, q1), f2 = esub(q3, q2), f3 = esub(q1, q3);
+    const EV3 n1 = ecross(e1, e2), m1 = ecross(f1, f2);
+    bool sep32 = false;
+    uint32_t undecided = 0;
+#define OIBVH_AXIS(K, AX)                                                        \
+    {                                                                            \
+        bool s32;                                                                \
+        const uint32_t c = project6_bounded((AX), p1, p2, p3, q1, q2, q3, s32);  \
+        if (c == 0u) return kPass1Separated;                                     \
+        sep32 |= s32;                                                            \
+        if (c == 2u) undecided |= 1u << (K);                                     \
+    }
+    OIBVH_AXIS(0, n1)
+    OIBVH_AXIS(1, m1)
+    OIBVH_AXIS(2, ecross(e1, f1))
+    OIBVH_AXIS(3, ecross(e1, f2))
+    OIBVH_AXIS(4, ecross(e1, f3))
+    OIBVH_AXIS(5, ecross(e2, f1))
+    OIBVH_AXIS(6, ecross(e2, f2))
+    OIBVH_AXIS(7, ecross(e2, f3))
+    OIBVH_AXIS(8, ecross(e3, f1))
+    OIBVH_AXIS(9, ecross(e3, f2))
+    OIBVH_AXIS(10, ecross(e3, f3))
+    OIBVH_AXIS(11, ecross(e1, n1))
+    OIBVH_AXIS(12, ecross(e2, n1))
+    OIBVH_AXIS(13, ecross(e3, n1))
+    OIBVH_AXIS(14, ecross(f1, m1))
+    OIBVH_AXIS(15, ecross(f2, m1))
+    OIBVH_AXIS(16, ecross(f3, m1))
+#undef OIBVH_AXIS
+    if (undecided == 0) return kPass1Hit;  // no axis separates, in any arithmetic
+    mask = undecided;
+    hit32 = !sep32;
+    return kPass1Undecided;
+}
+
 __device__ __forceinline__ V3 load_vertex(const float4* __restrict__ pos, uint32_t v)
 {
     const float4 p = __ldg(pos + v);
@@ -452,8 +690,115 @@ __global__ void __launch_bounds__(kDetectThreads) k_narrow(DetectArgs a)
     }
 }
 
+// Narrow phase of precision mode over stored candidates. Pass 1 (float with
+// error bounds) takes one candidate per lane; candidates it leaves undecided
+// are queued per warp in shared memory and settled in FP64 32 at a time, so
+// the FP64 work runs in full warps instead of in the few lanes that need it.
+constexpr uint32_t kFp64Queue = 64;  // <= 31 left over + 32 added per round
+
+__device__ __forceinline__ void load_tris(const DetectArgs& a, uint64_t c, V3& P1, V3& P2, V3& P3, V3& Q1, V3& Q2,
+                                          V3& Q3, uint4& rec)
+{
+    const PairView pv = a.pairs[bvtt_pair(c)];
+    const TreeView& TA = a.trees[pv.a];
+    const TreeView& TB = a.trees[pv.b];
+    const uint4 fa = __ldg(TA.face + bvtt_a(c));
+    const uint4 fb = __ldg(TB.face + bvtt_b(c));
+    P1 = load_vertex(TA.pos, fa.x);
+    P2 = load_vertex(TA.pos, fa.y);
+    P3 = load_vertex(TA.pos, fa.z);
+    Q1 = load_vertex(TB.pos, fb.x);
+    Q2 = load_vertex(TB.pos, fb.y);
+    Q3 = load_vertex(TB.pos, fb.z);
+    rec = make_uint4(pv.a, pv.b, fa.w, fb.w);
+}
+
+__device__ __forceinline__ void append_hit(const DetectArgs& a, bool hit, const uint4& rec, uint32_t lane)
+{
+    const uint32_t pos = warp_append(a.counts + kCountHits, hit, lane);
+    if (hit) {
+        if (pos < a.hit_cap) a.hits[pos] = rec;
+        else atomicOr(a.counts + kCountFlags, (uint32_t)kFlagHitOverflow);
+    }
+}
+
+// FP64 stage of `count` queued candidates (one per lane).
+__device__ __forceinline__ void settle_fp64(const DetectArgs& a, const uint64_t* qc, const uint32_t* qm,
+                                            uint32_t count, uint32_t lane)
+{
+    bool hit = false, disagree = false;
+    uint32_t evaluated = 0;
+    uint4 rec = make_uint4(0, 0, 0, 0);
+    if (lane < count) {
+        V3 P1, P2, P3, Q1, Q2, Q3;
+        load_tris(a, qc[lane], P1, P2, P3, Q1, Q2, Q3, rec);
+        const uint32_t m = qm[lane];
+        hit = !fp64_axes_separate(m & 0x1ffffu, P1, P2, P3, Q1, Q2, Q3, evaluated);
+        disagree = hit != ((m >> 31) != 0u);
+    }
+    append_hit(a, hit, rec, lane);
+    const uint32_t axes = __reduce_add_sync(0xffffffffu, evaluated);
+    const uint32_t cands = __popc(__ballot_sync(0xffffffffu, lane < count));
+    const uint32_t dis = __popc(__ballot_sync(0xffffffffu, disagree));
+    if (lane == 0) {
+        if (axes) atomicAdd(a.counts + kCountFp64Axes, axes);
+        if (cands) atomicAdd(a.counts + kCountFp64Cands, cands);
+        if (dis) atomicAdd(a.counts + kCountDisagree, dis);
+    }
+}
+
+__global__ void __launch_bounds__(kDetectThreads) k_narrow_prec(DetectArgs a)
+{
+    __shared__ uint64_t s_qc[kDetectThreads / 32][kFp64Queue];
+    __shared__ uint32_t s_qm[kDetectThreads / 32][kFp64Queue];
+    const uint32_t n = min(a.counts[kCountCandSlots], a.cand_cap);
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+    uint64_t* qc = s_qc[wib];
+    uint32_t* qm = s_qm[wib];
+    uint32_t qn = 0;  // warp-uniform
+    for (uint32_t base = warp * 32; base < n; base += n_warps * 32) {
+        const uint32_t i = base + lane;
+        bool hit = false, queue = false;
+        uint32_t mask = 0;
+        uint4 rec = make_uint4(0, 0, 0, 0);
+        uint64_t c = 0;
+        if (i < n) {
+            c = a.cand[i];
+            V3 P1, P2, P3, Q1, Q2, Q3;
+            load_tris(a, c, P1, P2, P3, Q1, Q2, Q3, rec);
+            bool hit32 = false;
+            const uint32_t st = tri_pass1(P1, P2, P3, Q1, Q2, Q3, mask, hit32);
+            hit = st == kPass1Hit;
+            queue = st == kPass1Undecided;
+            mask |= hit32 ? 0x80000000u : 0u;
+        }
+        append_hit(a, hit, rec, lane);
+        const uint32_t qmask = __ballot_sync(0xffffffffu, queue);
+        if (queue) {
+            const uint32_t slot = qn + __popc(qmask & ((1u << lane) - 1u));
+            qc[slot] = c;
+            qm[slot] = mask;
+        }
+        qn += __popc(qmask);
+        __syncwarp();
+        if (qn >= 32) {
+            settle_fp64(a, qc + qn - 32, qm + qn - 32, 32, lane);
+            qn -= 32;
+            __syncwarp();
+        }
+    }
+    if (qn > 0) settle_fp64(a, qc, qm, qn, lane);
+}
+
+// The traversal kernels' fused narrow phase is the float test only; precision
+// mode runs the broad phase alone and then k_narrow_prec.
+static inline bool fused_precision(const DetectArgs& a) { return a.precision && a.fuse_narrow; }
+
 cudaError_t launch_init_front(const DetectArgs& a, uint32_t total0, cudaStream_t s)
 {
+    if (fused_precision(a)) return cudaErrorInvalidValue;
     uint32_t blocks = (total0 + kDetectThreads - 1) / kDetectThreads;
     if (blocks > (uint32_t)a.grid) blocks = (uint32_t)a.grid;
     if (blocks == 0) blocks = 1;
@@ -464,6 +809,7 @@ cudaError_t launch_init_front(const DetectArgs& a, uint32_t total0, cudaStream_t
 
 cudaError_t launch_top(const DetectArgs& a, cudaStream_t s)
 {
+    if (fused_precision(a)) return cudaErrorInvalidValue;
     const int smem = (int)(2 * kTopCap * sizeof(uint64_t));
     static bool configured[64] = {};
     int dev = 0;
@@ -480,6 +826,7 @@ cudaError_t launch_top(const DetectArgs& a, cudaStream_t s)
 
 cudaError_t launch_walk(const DetectArgs& a, uint32_t round, cudaStream_t s)
 {
+    if (fused_precision(a)) return cudaErrorInvalidValue;
     note_launches(1);
     k_walk<<<a.grid, kDetectThreads, 0, s>>>(a, round);
     return cudaGetLastError();
@@ -495,7 +842,8 @@ int walk_blocks_per_sm()
 cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s)
 {
     note_launches(1);
-    k_narrow<<<a.grid, kDetectThreads, 0, s>>>(a);
+    if (a.precision) k_narrow_prec<<<a.grid, kDetectThreads, 0, s>>>(a);
+    else k_narrow<<<a.grid, kDetectThreads, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -318,6 +318,7 @@ struct oibvh_scene_s {
     // tuning (oibvh_scene_set_tuning / oibvh_scene_autotune)
     uint32_t tune_start_log2 = 16;  // start cross product ~ 2^this node pairs per pass
     uint32_t tune_handoff = 2048;   // front width at which k_top hands over to the walkers
+    uint32_t precision = 0;         // OIBVH_PRECISION_*
     uint32_t tune_walk_per_sm = 0;  // walker CTAs per SM, 0 = as many as fit
 
     // captured frame (CUDA graph): [transform] + refit + detect
@@ -431,9 +432,19 @@ int walk_grid(const oibvh_scene_s* s)
     return sm_count(s->device) * std::max(1, per);
 }
 
-// Broad phase (+ narrow phase when `narrow`) over every pair, pass by pass.
-int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expand, bool narrow, cudaStream_t st)
+int narrow_pass(oibvh_scene_s* s, uint32_t np, uint64_t hits_before, cudaStream_t st);
+
+// How detect_impl runs the narrow phase: fused into the traversal (float
+// test), not at all (broad phase only, candidates kept), or as a separate
+// kernel over each pass's candidates (precision mode: the filtered test
+// runs at its own occupancy instead of holding the traversal's registers).
+enum DetectMode { kDetectFused = 0, kDetectBroad = 1, kDetectSplit = 2 };
+inline int full_detect_mode(const oibvh_scene_s* s) { return s->precision ? kDetectSplit : kDetectFused; }
+
+// Broad phase (+ narrow phase unless kDetectBroad) over every pair, pass by pass.
+int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expand, int mode, cudaStream_t st)
 {
+    const bool narrow = mode == kDetectFused;  // narrow phase inside the traversal kernels
     if (device_type < 0)
         return fail(OIBVH_ERR_UNSUPPORTED,
                     "device type CPU: the reference's detectCollisionOnCPU is empty; this library has no CPU path");
@@ -509,6 +520,7 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
             a.fuse_narrow = narrow ? 1u : 0u;
             a.grid = grid;
             a.handoff = s->tune_handoff;
+            a.precision = s->precision;
             CUDA_TRY(launch_init_front(a, (uint32_t)plan.front0, st));
             CUDA_TRY(launch_top(a, st));
             uint32_t rounds = 1;  // list 1 is the first walk round's input
@@ -539,6 +551,9 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
                 continue;
             }
             s->stats.nodes_tested += c[kCountTested];
+            s->stats.fp64_axes += c[kCountFp64Axes];
+            s->stats.fp64_candidates += c[kCountFp64Cands];
+            s->stats.fp32_disagreements += c[kCountDisagree];
             s->stats.front_peak = std::max(s->stats.front_peak, peak);
             s->stats.steps = rounds;
             s->cand_count += c[kCountCands];
@@ -546,7 +561,9 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
             break;
         }
         s->stats.passes++;
-        if (!narrow) {
+        if (mode == kDetectSplit) {
+            OK_TRY(narrow_pass(s, np, hits_before, st));
+        } else if (!narrow) {
             if (n_pairs > kMaxPairsPerPass)
                 return fail(OIBVH_ERR_UNSUPPORTED, "the split broad phase handles at most 65536 pairs");
             s->last_pairs = plan.pv;
@@ -558,18 +575,21 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
     return OIBVH_OK;
 }
 
-int narrow_impl(oibvh_scene_s* s, cudaStream_t st)
+// Narrow phase over the stored candidates of the last broad pass (pairv holds
+// that pass's pair table); hits are appended after the first `hits_before`.
+int narrow_pass(oibvh_scene_s* s, uint32_t np, uint64_t hits_before, cudaStream_t st)
 {
-    if (!s->cands_valid) return fail(OIBVH_ERR_STATE, "narrow phase needs a broad phase first");
-    DeviceGuard g(s->device);
-    const uint32_t np = (uint32_t)s->last_pairs.size();
     for (int attempt = 0;; ++attempt) {
         if (attempt > 12) return fail(OIBVH_ERR_OVERFLOW, "hit queue kept overflowing");
-        // counts[kCountCandSlots] still holds the candidate count of the broad phase
-        uint32_t z[2] = {0, 0};
-        std::memcpy(s->h_counts.p, z, sizeof(z));
+        // counts[kCountCandSlots] still holds the candidate count of the broad phase;
+        // hits (from hits_before), flags and the precision-mode counters are reset
+        std::memset(s->h_counts.p, 0, kCountWork0 * sizeof(uint32_t));
+        s->h_counts.p[kCountHits] = (uint32_t)hits_before;
         CUDA_TRY(cudaMemcpyAsync(s->counts.p, s->h_counts.p, 2 * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(s->counts.p + kCountFp64Axes, s->h_counts.p + kCountFp64Axes,
+                                 (kCountWork0 - kCountFp64Axes) * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
         DetectArgs a{};
+        a.precision = s->precision;
         a.trees = s->views.p;
         a.pairs = s->pairv.p;
         a.n_pairs = np;
@@ -584,16 +604,28 @@ int narrow_impl(oibvh_scene_s* s, cudaStream_t st)
         CUDA_TRY(cudaMemcpyAsync(s->h_counts.p, s->counts.p, kCountTotal * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                                  st));
         CUDA_TRY(cudaStreamSynchronize(st));
-        if (s->h_counts.p[kCountFlags] & kFlagHitOverflow) {
-            const uint32_t want = grow_cap(s->h_counts.p[kCountHits], s->hit_cap);
-            OK_TRY(s->hits.ensure(want, "cudaMalloc(hits)"));
+        const uint32_t* c = s->h_counts.p;
+        if (c[kCountFlags] & kFlagHitOverflow) {
+            const uint32_t want = grow_cap(c[kCountHits], s->hit_cap);
+            OK_TRY(s->hits.grow_keep(want, hits_before, st, "cudaMalloc(hits)"));
             s->hit_cap = want;
             continue;
         }
-        s->hit_count = s->h_counts.p[kCountHits];
+        s->hit_count = c[kCountHits];
         s->stats.hits = s->hit_count;
+        s->stats.fp64_axes += c[kCountFp64Axes];
+        s->stats.fp64_candidates += c[kCountFp64Cands];
+        s->stats.fp32_disagreements += c[kCountDisagree];
         return OIBVH_OK;
     }
+}
+
+int narrow_impl(oibvh_scene_s* s, cudaStream_t st)
+{
+    if (!s->cands_valid) return fail(OIBVH_ERR_STATE, "narrow phase needs a broad phase first");
+    DeviceGuard g(s->device);
+    s->stats.fp64_axes = s->stats.fp64_candidates = s->stats.fp32_disagreements = 0;
+    return narrow_pass(s, (uint32_t)s->last_pairs.size(), 0, st);
 }
 
 }  // namespace
@@ -891,7 +923,7 @@ API int oibvh_scene_detect(oibvh_scene_t s, int device_type, uint32_t entry_leve
 {
     GUARD_BEGIN
     if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
-    return detect_impl(s, device_type, entry_level, expand_levels, true, (cudaStream_t)stream);
+    return detect_impl(s, device_type, entry_level, expand_levels, full_detect_mode(s), (cudaStream_t)stream);
     GUARD_END
 }
 
@@ -899,7 +931,7 @@ API int oibvh_scene_broad(oibvh_scene_t s, int device_type, uint32_t entry_level
 {
     GUARD_BEGIN
     if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
-    return detect_impl(s, device_type, entry_level, expand_levels, false, (cudaStream_t)stream);
+    return detect_impl(s, device_type, entry_level, expand_levels, kDetectBroad, (cudaStream_t)stream);
     GUARD_END
 }
 
@@ -1013,6 +1045,18 @@ API int oibvh_scene_set_queue_capacity(oibvh_scene_t s, uint32_t front, uint32_t
     s->frame_stale = true;  // a captured frame points at the released buffers
     return OIBVH_OK;
 }
+
+API int oibvh_scene_set_precision(oibvh_scene_t s, int mode)
+{
+    if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
+    if (mode != OIBVH_PRECISION_FP32 && mode != OIBVH_PRECISION_FP64_FILTERED)
+        return fail(OIBVH_ERR_ARG, "unknown precision mode");
+    if ((uint32_t)mode != s->precision) s->frame_stale = true;
+    s->precision = (uint32_t)mode;
+    return OIBVH_OK;
+}
+
+API int oibvh_scene_get_precision(oibvh_scene_t s) { return s ? (int)s->precision : -1; }
 
 API int oibvh_scene_get_stats(oibvh_scene_t s, oibvh_detect_stats* out)
 {
@@ -1188,19 +1232,19 @@ API int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t rep
     oibvh_tuning bt{};
     int st = OIBVH_OK;
     // warm-up sizes the queues
-    st = detect_impl(s, s->device, entry_level, 1, true, 0);
+    st = detect_impl(s, s->device, entry_level, 1, full_detect_mode(s), 0);
     for (uint32_t sl : starts) {
         for (uint32_t h : handoffs) {
             for (int per = std::max(1, fit / 2); per <= fit && st == OIBVH_OK; per += std::max(1, fit / 2)) {
                 s->tune_start_log2 = sl;
                 s->tune_handoff = h;
                 s->tune_walk_per_sm = (uint32_t)per;
-                st = detect_impl(s, s->device, entry_level, 1, true, 0);
+                st = detect_impl(s, s->device, entry_level, 1, full_detect_mode(s), 0);
                 if (st != OIBVH_OK) break;
                 float tot = 0.0f;
                 for (uint32_t r = 0; r < reps && st == OIBVH_OK; ++r) {
                     cudaEventRecord(e0, 0);
-                    st = detect_impl(s, s->device, entry_level, 1, true, 0);
+                    st = detect_impl(s, s->device, entry_level, 1, full_detect_mode(s), 0);
                     cudaEventRecord(e1, 0);
                     cudaEventSynchronize(e1);
                     float ms = 0.0f;
@@ -1223,7 +1267,7 @@ API int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t rep
     s->tune_handoff = bt.handoff;
     s->tune_walk_per_sm = bt.walk_blocks_per_sm;
     // capacities: the largest work list and hit count seen, doubled
-    st = detect_impl(s, s->device, entry_level, 1, true, 0);
+    st = detect_impl(s, s->device, entry_level, 1, full_detect_mode(s), 0);
     if (st != OIBVH_OK) return st;
     s->front_cap = grow_cap(2 * s->stats.front_peak, s->front_cap);
     if (s->hit_count * 2 > s->hit_cap) {
@@ -1256,7 +1300,7 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
     // warm-up frame outside the capture: sizes every buffer and uploads the tables
     if (s->frame_rest) OK_TRY(oibvh_scene_transform(s, (const float*)s->frame_rest, s->frame_mats, st));
     if (s->frame_refit) OK_TRY(oibvh_scene_refit(s, st));
-    OK_TRY(detect_impl(s, s->device, s->frame_entry, s->frame_expand, true, st));
+    OK_TRY(detect_impl(s, s->device, s->frame_entry, s->frame_expand, full_detect_mode(s), st));
     // walk rounds: the warm-up frame used steps - 1 of them; two more for headroom
     // (a round with an empty input list returns at once)
     s->frame_rounds = std::min(kMaxRounds - 1, std::max(3u, s->stats.steps + 1));
@@ -1268,6 +1312,11 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
         const uint32_t want = grow_cap(2 * s->hit_count, s->hit_cap);
         OK_TRY(s->hits.ensure(want, "cudaMalloc(hits)"));
         s->hit_cap = want;
+    }
+    if (s->precision) {
+        // split narrow phase: the candidates of the whole frame are stored
+        s->cand_cap = std::max(s->cand_cap, grow_cap(2 * s->cand_count, s->cand_cap));
+        OK_TRY(s->cand.ensure(s->cand_cap, "cudaMalloc(candidates)"));
     }
     OK_TRY(s->h_frame_counts.ensure(kCountTotal, "cudaMallocHost(frame counts)"));
     PassPlan plan;
@@ -1291,9 +1340,12 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
     a.hits = s->hits.p;
     a.hit_cap = s->hit_cap;
     a.counts = s->counts.p;
-    a.fuse_narrow = 1;
+    a.fuse_narrow = s->precision ? 0u : 1u;
+    a.cand = s->precision ? s->cand.p : nullptr;
+    a.cand_cap = s->precision ? s->cand_cap : 0u;
     a.grid = walk_grid(s);
     a.handoff = s->tune_handoff;
+    a.precision = s->precision;
 
     // capture on a private non-blocking stream (the legacy default stream
     // cannot be captured); the graph is launched on the caller's stream
@@ -1319,6 +1371,13 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
     kernels += 2;
     for (uint32_t r = 1; r <= s->frame_rounds && e == cudaSuccess; ++r) {
         e = launch_walk(a, r, st);
+        ++kernels;
+    }
+    if (s->precision && e == cudaSuccess) {
+        DetectArgs n = a;
+        n.fuse_narrow = 1;
+        n.grid = sm_count(s->device) * 8;
+        e = launch_narrow(n, st);
         ++kernels;
     }
     if (e == cudaSuccess)
@@ -1389,7 +1448,7 @@ API int oibvh_scene_finish_frame(oibvh_scene_t s, void* stream)
         // synchronous way (the refit already ran) and capture again next frame
         s->frame_stale = true;
         s->frame_redos++;
-        OK_TRY(detect_impl(s, s->device, s->frame_entry, s->frame_expand, true, st));
+        OK_TRY(detect_impl(s, s->device, s->frame_entry, s->frame_expand, full_detect_mode(s), st));
         s->stats.retries++;
         return OIBVH_OK;
     }
@@ -1397,6 +1456,9 @@ API int oibvh_scene_finish_frame(oibvh_scene_t s, void* stream)
     s->stats.passes = 1;
     s->stats.steps = s->frame_rounds;
     s->stats.nodes_tested = c[kCountTested];
+    s->stats.fp64_axes = c[kCountFp64Axes];
+    s->stats.fp64_candidates = c[kCountFp64Cands];
+    s->stats.fp32_disagreements = c[kCountDisagree];
     uint64_t peak = 0;
     for (uint32_t k = 0; k <= s->frame_rounds + 1; ++k) peak = std::max<uint64_t>(peak, c[kCountWork0 + k]);
     s->stats.front_peak = peak;

@@ -77,6 +77,7 @@ struct DetectArgs {
     uint32_t fuse_narrow;  // 1: test candidates in the traversal; 0: store them
     int grid;              // CTAs of the grid-stride / persistent kernels
     uint32_t handoff;      // front width at which k_top hands over to the walkers (<= 8192)
+    uint32_t precision;    // 0: float triangle test (reference arithmetic); 1: FP64-filtered
 };
 cudaError_t launch_init_front(const DetectArgs& a, uint32_t total0, cudaStream_t s);
 cudaError_t launch_top(const DetectArgs& a, cudaStream_t s);
@@ -85,11 +86,13 @@ int walk_blocks_per_sm();
 cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s);
 
 // counts[]: hits, flags, candidates found, candidate slots used (broad-only),
-// BVTT pairs tested, then the work-list size of each traversal round (list
+// BVTT pairs tested, (precision mode) axes evaluated in FP64, candidates with
+// at least one such axis, candidates whose float and FP64 answers differ,
+// then the work-list size of each traversal round (list
 // 0: the overlapping start pairs; list 1: the front k_top hands over; list
 // r+1: what walk round r spilled).
 constexpr uint32_t kMaxRounds = 16;
 constexpr uint32_t kCountHits = 0, kCountFlags = 1, kCountCands = 2, kCountCandSlots = 3, kCountTested = 4,
-                   kCountWork0 = 8, kCountTotal = kCountWork0 + kMaxRounds + 1;
+                   kCountFp64Axes = 5, kCountFp64Cands = 6, kCountDisagree = 7, kCountWork0 = 8, kCountTotal = kCountWork0 + kMaxRounds + 1;
 
 } // namespace oibvh

@@ -13,6 +13,13 @@ batched     `n_pairs` independent pairs of noise-displaced icospheres whose
             subdivision is drawn so triangle counts are log-uniform over
             1k..1M; each pair gets a seeded rigid transform that puts
             30..70% of B's surface inside A.
+sheets      `n_pairs` pairs of n x n-quad grid sheets (2n^2 triangles) with a
+            sine height field (amplitude 0.1, wavelength U(0.05, 0.5), seeded
+            direction and phase). B is the same surface sampled on the grid
+            shifted by n - round(0.1 n) columns, so its first 10% of columns
+            coincide with A's last ones; odd pairs also lift B by a seeded
+            dz in [-1e-7, 1e-7]. Those triangles are coplanar with A's (or
+            within 1e-7 of them): the precision stress.
 
 "Overlap fraction" of a pair = fraction of B's surface inside A's ball,
 computed from the sphere-cap area: for balls of radii a >= b at distance d
@@ -207,3 +214,65 @@ def noise_displace_mesh(subdiv: int, amplitude: float, seed: int) -> "M.Mesh":
     if subdiv not in _ICO_CACHE:
         _ICO_CACHE[subdiv] = M.icosphere(subdiv)
     return M.noise_displace(_ICO_CACHE[subdiv], amplitude, seed=seed)
+
+
+def sheet_pair_meshes(n: int, wavelength: float, theta: float, phase: float, dz: float,
+                      amplitude: float = 0.1, overlap: float = 0.1):
+    """Sheets A and B of one pair (float32 positions, uint32 faces).
+
+    Vertex (i, j) of a sheet whose first column is c0 sits at
+    x = (c0 + i) / n, y = j / n (exact in float32), height
+    z = amplitude * sin(2 pi (x cos(theta) + y sin(theta)) / wavelength + phase)
+    computed in float64 and rounded once; B's heights get `dz` added before
+    rounding. Faces split each quad (v00, v10, v11), (v00, v11, v01), row-major.
+    """
+    shift = n - int(round(overlap * n))
+
+    def sheet(c0: int, lift: float) -> "M.Mesh":
+        cols = np.arange(n + 1, dtype=np.float64) + c0
+        rows = np.arange(n + 1, dtype=np.float64)
+        x, y = np.meshgrid(cols / n, rows / n, indexing="xy")
+        x = x.reshape(-1)
+        y = y.reshape(-1)
+        arg = 2.0 * np.pi * (x * math.cos(theta) + y * math.sin(theta)) / wavelength + phase
+        z = amplitude * M._sin_poly(arg) + lift
+        xyz = np.stack([x, y, z], 1).astype(np.float32)
+        q = np.arange(n, dtype=np.int64)
+        qx, qy = np.meshgrid(q, q, indexing="xy")
+        v00 = (qy * (n + 1) + qx).reshape(-1)
+        v10, v01 = v00 + 1, v00 + (n + 1)
+        v11 = v01 + 1
+        tri = np.empty((2 * n * n, 3), dtype=np.int64)
+        tri[0::2] = np.stack([v00, v10, v11], 1)
+        tri[1::2] = np.stack([v00, v11, v01], 1)
+        return M.Mesh(xyz, tri.astype(np.uint32))
+
+    return sheet(0, 0.0), sheet(shift, dz)
+
+
+@dataclass
+class SheetWorkload:
+    name: str
+    meshes: list
+    pairs: list
+    info: dict = field(default_factory=dict)
+
+
+def sheets(n_pairs: int = 64, n: int = 256, seed: int = 4242, overlap: float = 0.1) -> SheetWorkload:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    meshes, pairs, lifts = [], [], []
+    for p in range(n_pairs):
+        wl = float(rng.uniform(0.05, 0.5))
+        theta = float(rng.uniform(0.0, 2.0 * math.pi))
+        phase = float(rng.uniform(0.0, 2.0 * math.pi))
+        dz = 0.0 if p % 2 == 0 else float(rng.uniform(-1e-7, 1e-7))
+        a, b = sheet_pair_meshes(n, wl, theta, phase, dz, overlap=overlap)
+        meshes += [a, b]
+        pairs.append((2 * p, 2 * p + 1))
+        lifts.append(dz)
+    w = SheetWorkload(f"sheets: {n_pairs} pairs of {n}x{n}-quad sine sheets, {overlap:.0%} coplanar or within 1e-7",
+                      meshes, pairs)
+    w.info = {"n_pairs": n_pairs, "quads": n, "triangles_per_sheet": 2 * n * n, "vertices_per_sheet": (n + 1) ** 2,
+              "overlap_columns": int(round(overlap * n)), "lifted_pairs": int(sum(1 for d in lifts if d != 0.0)),
+              "triangles_total": 2 * n * n * 2 * n_pairs}
+    return w

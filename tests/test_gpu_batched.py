@@ -87,6 +87,8 @@ def test_captured_frame_graph_vs_oracle(gpu):
         want, wc = _oracle(w.positions(frame), [m.tri for m in w.rest], w.pairs)
         assert np.array_equal(sc.int_tri_pairs(), want), f"frame {frame}"
         assert sc.candidate_count() == wc
+    # the captured walk rounds cover these frames: none was redone synchronously
+    assert sc.stats()["frame_redos"] == 0
 
 
 def test_frame_graph_recovers_from_small_queues(gpu):

@@ -40,3 +40,32 @@ def mixed_scene(seed):
         pick = rng.choice(len(allp), size=min(5, len(allp)), replace=False)
         pairs = np.array([allp[i] for i in pick], dtype=np.uint32)
     return meshes, pairs
+
+
+def near_degenerate_pair(seed, n_tri=2000):
+    """Triangles built to sit on the float/FP64 boundary: B holds, for each
+    A triangle, one that shares an edge (folded by a tiny angle), one that is
+    coplanar and shifted in-plane, one that touches at a vertex, and one lifted
+    off the plane by a few ulps."""
+    rng = np.random.Generator(np.random.PCG64(5000 + seed))
+    base = rng.uniform(-1.0, 1.0, size=(n_tri, 1, 3))
+    A = (base + rng.uniform(-0.05, 0.05, size=(n_tri, 3, 3))).astype(np.float64)
+    out = []
+    for t in A:
+        p0, p1, p2 = t
+        n = np.cross(p1 - p0, p2 - p0)
+        n /= np.linalg.norm(n)
+        eps = float(rng.choice([0.0, 1e-9, 1e-8, 1e-7, 1e-6]))
+        # folded about edge p0-p1
+        out.append([p0, p1, p2 + eps * n + (p0 - p2) * 0.5])
+        # coplanar, shifted in-plane
+        d = (p1 - p0) * rng.uniform(-0.6, 0.6)
+        out.append([p0 + d, p1 + d, p2 + d])
+        # touching at a vertex
+        out.append([p2, p2 + (p2 - p0) * 0.7 + eps * n, p2 + (p2 - p1) * 0.7])
+        # lifted by eps
+        out.append([p0 + eps * n, p1 + eps * n, p2 + eps * n])
+    B = np.asarray(out, dtype=np.float64)
+    ma = M.Mesh(A.reshape(-1, 3).astype(np.float32), np.arange(3 * n_tri, dtype=np.uint32).reshape(-1, 3))
+    mb = M.Mesh(B.reshape(-1, 3).astype(np.float32), np.arange(3 * len(out), dtype=np.uint32).reshape(-1, 3))
+    return ma, mb
