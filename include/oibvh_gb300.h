@@ -265,6 +265,67 @@ int oibvh_scene_get_stats(oibvh_scene_t s, oibvh_detect_stats* out);
 
 int oibvh_scene_destroy(oibvh_scene_t s);
 
+/* ------------------------------------------------------------ serving */
+
+/* A request loop over a pool of resident meshes with continuous batching.
+ * No counterpart in the reference (its Scene detects a fixed set of meshes
+ * per call, src/cuda/scene.cu:157-185); each query runs the reference's
+ * steps for one pair: B transformed by a rigid transform (Mesh::transform),
+ * B's tree refit (OibvhTree::refit), broad + narrow phase against A at rest
+ * (Scene::detectCollision).
+ *
+ * create: a device arena of memory_budget_bytes holds one slot per admitted
+ * query (B's transformed positions and tree boxes, 16 B per vertex + 32 B per
+ * internal node), allocated up front; n_lanes CUDA streams each carry one
+ * batch at a time (at most max_batch queries). add_mesh registers built
+ * trees (their current positions are the rest positions; the trees must
+ * outlive the server); start launches the loop thread. submit is
+ * thread-safe and returns at once; a query waits until its slot fits in the
+ * arena (FIFO) and a lane is idle, then runs with every query admitted at
+ * that moment. wait blocks until the query is done (OIBVH_ERR_TIMEOUT after
+ * timeout_ms); get_pairs returns its (triA, triB) pairs, original face
+ * indices, 2 uint32 each; release frees its record. A query's pair set does
+ * not depend on what it was batched with. destroy finishes the queries
+ * already submitted, then stops. */
+typedef struct oibvh_server_s* oibvh_server_t;
+enum {
+    OIBVH_QUERY_QUEUED = 0,
+    OIBVH_QUERY_RUNNING = 1,
+    OIBVH_QUERY_DONE = 2,
+    OIBVH_QUERY_FAILED = 3,
+};
+typedef struct oibvh_query_result {
+    int status;           /* OIBVH_QUERY_* */
+    int error;            /* OIBVH_OK, or the status of its failed batch */
+    uint32_t lane;        /* lane (stream) it ran on */
+    uint32_t batch_size;  /* queries launched with it */
+    uint64_t n_pairs;     /* colliding triangle pairs */
+    double queue_us;      /* submit -> launch */
+    double service_us;    /* launch -> results on the host */
+} oibvh_query_result;
+typedef struct oibvh_server_stats {
+    uint64_t submitted, completed, failed;
+    uint64_t batches, max_batch_seen;
+    uint64_t redos;              /* batches redone with larger queues */
+    uint64_t candidates, hits;
+    uint64_t arena_bytes, arena_used_bytes, arena_peak_bytes;
+    uint64_t queued;             /* waiting for admission */
+} oibvh_server_stats;
+int oibvh_server_create(int device, uint64_t memory_budget_bytes, uint32_t max_batch, uint32_t n_lanes,
+                        oibvh_server_t* out);
+int oibvh_server_set_entry_level(oibvh_server_t s, uint32_t entry_level);
+/* Starting capacities (entries) of each lane's BVTT work lists and hit
+ * queue; they grow on demand (the batch is redone). 0 keeps a value. */
+int oibvh_server_set_queue_capacity(oibvh_server_t s, uint32_t front, uint32_t hits);
+int oibvh_server_add_mesh(oibvh_server_t s, oibvh_tree_t t, uint32_t* id);
+int oibvh_server_start(oibvh_server_t s);
+int oibvh_server_submit(oibvh_server_t s, uint32_t mesh_a, uint32_t mesh_b, const float* mat_b, uint64_t* ticket);
+int oibvh_server_wait(oibvh_server_t s, uint64_t ticket, uint32_t timeout_ms, oibvh_query_result* out);
+int oibvh_server_get_pairs(oibvh_server_t s, uint64_t ticket, uint32_t* out2, uint64_t cap, uint64_t* n);
+int oibvh_server_release(oibvh_server_t s, uint64_t ticket);
+int oibvh_server_get_stats(oibvh_server_t s, oibvh_server_stats* out);
+int oibvh_server_destroy(oibvh_server_t s);
+
 /* ------------------------------------------------------- no allocation */
 
 /* Collision detection for ONE mesh pair (tree a against tree b) that

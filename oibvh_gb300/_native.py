@@ -28,6 +28,7 @@ ERR_UNSUPPORTED = 6
 ERR_TIMEOUT = 7
 PRECISION_FP32 = 0
 PRECISION_FP64_FILTERED = 1
+QUERY_QUEUED, QUERY_RUNNING, QUERY_DONE, QUERY_FAILED = 0, 1, 2, 3
 
 DEVICE_CPU = -1
 
@@ -46,6 +47,24 @@ class DetectStats(ctypes.Structure):
         ("fp64_candidates", ctypes.c_uint64),
         ("fp32_disagreements", ctypes.c_uint64),
     ]
+
+
+class QueryResult(ctypes.Structure):
+    _fields_ = [
+        ("status", ctypes.c_int),
+        ("error", ctypes.c_int),
+        ("lane", ctypes.c_uint32),
+        ("batch_size", ctypes.c_uint32),
+        ("n_pairs", ctypes.c_uint64),
+        ("queue_us", ctypes.c_double),
+        ("service_us", ctypes.c_double),
+    ]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_uint64) for k in (
+        "submitted", "completed", "failed", "batches", "max_batch_seen", "redos", "candidates", "hits",
+        "arena_bytes", "arena_used_bytes", "arena_peak_bytes", "queued")]
 
 
 class Tuning(ctypes.Structure):
@@ -103,6 +122,17 @@ SIGNATURES = [
     ("oibvh_scene_get_stats", ctypes.c_int, [_vp, ctypes.POINTER(DetectStats)]),
     ("oibvh_scene_destroy", ctypes.c_int, [_vp]),
     ("oibvh_pair_detect_noalloc", ctypes.c_int, [_vp, _vp, _u32, _vp, _u32, _u32p, _vp]),
+    ("oibvh_server_create", ctypes.c_int, [ctypes.c_int, _u64, _u32, _u32, ctypes.POINTER(_vp)]),
+    ("oibvh_server_set_entry_level", ctypes.c_int, [_vp, _u32]),
+    ("oibvh_server_set_queue_capacity", ctypes.c_int, [_vp, _u32, _u32]),
+    ("oibvh_server_add_mesh", ctypes.c_int, [_vp, _vp, _u32p]),
+    ("oibvh_server_start", ctypes.c_int, [_vp]),
+    ("oibvh_server_submit", ctypes.c_int, [_vp, _u32, _u32, _f32p, ctypes.POINTER(_u64)]),
+    ("oibvh_server_wait", ctypes.c_int, [_vp, _u64, _u32, ctypes.POINTER(QueryResult)]),
+    ("oibvh_server_get_pairs", ctypes.c_int, [_vp, _u64, _u32p, _u64, ctypes.POINTER(_u64)]),
+    ("oibvh_server_release", ctypes.c_int, [_vp, _u64]),
+    ("oibvh_server_get_stats", ctypes.c_int, [_vp, ctypes.POINTER(ServerStats)]),
+    ("oibvh_server_destroy", ctypes.c_int, [_vp]),
 ]
 
 _lib = None

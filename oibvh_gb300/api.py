@@ -22,7 +22,7 @@ import numpy as np
 from . import _native as N
 from .meshes import Mesh
 
-__all__ = ["DeviceType", "OibvhTree", "Scene", "OibvhError"]
+__all__ = ["DeviceType", "OibvhTree", "Scene", "Server", "OibvhError"]
 
 OibvhError = N.OibvhError
 
@@ -314,3 +314,83 @@ class Scene:
         st = N.DetectStats()
         N.check(N.lib().oibvh_scene_get_stats(self._h, ctypes.byref(st)), "oibvh_scene_get_stats")
         return {k: int(getattr(st, k)) for k, _ in N.DetectStats._fields_}
+
+
+class Server:
+    """Continuous-batching request loop over a pool of resident meshes
+    (oibvh_server_* in include/oibvh_gb300.h). A query is (mesh A, mesh B,
+    3x4 rigid transform of B); its result is B-transformed against A at rest.
+
+        srv = Server(memory_budget=8 << 30, max_batch=256, lanes=4)
+        ids = [srv.add_mesh(t) for t in trees]   # built OibvhTree objects
+        srv.start()
+        t = srv.submit(ids[0], ids[1], mat12)
+        info = srv.wait(t); pairs = srv.pairs(t); srv.release(t)
+    """
+
+    def __init__(self, device: int = 0, memory_budget: int = 1 << 30, max_batch: int = 256, lanes: int = 4):
+        h = ctypes.c_void_p()
+        N.check(N.lib().oibvh_server_create(int(device), int(memory_budget), int(max_batch), int(lanes),
+                                            ctypes.byref(h)), "oibvh_server_create")
+        self._h = h
+        self._trees = []  # the pool trees must outlive the server
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            N.lib().oibvh_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_entry_level(self, level: int) -> None:
+        N.check(N.lib().oibvh_server_set_entry_level(self._h, int(level)), "oibvh_server_set_entry_level")
+
+    def set_queue_capacity(self, front: int = 0, hits: int = 0) -> None:
+        N.check(N.lib().oibvh_server_set_queue_capacity(self._h, int(front), int(hits)),
+                "oibvh_server_set_queue_capacity")
+
+    def add_mesh(self, tree: "OibvhTree") -> int:
+        i = ctypes.c_uint32()
+        N.check(N.lib().oibvh_server_add_mesh(self._h, tree.handle, ctypes.byref(i)), "oibvh_server_add_mesh")
+        self._trees.append(tree)
+        return int(i.value)
+
+    def start(self) -> None:
+        N.check(N.lib().oibvh_server_start(self._h), "oibvh_server_start")
+
+    def submit(self, mesh_a: int, mesh_b: int, mat_b) -> int:
+        m = np.ascontiguousarray(np.asarray(mat_b, dtype=np.float32).reshape(12))
+        t = ctypes.c_uint64()
+        N.check(N.lib().oibvh_server_submit(self._h, int(mesh_a), int(mesh_b), m.ctypes.data_as(N._f32p),
+                                            ctypes.byref(t)), "oibvh_server_submit")
+        return int(t.value)
+
+    def wait(self, ticket: int, timeout_ms: int = 60000) -> dict:
+        r = N.QueryResult()
+        N.check(N.lib().oibvh_server_wait(self._h, int(ticket), int(timeout_ms), ctypes.byref(r)), "oibvh_server_wait")
+        return {k: getattr(r, k) for k, _ in N.QueryResult._fields_}
+
+    def pairs(self, ticket: int) -> np.ndarray:
+        """uint32[n, 2] (triA, triB) with original face indices, sorted."""
+        n = ctypes.c_uint64()
+        N.check(N.lib().oibvh_server_get_pairs(self._h, int(ticket), None, 0, ctypes.byref(n)),
+                "oibvh_server_get_pairs")
+        out = np.empty((max(int(n.value), 1), 2), dtype=np.uint32)
+        N.check(N.lib().oibvh_server_get_pairs(self._h, int(ticket), out.ctypes.data_as(N._u32p), int(n.value),
+                                               ctypes.byref(n)), "oibvh_server_get_pairs")
+        out = out[: int(n.value)]
+        if out.shape[0]:
+            out = out[np.lexsort((out[:, 1], out[:, 0]))]
+        return out
+
+    def release(self, ticket: int) -> None:
+        N.check(N.lib().oibvh_server_release(self._h, int(ticket)), "oibvh_server_release")
+
+    def stats(self) -> dict:
+        st = N.ServerStats()
+        N.check(N.lib().oibvh_server_get_stats(self._h, ctypes.byref(st)), "oibvh_server_get_stats")
+        return {k: int(getattr(st, k)) for k, _ in N.ServerStats._fields_}

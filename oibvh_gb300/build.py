@@ -20,7 +20,7 @@ LIBDIR = os.path.join(HERE, "_lib")
 LIBNAME = "liboibvh_gb300.so"
 LIB = os.path.join(LIBDIR, LIBNAME)
 OBJDIR = os.path.join(LIBDIR, "obj")
-SOURCES = ["build_kernels.cu", "refit_kernels.cu", "detect_kernels.cu", "host.cu", "noalloc.cu"]
+SOURCES = ["build_kernels.cu", "refit_kernels.cu", "detect_kernels.cu", "host.cu", "noalloc.cu", "serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -473,7 +473,8 @@ __global__ void __launch_bounds__(256) k_transform_multi(const BuildJob* __restr
     const BuildJob& job = jobs[j];
     const uint32_t v = (blockIdx.x - job.vblock_begin) * blockDim.x + threadIdx.x;
     if (v >= job.nV) return;
-    const float4 p = __ldg(rest + job.vert_off + v);
+    // packed rest positions of all jobs, or (rest == nullptr) each job's own source
+    const float4 p = __ldg(rest ? rest + job.vert_off + v : job.pos + v);
     const float* m = mats + 12 * (size_t)j;
     float o[3];
 #pragma unroll

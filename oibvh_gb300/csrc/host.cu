@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "../../include/oibvh_gb300.h"
+#include "host_util.h"
 #include "oibvh_common.cuh"
 #include "oibvh_launch.h"
 
@@ -32,178 +33,9 @@ static std::atomic<uint64_t> g_launches{0};
 void note_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 }  // namespace oibvh
 
-namespace {
-
+namespace oibvh_host {
 thread_local std::string g_last_error;
-
-int fail(int code, const std::string& msg)
-{
-    g_last_error = msg;
-    return code;
-}
-
-int cuda_fail(cudaError_t e, const char* what)
-{
-    const int code = (e == cudaErrorMemoryAllocation) ? OIBVH_ERR_OOM : OIBVH_ERR_CUDA;
-    g_last_error = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
-    return code;
-}
-
-#define CUDA_TRY(expr)                                   \
-    do {                                                 \
-        cudaError_t _e = (expr);                         \
-        if (_e != cudaSuccess) return cuda_fail(_e, #expr); \
-    } while (0)
-
-#define OK_TRY(expr)              \
-    do {                          \
-        int _s = (expr);          \
-        if (_s != OIBVH_OK) return _s; \
-    } while (0)
-
-struct DeviceGuard {
-    int prev = -1;
-    bool ok = true;
-    explicit DeviceGuard(int dev)
-    {
-        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-        if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
-    }
-    ~DeviceGuard()
-    {
-        int cur = -1;
-        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
-    }
-};
-
-int sm_count(int dev)
-{
-    static int cache[64] = {};
-    if (dev >= 0 && dev < 64 && cache[dev]) return cache[dev];
-    int n = 0;
-    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
-    if (dev >= 0 && dev < 64) cache[dev] = n;
-    return n;
-}
-
-template <class T>
-struct DevBuf {
-    T* p = nullptr;
-    size_t n = 0;
-    DevBuf() = default;
-    DevBuf(const DevBuf&) = delete;
-    DevBuf& operator=(const DevBuf&) = delete;
-    ~DevBuf() { release(); }
-    void release()
-    {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-    // grow to at least `want` elements; contents are not kept
-    int ensure(size_t want, const char* what)
-    {
-        if (want <= n && p) return OIBVH_OK;
-        release();
-        if (want == 0) want = 1;
-        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
-        if (e != cudaSuccess) {
-            p = nullptr;
-            cudaGetLastError();
-            return cuda_fail(e, what);
-        }
-        n = want;
-        return OIBVH_OK;
-    }
-    // grow keeping the first `keep` elements (stream-ordered copy)
-    int grow_keep(size_t want, size_t keep, cudaStream_t s, const char* what)
-    {
-        if (want <= n && p) return OIBVH_OK;
-        T* q = nullptr;
-        cudaError_t e = cudaMalloc(&q, want * sizeof(T));
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            return cuda_fail(e, what);
-        }
-        if (p && keep) {
-            e = cudaMemcpyAsync(q, p, std::min(keep, n) * sizeof(T), cudaMemcpyDeviceToDevice, s);
-            if (e != cudaSuccess) {
-                cudaFree(q);
-                return cuda_fail(e, what);
-            }
-            e = cudaStreamSynchronize(s);
-            if (e != cudaSuccess) {
-                cudaFree(q);
-                return cuda_fail(e, what);
-            }
-        }
-        release();
-        p = q;
-        n = want;
-        return OIBVH_OK;
-    }
-};
-
-template <class T>
-struct PinnedBuf {
-    T* p = nullptr;
-    size_t n = 0;
-    PinnedBuf() = default;
-    PinnedBuf(const PinnedBuf&) = delete;
-    PinnedBuf& operator=(const PinnedBuf&) = delete;
-    ~PinnedBuf()
-    {
-        if (p) cudaFreeHost(p);
-    }
-    int ensure(size_t want, const char* what)
-    {
-        if (want <= n && p) return OIBVH_OK;
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        n = 0;
-        if (want == 0) want = 1;
-        cudaError_t e = cudaMallocHost(&p, want * sizeof(T));
-        if (e != cudaSuccess) {
-            p = nullptr;
-            cudaGetLastError();
-            return cuda_fail(e, what);
-        }
-        n = want;
-        return OIBVH_OK;
-    }
-};
-
-}  // namespace
-
-// ============================================================================
-// Tree
-// ============================================================================
-struct oibvh_tree_s {
-    int device = 0;
-    uint32_t nV = 0, nT = 0;
-    TreeShape shape{};
-    DevBuf<float> xyz;          // staging for positions given as xyz (3 * nV)
-    DevBuf<float4> pos4;        // owned positions in the device layout (x, y, z, 0)
-    const float4* cur_pos = nullptr;  // positions the next refit / detect use (owned or borrowed)
-    DevBuf<uint32_t> tri;       // faces as given (3 * nT)
-    DevBuf<uint4> face;         // Morton-ordered faces (v0, v1, v2, original index)
-    DevBuf<float4> box;         // 2 * (size - nT): internal nodes only
-    DevBuf<uint32_t> counters;  // refit climbing counters
-    bool built = false;
-
-    RefitJob job() const
-    {
-        RefitJob j{};
-        j.box = box.p;
-        j.face = face.p;
-        j.pos = cur_pos;
-        j.shape = shape;
-        j.block_begin = 0;
-        j.n_blocks = refit_blocks_for(nT);
-        j.counters = counters.p;
-        return j;
-    }
-};
+}  // namespace oibvh_host
 
 static int tree_alloc(oibvh_tree_t t)
 {

@@ -26,7 +26,7 @@ struct RefitJob {
 
 // One tree of a multi-tree build / transform launch.
 struct BuildJob {
-    const float4* pos;      // positions to build from
+    const float4* pos;      // positions to build from (transform source when no packed rest array is given)
     const uint32_t* tri;    // faces as given (3 * nT)
     uint4* face_out;        // Morton-ordered face records
     uint32_t* bound_keys;   // 6 words of scratch (mesh bounds)

@@ -13,6 +13,12 @@ batched     `n_pairs` independent pairs of noise-displaced icospheres whose
             subdivision is drawn so triangle counts are log-uniform over
             1k..1M; each pair gets a seeded rigid transform that puts
             30..70% of B's surface inside A.
+serving     a pool of `n_meshes` noise-displaced icospheres, subdivision drawn
+            so triangle counts are log-uniform over 500..2M (s = 3..8, a few
+            noise variants per subdivision, each pool entry its own resident
+            tree), and a seeded stream of queries (mesh A, mesh B, rigid
+            transform of B: random rotation, translation of length
+            U(0.3, 1.8) so that most pairs overlap partially).
 sheets      `n_pairs` pairs of n x n-quad grid sheets (2n^2 triangles) with a
             sine height field (amplitude 0.1, wavelength U(0.05, 0.5), seeded
             direction and phase). B is the same surface sampled on the grid
@@ -93,10 +99,10 @@ def deforming(subdiv: int = 8, seed: int = 2024, overlap: float = 0.01, noise: f
 _BATCH_SUBDIVS = (3, 4, 5, 6, 7)
 
 
-def _subdiv_probs(lo: float = 1e3, hi: float = 1e6) -> np.ndarray:
+def _subdiv_probs(lo: float = 1e3, hi: float = 1e6, subdivs=_BATCH_SUBDIVS) -> np.ndarray:
     """Probability of each subdivision so that log(T) is uniform over [lo, hi]:
     each s takes the log-mass of the interval around its T (midpoints in log space)."""
-    logs = np.array([math.log(20 * 4 ** s) for s in _BATCH_SUBDIVS])
+    logs = np.array([math.log(20 * 4 ** s) for s in subdivs])
     edges = np.concatenate([[math.log(lo)], (logs[1:] + logs[:-1]) / 2, [math.log(hi)]])
     w = np.clip(np.diff(edges), 0, None)
     return w / w.sum()
@@ -139,19 +145,22 @@ class BatchWorkload:
         x' = ((m0 x + m1 y) + m2 z) + m3 with float32 rounding at each step."""
         mats = self.matrices(frame)
         idx = range(len(self.rest)) if which is None else which
-        res = []
-        for i in idx:
-            m, M = self.rest[i], mats[i]
-            x, y, z = (m.xyz[:, k] for k in range(3))
-            rows = []
-            for r in range(3):
-                a = (M[4 * r] * x + M[4 * r + 1] * y) + M[4 * r + 2] * z
-                rows.append((a + M[4 * r + 3]).astype(np.float32))
-            res.append(np.stack(rows, 1))
-        return res
+        return [rigid_apply(self.rest[i].xyz, mats[i]) for i in idx]
 
     def packed_rest_xyzw(self) -> np.ndarray:
         return np.concatenate([np.pad(m.xyz, ((0, 0), (0, 1))) for m in self.rest], 0).astype(np.float32)
+
+
+def rigid_apply(xyz: np.ndarray, mat12) -> np.ndarray:
+    """x' = ((m0 x + m1 y) + m2 z) + m3 per row, float32 rounding at each
+    step: the device transform's arithmetic (row-major 3x4 matrix)."""
+    M = np.asarray(mat12, dtype=np.float32).reshape(12)
+    x, y, z = (np.asarray(xyz, dtype=np.float32)[:, k] for k in range(3))
+    rows = []
+    for r in range(3):
+        a = (M[4 * r] * x + M[4 * r + 1] * y) + M[4 * r + 2] * z
+        rows.append((a + M[4 * r + 3]).astype(np.float32))
+    return np.stack(rows, 1)
 
 
 def _axis_angle(axis, ang):
@@ -275,4 +284,49 @@ def sheets(n_pairs: int = 64, n: int = 256, seed: int = 4242, overlap: float = 0
     w.info = {"n_pairs": n_pairs, "quads": n, "triangles_per_sheet": 2 * n * n, "vertices_per_sheet": (n + 1) ** 2,
               "overlap_columns": int(round(overlap * n)), "lifted_pairs": int(sum(1 for d in lifts if d != 0.0)),
               "triangles_total": 2 * n * n * 2 * n_pairs}
+    return w
+
+
+_SERVE_SUBDIVS = (3, 4, 5, 6, 7, 8)
+
+
+@dataclass
+class ServingWorkload:
+    name: str
+    meshes: list        # pool entry -> mesh (entries share the variant meshes)
+    variant_of: list    # pool entry -> (subdivision, variant)
+    info: dict = field(default_factory=dict)
+
+    def queries(self, n: int, seed: int = 1):
+        """n queries: (mesh A, mesh B, float32[12] row-major 3x4 transform of B)."""
+        from . import meshes as M
+
+        rng = np.random.Generator(np.random.PCG64(seed))
+        ab = rng.integers(0, len(self.meshes), size=(n, 2))
+        mats = np.empty((n, 12), dtype=np.float32)
+        for k in range(n):
+            R = M.random_rotation(rng)
+            t = _unit_vector(rng) * float(rng.uniform(0.3, 1.8))
+            mats[k] = np.concatenate([R, t[:, None]], 1).reshape(12)
+        return ab.astype(np.uint32), mats
+
+
+def serving(n_meshes: int = 2000, seed: int = 5150, variants: int = 3, noise: float = 0.05,
+            lo: float = 500.0, hi: float = 2e6) -> ServingWorkload:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    probs = _subdiv_probs(lo, hi, _SERVE_SUBDIVS)
+    cache = {}
+    meshes, var = [], []
+    for _ in range(n_meshes):
+        s_ = int(rng.choice(_SERVE_SUBDIVS, p=probs))
+        k = int(rng.integers(0, variants))
+        if (s_, k) not in cache:
+            cache[(s_, k)] = noise_displace_mesh(s_, noise, seed * 1000 + 10 * s_ + k)
+        meshes.append(cache[(s_, k)])
+        var.append((s_, k))
+    tri = np.array([m.n_triangles for m in meshes], dtype=np.int64)
+    w = ServingWorkload(f"serving: pool of {n_meshes} noise icospheres, T log-uniform 500-2M", meshes, var)
+    w.info = {"pool_meshes": n_meshes, "triangles_total": int(tri.sum()), "triangles_min": int(tri.min()),
+              "triangles_max": int(tri.max()), "triangles_mean": float(tri.mean()),
+              "distinct_host_meshes": len(cache)}
     return w
