@@ -52,7 +52,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["batched", "precision", "deforming", "plain"], default="batched")
+    ap.add_argument("--workload", choices=["batched", "precision", "serving", "deforming", "plain"], default="batched")
+    ap.add_argument("--rates", default="1000,3000,10000,30000,100000", help="serving: offered query rates (1/s)")
+    ap.add_argument("--pool", type=int, default=2000, help="serving: resident meshes")
+    ap.add_argument("--budget-gb", type=float, default=16.0, help="serving: device memory budget for query slots")
     ap.add_argument("--pairs", type=int, default=512, help="mesh pairs of the batched workload")
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -1080,14 +1083,225 @@ def run_reference_precision(args, rank, world):
             "e2e": {"value": round(value, 3), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# --------------------------------------------------------------------------- serving workload
+def run_ours_serving(args, rank, world, local):
+    """A pool of resident meshes (2,000 noise icospheres, T log-uniform
+    500..2M) behind the continuous-batching server; Poisson query streams at
+    each offered rate; per-query latency = (submit - scheduled arrival) +
+    queue + service (launch to results on the host). The plain path is the
+    same queries one at a time (each alone on the GPU)."""
+    import ctypes as C
+
+    import torch
+
+    from oibvh_gb300 import OibvhTree, Scene, Server, _native
+    from oibvh_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    dev = local
+    t0 = time.perf_counter()
+    w = W.serving(args.pool)
+    trees = [OibvhTree(m, device=dev) for m in w.meshes]
+    sc = Scene(dev)
+    for t in trees:
+        sc.addOibvhTree(t)
+    sc.build()  # one launch per build stage for the whole pool
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    srv = Server(dev, int(args.budget_gb * (1 << 30)), 4096, 4)
+    for t in trees:
+        srv.add_mesh(t)
+    srv.start()
+    L = _native.lib()
+    rates = [float(r) for r in args.rates.split(",") if r]
+    sampler = ClockSampler(dev) if rank == 0 else None
+    if sampler:
+        sampler.start()
+
+    def run_stream(rate, n, seed):
+        ab, mats = w.queries(n, seed=seed)
+        rng = np.random.Generator(np.random.PCG64(seed + 7))
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
+        mp = mats.ctypes.data
+        tickets = np.empty(n, dtype=np.uint64)
+        lag = np.empty(n, dtype=np.float64)
+        tk = C.c_uint64()
+        submit = L.oibvh_server_submit
+        start = time.perf_counter() + 0.002
+        for k in range(n):
+            target = start + arrivals[k]
+            now = time.perf_counter()
+            while now < target:
+                now = time.perf_counter()
+            st = submit(srv._h, int(ab[k, 0]), int(ab[k, 1]), C.cast(C.c_void_p(mp + 48 * k), _native._f32p),
+                        C.byref(tk))
+            if st:
+                raise RuntimeError(L.oibvh_last_error().decode())
+            tickets[k] = tk.value
+            lag[k] = now - target
+        lat = np.empty(n)
+        sizes = np.empty(n)
+        pairs = 0
+        r = _native.QueryResult()
+        t_last = 0.0
+        for k in range(n):
+            _native.check(L.oibvh_server_wait(srv._h, int(tickets[k]), 600000, C.byref(r)), "oibvh_server_wait")
+            lat[k] = 1e3 * lag[k] + (r.queue_us + r.service_us) / 1e3
+            sizes[k] = r.batch_size
+            pairs += r.n_pairs
+            t_last = max(t_last, arrivals[k] + lag[k] + (r.queue_us + r.service_us) / 1e6)
+            L.oibvh_server_release(srv._h, int(tickets[k]))
+        return {"offered_per_s": rate, "queries": n, "throughput_per_s": round(n / t_last, 1),
+                "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 4),
+                               "p99": round(float(np.percentile(lat, 99)), 4),
+                               "max": round(float(lat.max()), 4)},
+                "mean_batch": round(float(sizes.mean()), 2), "pairs": int(pairs)}
+
+    # warm-up stream (lane buffers grow to their working sizes)
+    run_stream(2000.0, 2000, seed=99)
+    sweep = []
+    for i, rate in enumerate(rates):
+        n = int(min(max(2000, rate * 0.4), 40000))
+        sweep.append(run_stream(rate, n, seed=1000 + i))
+    clocks = sampler.stop() if sampler else None
+
+    # plain: the same kind of queries one at a time, each alone on the GPU
+    n_plain = 400
+    ab, mats = w.queries(n_plain, seed=4242)
+    plain_lat = []
+    tp0 = time.perf_counter()
+    r = _native.QueryResult()
+    tk = C.c_uint64()
+    for k in range(n_plain):
+        q0 = time.perf_counter()
+        _native.check(L.oibvh_server_submit(srv._h, int(ab[k, 0]), int(ab[k, 1]),
+                                            C.cast(C.c_void_p(mats.ctypes.data + 48 * k), _native._f32p),
+                                            C.byref(tk)), "oibvh_server_submit")
+        _native.check(L.oibvh_server_wait(srv._h, tk.value, 600000, C.byref(r)), "oibvh_server_wait")
+        L.oibvh_server_release(srv._h, tk.value)
+        plain_lat.append(1e3 * (time.perf_counter() - q0))
+    plain_qps = n_plain / (time.perf_counter() - tp0)
+    st = srv.stats()
+    srv.close()
+    top = max(sweep, key=lambda x: x["throughput_per_s"])
+    line = {
+        "metric": "served collision queries/s (Poisson arrivals, continuous batching) with p50/p99 latency",
+        "value": top["throughput_per_s"], "unit": "queries/s", "n_gpus": world, "steps": len(rates),
+        "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded noise icospheres, seeded query stream)",
+        "config": {"workload": w.name, **w.info, "memory_budget_gb": args.budget_gb, "lanes": 4,
+                   "max_batch": 4096, "entry_level": 4, "parallelism": f"replicas{world}",
+                   "l2": "inputs far larger than L2 (pool of " + str(w.info["triangles_total"]) + " triangles)"},
+        "sweep": sweep,
+        "plain_one_at_a_time": {"queries_per_s": round(plain_qps, 1),
+                                "latency_ms": {"p50": round(float(np.percentile(plain_lat, 50)), 4),
+                                               "p99": round(float(np.percentile(plain_lat, 99)), 4)}},
+        "served_over_plain": round(top["throughput_per_s"] / plain_qps, 2),
+        "server_stats": st,
+        "e2e": {"value": top["throughput_per_s"], "unit": "queries/s", "h2d_bytes_per_step": 48,
+                "d2h_bytes_per_step": None, "note": "every served query is end to end: host submit -> host pairs"},
+        "gpu_launches": None,
+        "clocks": clocks,
+        "setup_s": round(setup_s, 2),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_serving(w, args.cpu_seconds)
+    return line
+
+
+def cpu_baseline_serving(w, seconds):
+    """The reference CPU path per query on 1 core: B's SimpleBVH refit to the
+    transformed positions, then detect against A (both meshes resident)."""
+    from oracle.oracle import Port
+    from oibvh_gb300 import workloads as W
+
+    ab, mats = w.queries(64, seed=777)
+    t0 = time.perf_counter()
+    n = 0
+    ports = {}
+    t_run = 0.0
+    for k in range(64):
+        a, b = int(ab[k, 0]), int(ab[k, 1])
+        if (a, b) not in ports:
+            p = Port()
+            p.add_mesh(w.meshes[a].xyz, w.meshes[a].tri)
+            p.add_mesh(w.meshes[b].xyz, w.meshes[b].tri)
+            ports[(a, b)] = p
+        p = ports[(a, b)]
+        xb = W.rigid_apply(w.meshes[b].xyz, mats[k])
+        q0 = time.perf_counter()
+        p.set_positions(1, xb)
+        p.detect()
+        t_run += time.perf_counter() - q0
+        n += 1
+        del ports[(a, b)]
+        if time.perf_counter() - t0 > seconds:
+            break
+    return {"value": round(n / t_run, 3), "unit": "queries/s", "cores": 1, "kind": "port",
+            "sample": f"{n} queries of the stream (refit B + detect; BVH build and the transform untimed), "
+                      f"{t_run:.1f} s"}
+
+
+def run_reference_serving(args, rank, world):
+    """The reference CPU path on every host core: queries of the stream run
+    independently, one per thread, refit + detect each."""
+    if rank != 0:
+        return None
+    from oracle.oracle import Port
+    from oibvh_gb300 import workloads as W
+
+    w = W.serving(args.pool)
+    threads = os.cpu_count() or 1
+    ab, mats = w.queries(threads, seed=777)
+    ports = []
+    for k in range(threads):
+        a, b = int(ab[k, 0]), int(ab[k, 1])
+        p = Port()
+        p.add_mesh(w.meshes[a].xyz, w.meshes[a].tri)
+        p.add_mesh(w.meshes[b].xyz, w.meshes[b].tri)
+        ports.append((p, W.rigid_apply(w.meshes[b].xyz, mats[k])))
+
+    def one_step():
+        def work(k):
+            p, xb = ports[k]
+            p.set_positions(1, xb)
+            p.detect()
+
+        tt = [threading.Thread(target=work, args=(k,)) for k in range(threads)]
+        for t in tt:
+            t.start()
+        for t in tt:
+            t.join()
+
+    for _ in range(args.warmup):
+        one_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        one_step()
+    el = time.perf_counter() - t0
+    value = args.steps * threads / el
+    return {"metric": "served collision queries/s (Poisson arrivals, continuous batching) with p50/p99 latency",
+            "value": round(value, 3), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1e3 * el / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded noise icospheres, seeded query stream)",
+            "config": {"workload": w.name, **w.info, "parallelism": f"{threads} host threads, 1 query each"},
+            "impl": "reference",
+            "cpu_baseline": {"value": round(value, 3), "unit": "queries/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps * threads} queries (refit B + detect), {threads} per step"},
+            "e2e": {"value": round(value, 3), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
-        line = {"batched": run_reference_batched, "precision": run_reference_precision}.get(
+        line = {"batched": run_reference_batched, "precision": run_reference_precision,
+                "serving": run_reference_serving}.get(
             args.workload, run_reference)(args, rank, world)
     else:
-        line = {"batched": run_ours_batched, "precision": run_ours_precision}.get(
+        line = {"batched": run_ours_batched, "precision": run_ours_precision,
+                "serving": run_ours_serving}.get(
             args.workload, run_ours)(args, rank, world, local)
     if line is not None:
         print(json.dumps(line), flush=True)
