@@ -378,9 +378,15 @@ constexpr uint32_t kHandoff = 2048;     // front width at which the walkers take
 constexpr uint32_t kWalkCap = 128;      // per-warp front capacity of the walkers
 
 struct WarpCands {
-    uint64_t* buf;  // kCandBuf entries
-    uint32_t n;     // warp-uniform
+    uint64_t* buf;       // kCandBuf entries
+    uint32_t n;          // warp-uniform
+    uint32_t found = 0;  // candidates found by this warp (added to the counter once, at the end)
 };
+
+__device__ __forceinline__ void flush_found(const DetectArgs& a, const WarpCands& wc, uint32_t lane)
+{
+    if (lane == 0 && wc.found) atomicAdd(a.counts + kCountCands, wc.found);
+}
 
 __device__ __forceinline__ void test_candidates(const DetectArgs& a, const uint64_t* buf, uint32_t count,
                                                 uint32_t lane)
@@ -411,7 +417,7 @@ __device__ __forceinline__ void push_candidate(const DetectArgs& a, WarpCands& w
 {
     const uint32_t mask = __ballot_sync(0xffffffffu, pred);
     if (mask == 0) return;
-    if (lane == 0) atomicAdd(a.counts + kCountCands, (uint32_t)__popc(mask));
+    wc.found += __popc(mask);
     if (!a.fuse_narrow) {
         // broad phase only: candidates go to the global queue
         uint32_t base = 0;
@@ -568,6 +574,7 @@ __global__ void __launch_bounds__(kDetectThreads) k_init_front(DetectArgs a, uin
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.counts + kCountTested, total0);
+    flush_found(a, wc, lane);
     if (a.fuse_narrow && wc.n > 0) test_candidates(a, wc.buf, wc.n, lane);
 }
 
@@ -622,6 +629,7 @@ __global__ void __launch_bounds__(kTopThreads) k_top(DetectArgs a)
         cur ^= 1;
     }
     if (lane == 0 && tested) atomicAdd(a.counts + kCountTested, tested);
+    flush_found(a, wc, lane);
     if (a.fuse_narrow && wc.n > 0) test_candidates(a, wc.buf, wc.n, lane);
 }
 
@@ -673,6 +681,7 @@ __global__ void __launch_bounds__(kDetectThreads) k_walk(DetectArgs a, uint32_t 
         }
     }
     if (lane == 0 && tested) atomicAdd(a.counts + kCountTested, tested);
+    flush_found(a, wc, lane);
     if (a.fuse_narrow && wc.n > 0) test_candidates(a, wc.buf, wc.n, lane);
 }
 
