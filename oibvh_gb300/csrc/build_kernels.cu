@@ -359,8 +359,10 @@ cudaError_t launch_gather_faces(const uint32_t* tri, const uint32_t* perm, uint3
 // stable sort by Morton code followed by one stable sort by tree id gives,
 // per tree, the order of the single-tree build: (code, original index).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t find_job(const BuildJob* jobs, uint32_t n, uint32_t block, bool faces)
+__device__ __forceinline__ uint32_t find_job(const BuildJob* jobs, uint32_t n, uint32_t block, bool faces,
+                                             const uint32_t* __restrict__ table)
 {
+    if (table) return __ldg(table + block);  // host-built block -> job map: one load
     uint32_t lo = 0, hi = n - 1;
     while (lo < hi) {
         const uint32_t mid = (lo + hi + 1) >> 1;
@@ -382,9 +384,10 @@ __global__ void k_bounds_init_multi(const BuildJob* __restrict__ jobs, uint32_t 
     }
 }
 
-__global__ void __launch_bounds__(256) k_mesh_bounds_multi(const BuildJob* __restrict__ jobs, uint32_t n_jobs)
+__global__ void __launch_bounds__(256) k_mesh_bounds_multi(const BuildJob* __restrict__ jobs, uint32_t n_jobs,
+                                                           const uint32_t* __restrict__ vjob)
 {
-    const uint32_t j = find_job(jobs, n_jobs, blockIdx.x, false);
+    const uint32_t j = find_job(jobs, n_jobs, blockIdx.x, false, vjob);
     const BuildJob job = jobs[j];
     const uint32_t v = (blockIdx.x - job.vblock_begin) * blockDim.x + threadIdx.x;
     uint32_t mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu};
@@ -412,10 +415,11 @@ __global__ void __launch_bounds__(256) k_mesh_bounds_multi(const BuildJob* __res
 }
 
 __global__ void __launch_bounds__(256) k_leaf_morton_multi(const BuildJob* __restrict__ jobs, uint32_t n_jobs,
+                                                           const uint32_t* __restrict__ fjob,
                                                            uint32_t* __restrict__ codes, uint32_t* __restrict__ idx,
                                                            uint32_t* __restrict__ tree_of)
 {
-    const uint32_t j = find_job(jobs, n_jobs, blockIdx.x, true);
+    const uint32_t j = find_job(jobs, n_jobs, blockIdx.x, true, fjob);
     const BuildJob job = jobs[j];
     const uint32_t i = (blockIdx.x - job.fblock_begin) * blockDim.x + threadIdx.x;
     if (i >= job.nT) return;
@@ -466,10 +470,11 @@ __global__ void __launch_bounds__(256) k_gather_faces_multi(const BuildJob* __re
 // Rigid transforms of every tree: pos = M * rest, M a row-major 3x4 matrix per
 // tree, each product and sum rounded on its own: x' = ((m0 x + m1 y) + m2 z) + m3.
 __global__ void __launch_bounds__(256) k_transform_multi(const BuildJob* __restrict__ jobs, uint32_t n_jobs,
+                                                         const uint32_t* __restrict__ vjob,
                                                          const float4* __restrict__ rest,
                                                          const float* __restrict__ mats)
 {
-    const uint32_t j = find_job(jobs, n_jobs, blockIdx.x, false);
+    const uint32_t j = find_job(jobs, n_jobs, blockIdx.x, false, vjob);
     const BuildJob& job = jobs[j];
     const uint32_t v = (blockIdx.x - job.vblock_begin) * blockDim.x + threadIdx.x;
     if (v >= job.nV) return;
@@ -486,7 +491,8 @@ __global__ void __launch_bounds__(256) k_transform_multi(const BuildJob* __restr
 }
 
 cudaError_t launch_build_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, uint32_t f_blocks,
-                               uint32_t n_faces, uint32_t tree_bits, void* scratch, cudaStream_t s)
+                               const uint32_t* vjob, const uint32_t* fjob, uint32_t n_faces, uint32_t tree_bits,
+                               void* scratch, cudaStream_t s)
 {
     // scratch: codes, idx, tree_of, keys2 (4 x n_faces u32), then the sort scratch
     uint32_t* codes = (uint32_t*)scratch;
@@ -496,8 +502,8 @@ cudaError_t launch_build_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t
     void* sort_scratch = keys2 + n_faces;
     note_launches(4);
     k_bounds_init_multi<<<(n_jobs + 255) / 256, 256, 0, s>>>(d_jobs, n_jobs);
-    k_mesh_bounds_multi<<<v_blocks, 256, 0, s>>>(d_jobs, n_jobs);
-    k_leaf_morton_multi<<<f_blocks, 256, 0, s>>>(d_jobs, n_jobs, codes, idx, tree_of);
+    k_mesh_bounds_multi<<<v_blocks, 256, 0, s>>>(d_jobs, n_jobs, vjob);
+    k_leaf_morton_multi<<<f_blocks, 256, 0, s>>>(d_jobs, n_jobs, fjob, codes, idx, tree_of);
     cudaError_t e = launch_radix_sort(codes, idx, n_faces, 30, sort_scratch, s);
     if (e != cudaSuccess) return e;
     k_gather_u32<<<(n_faces + 255) / 256, 256, 0, s>>>(tree_of, idx, n_faces, keys2);
@@ -515,11 +521,11 @@ size_t build_multi_scratch_bytes(uint32_t n_faces)
     return 4 * (size_t)n_faces * sizeof(uint32_t) + radix_sort_scratch_bytes(n_faces);
 }
 
-cudaError_t launch_transform_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, const float4* rest,
-                                   const float* mats, cudaStream_t s)
+cudaError_t launch_transform_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, const uint32_t* vjob,
+                                   const float4* rest, const float* mats, cudaStream_t s)
 {
     note_launches(1);
-    k_transform_multi<<<v_blocks, 256, 0, s>>>(d_jobs, n_jobs, rest, mats);
+    k_transform_multi<<<v_blocks, 256, 0, s>>>(d_jobs, n_jobs, vjob, rest, mats);
     return cudaGetLastError();
 }
 

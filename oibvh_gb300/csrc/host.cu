@@ -136,6 +136,7 @@ struct oibvh_scene_s {
 
     // multi-tree refit: job table as last uploaded
     DevBuf<RefitJob> refit_jobs;
+    DevBuf<uint32_t> refit_block_job;  // refit CTA -> job
     DevBuf<uint32_t> refit_counters;
     PinnedBuf<RefitJob> h_refit_jobs;
     std::vector<RefitJob> refit_cache;
@@ -143,6 +144,7 @@ struct oibvh_scene_s {
 
     // multi-tree build / transform: job table for the current tree list
     DevBuf<BuildJob> build_jobs;
+    DevBuf<uint32_t> vblock_job, fblock_job;  // 256-vertex / 256-face block -> job
     DevBuf<uint32_t> bound_keys;
     std::vector<BuildJob> build_cache;
     uint32_t v_blocks = 0, f_blocks = 0, n_faces = 0, n_verts = 0;
@@ -802,13 +804,22 @@ API int oibvh_scene_refit(oibvh_scene_t s, void* stream)
     if (!same) {
         OK_TRY(s->refit_jobs.ensure(n, "cudaMalloc(refit jobs)"));
         OK_TRY(s->h_refit_jobs.ensure(n, "cudaMallocHost(refit jobs)"));
+        OK_TRY(s->refit_block_job.ensure(std::max(1u, blocks), "cudaMalloc(refit block map)"));
         CUDA_TRY(cudaStreamSynchronize(st));  // the staging buffer may feed an earlier copy
         std::memcpy(s->h_refit_jobs.p, jobs.data(), n * sizeof(RefitJob));
         CUDA_TRY(cudaMemcpyAsync(s->refit_jobs.p, s->h_refit_jobs.p, n * sizeof(RefitJob), cudaMemcpyHostToDevice, st));
+        std::vector<uint32_t> map(blocks);
+        for (size_t i = 0; i < n; ++i)
+            std::fill(map.begin() + jobs[i].block_begin, map.begin() + jobs[i].block_begin + jobs[i].n_blocks,
+                      (uint32_t)i);
+        CUDA_TRY(cudaMemcpyAsync(s->refit_block_job.p, map.data(), blocks * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                 st));
+        CUDA_TRY(cudaStreamSynchronize(st));  // map is a pageable host vector
         s->refit_cache = jobs;
     }
     s->refit_blocks = blocks;
-    CUDA_TRY(launch_refit(s->refit_jobs.p, (uint32_t)n, blocks, s->refit_counters.p, per * n, st));
+    CUDA_TRY(launch_refit(s->refit_jobs.p, (uint32_t)n, blocks, s->refit_block_job.p, s->refit_counters.p, per * n,
+                          st));
     return OIBVH_OK;
     GUARD_END
 }
@@ -973,8 +984,20 @@ int ensure_build_jobs(oibvh_scene_s* s, cudaStream_t st)
     for (size_t i = 0; same && i < n; ++i) same = std::memcmp(&jobs[i], &s->build_cache[i], sizeof(BuildJob)) == 0;
     if (!same) {
         OK_TRY(s->build_jobs.ensure(std::max<size_t>(n, 1), "cudaMalloc(build jobs)"));
+        OK_TRY(s->vblock_job.ensure(std::max(1u, vb), "cudaMalloc(vertex block map)"));
+        OK_TRY(s->fblock_job.ensure(std::max(1u, fb), "cudaMalloc(face block map)"));
+        std::vector<uint32_t> vmap(vb), fmap(fb);
+        for (size_t i = 0; i < n; ++i) {
+            const oibvh_tree_t t = s->trees[i];
+            std::fill(vmap.begin() + jobs[i].vblock_begin, vmap.begin() + jobs[i].vblock_begin + (t->nV + 255) / 256,
+                      (uint32_t)i);
+            std::fill(fmap.begin() + jobs[i].fblock_begin, fmap.begin() + jobs[i].fblock_begin + (t->nT + 255) / 256,
+                      (uint32_t)i);
+        }
         CUDA_TRY(cudaMemcpyAsync(s->build_jobs.p, jobs.data(), n * sizeof(BuildJob), cudaMemcpyHostToDevice, st));
-        CUDA_TRY(cudaStreamSynchronize(st));  // jobs is a pageable host vector
+        CUDA_TRY(cudaMemcpyAsync(s->vblock_job.p, vmap.data(), vb * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(s->fblock_job.p, fmap.data(), fb * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaStreamSynchronize(st));  // jobs and the maps are pageable host vectors
         s->build_cache = jobs;
     }
     return OIBVH_OK;
@@ -994,7 +1017,8 @@ API int oibvh_scene_build(oibvh_scene_t s, void* stream)
     OK_TRY(scratch.ensure(build_multi_scratch_bytes(s->n_faces), "cudaMalloc(build scratch)"));
     const uint32_t n = (uint32_t)s->trees.size();
     const uint32_t tree_bits = n <= 1 ? 0u : ilog2(next_pow2(n));
-    CUDA_TRY(launch_build_multi(s->build_jobs.p, n, s->v_blocks, s->f_blocks, s->n_faces, tree_bits, scratch.p, st));
+    CUDA_TRY(launch_build_multi(s->build_jobs.p, n, s->v_blocks, s->f_blocks, s->vblock_job.p, s->fblock_job.p,
+                                s->n_faces, tree_bits, scratch.p, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     for (auto t : s->trees) t->built = true;
     const int r = oibvh_scene_refit(s, stream);
@@ -1014,7 +1038,7 @@ API int oibvh_scene_transform(oibvh_scene_t s, const float* d_rest_xyzw, const f
     cudaStream_t st = (cudaStream_t)stream;
     for (auto t : s->trees) t->cur_pos = t->pos4.p;  // the transform writes each tree's own positions
     OK_TRY(ensure_build_jobs(s, st));
-    CUDA_TRY(launch_transform_multi(s->build_jobs.p, (uint32_t)s->trees.size(), s->v_blocks,
+    CUDA_TRY(launch_transform_multi(s->build_jobs.p, (uint32_t)s->trees.size(), s->v_blocks, s->vblock_job.p,
                                     (const float4*)d_rest_xyzw, d_mats, st));
     return OIBVH_OK;
     GUARD_END
@@ -1188,13 +1212,13 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
     uint32_t kernels = 0;
     cudaError_t e = cudaSuccess;
     if (s->frame_rest && e == cudaSuccess) {
-        e = launch_transform_multi(s->build_jobs.p, (uint32_t)s->trees.size(), s->v_blocks, s->frame_rest,
-                                   s->frame_mats, st);
+        e = launch_transform_multi(s->build_jobs.p, (uint32_t)s->trees.size(), s->v_blocks, s->vblock_job.p,
+                                   s->frame_rest, s->frame_mats, st);
         ++kernels;
     }
     if (s->frame_refit && e == cudaSuccess) {
-        e = launch_refit(s->refit_jobs.p, (uint32_t)s->trees.size(), s->refit_blocks, s->refit_counters.p,
-                         refit_counters_per_tree() * s->trees.size(), st);
+        e = launch_refit(s->refit_jobs.p, (uint32_t)s->trees.size(), s->refit_blocks, s->refit_block_job.p,
+                         s->refit_counters.p, refit_counters_per_tree() * s->trees.size(), st);
         ++kernels;
     }
     if (e == cudaSuccess) e = cudaMemsetAsync(s->counts.p, 0, kCountTotal * sizeof(uint32_t), st);

@@ -41,10 +41,13 @@ struct BuildJob {
 // build_kernels.cu
 size_t radix_sort_scratch_bytes(uint32_t n);
 size_t build_multi_scratch_bytes(uint32_t n_faces);
+// vjob / fjob: optional host-built maps from a 256-vertex / 256-face block
+// to its job (nullptr: each CTA binary-searches the job table).
 cudaError_t launch_build_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, uint32_t f_blocks,
-                               uint32_t n_faces, uint32_t tree_bits, void* scratch, cudaStream_t s);
-cudaError_t launch_transform_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, const float4* rest,
-                                   const float* mats, cudaStream_t s);
+                               const uint32_t* vjob, const uint32_t* fjob, uint32_t n_faces, uint32_t tree_bits,
+                               void* scratch, cudaStream_t s);
+cudaError_t launch_transform_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, const uint32_t* vjob,
+                                   const float4* rest, const float* mats, cudaStream_t s);
 cudaError_t launch_xyz_to_pos4(const float* xyz, uint32_t nV, float4* pos, cudaStream_t s);
 cudaError_t launch_mesh_bounds(const float4* pos, uint32_t nV, uint32_t* bound_keys, int num_sms, cudaStream_t s);
 cudaError_t launch_leaf_morton(const uint32_t* tri, const float4* pos, uint32_t nT, const uint32_t* bound_keys,
@@ -58,8 +61,10 @@ uint32_t refit_blocks_for(uint32_t nT);
 uint32_t refit_counters_per_tree();
 cudaError_t launch_refit_one(const RefitJob& job, cudaStream_t s);
 cudaError_t launch_leaf_boxes(const uint4* face, const float4* pos, uint32_t nT, float4* out, cudaStream_t s);
-cudaError_t launch_refit(const RefitJob* d_jobs, uint32_t n_jobs, uint32_t total_blocks, uint32_t* d_counters,
-                         size_t n_counters, cudaStream_t s);
+// block_job: optional host-built map from a refit CTA to its job (nullptr:
+// each CTA binary-searches the job table).
+cudaError_t launch_refit(const RefitJob* d_jobs, uint32_t n_jobs, uint32_t total_blocks, const uint32_t* block_job,
+                         uint32_t* d_counters, size_t n_counters, cudaStream_t s);
 
 // detect_kernels.cu
 struct DetectArgs {

@@ -127,13 +127,15 @@ __device__ __forceinline__ void reduce_block(Box v[4], const TreeShape& S, float
 
 // `jobs` == nullptr: a single tree passed by value in `one`.
 __global__ void __launch_bounds__(kRefitThreads, 5) k_refit(const RefitJob* __restrict__ jobs, uint32_t n_jobs,
-                                                         const RefitJob one)
+                                                         const uint32_t* __restrict__ block_job, const RefitJob one)
 {
     __shared__ Box sm8[8];
     __shared__ uint32_t s_last;
 
     RefitJob job = one;
-    if (jobs != nullptr) {
+    if (jobs != nullptr && block_job != nullptr) {
+        job = jobs[__ldg(block_job + blockIdx.x)];
+    } else if (jobs != nullptr) {
         uint32_t lo = 0, hi = n_jobs - 1;
         while (lo < hi) {
             const uint32_t mid = (lo + hi + 1) >> 1;
@@ -209,19 +211,19 @@ cudaError_t launch_refit_one(const RefitJob& job, cudaStream_t s)
     cudaError_t e = cudaMemsetAsync(job.counters, 0, refit_counters_per_tree() * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     note_launches(1);
-    k_refit<<<job.n_blocks, kRefitThreads, 0, s>>>(nullptr, 1, job);
+    k_refit<<<job.n_blocks, kRefitThreads, 0, s>>>(nullptr, 1, nullptr, job);
     return cudaGetLastError();
 }
 
-cudaError_t launch_refit(const RefitJob* d_jobs, uint32_t n_jobs, uint32_t total_blocks, uint32_t* d_counters,
-                         size_t n_counters, cudaStream_t s)
+cudaError_t launch_refit(const RefitJob* d_jobs, uint32_t n_jobs, uint32_t total_blocks, const uint32_t* block_job,
+                         uint32_t* d_counters, size_t n_counters, cudaStream_t s)
 {
     if (n_jobs == 0 || total_blocks == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(d_counters, 0, n_counters * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     RefitJob none{};
     note_launches(1);
-    k_refit<<<total_blocks, kRefitThreads, 0, s>>>(d_jobs, n_jobs, none);
+    k_refit<<<total_blocks, kRefitThreads, 0, s>>>(d_jobs, n_jobs, block_job, none);
     return cudaGetLastError();
 }
 
