@@ -395,9 +395,9 @@ __device__ __forceinline__ void test_candidates(const DetectArgs& a, const uint6
     uint4 rec = make_uint4(0, 0, 0, 0);
     if (lane < count) {
         const uint64_t c = buf[lane];
-        const PairView pv = a.pairs[bvtt_pair(c)];
-        const TreeView& TA = a.trees[pv.a];
-        const TreeView& TB = a.trees[pv.b];
+        const PairView& pv = a.pairs[bvtt_pair(c)];
+        const TreeView& TA = pv.ta;
+        const TreeView& TB = pv.tb;
         const uint4 fa = __ldg(TA.face + bvtt_a(c));
         const uint4 fb = __ldg(TB.face + bvtt_b(c));
         hit = tri_intersect_exact(load_vertex(TA.pos, fa.x), load_vertex(TA.pos, fa.y), load_vertex(TA.pos, fa.z),
@@ -458,9 +458,9 @@ __device__ __forceinline__ uint32_t expand_pair(const DetectArgs& a, WarpCands& 
     if (valid) {
         pair = bvtt_pair(node);
         const uint32_t ia = bvtt_a(node), ib = bvtt_b(node);
-        const PairView pv = a.pairs[pair];
-        const TreeView& TA = a.trees[pv.a];
-        const TreeView& TB = a.trees[pv.b];
+        const PairView& pv = a.pairs[pair];
+        const TreeView& TA = pv.ta;
+        const TreeView& TB = pv.tb;
         const uint32_t la = ilog2(ia + 1u), lb = ilog2(ib + 1u);
         expand_side(TA.shape, ia, la, 1, fa, na);
         expand_side(TB.shape, ib, lb, 1, fb, nb);
@@ -554,12 +554,12 @@ __global__ void __launch_bounds__(kDetectThreads) k_init_front(DetectArgs a, uin
                 if (a.pairs[mid].front_off <= i) lo = mid;
                 else hi = mid - 1;
             }
-            const PairView pv = a.pairs[lo];
+            const PairView& pv = a.pairs[lo];
             const uint32_t k = i - pv.front_off;
             const uint32_t x = k / pv.front_cnt_b, y = k - x * pv.front_cnt_b;
             const uint32_t ia = (1u << pv.entry_a) - 1u + x, ib = (1u << pv.entry_b) - 1u + y;
-            const TreeView& TA = a.trees[pv.a];
-            const TreeView& TB = a.trees[pv.b];
+            const TreeView& TA = pv.ta;
+            const TreeView& TB = pv.tb;
             ov = overlap(node_box(TA, ia, pv.entry_a), node_box(TB, ib, pv.entry_b));
             leafpair = ov && pv.entry_a == TA.shape.L && pv.entry_b == TB.shape.L;
             node = bvtt_pack(lo, ia, ib);
@@ -708,9 +708,9 @@ constexpr uint32_t kFp64Queue = 64;  // <= 31 left over + 32 added per round
 __device__ __forceinline__ void load_tris(const DetectArgs& a, uint64_t c, V3& P1, V3& P2, V3& P3, V3& Q1, V3& Q2,
                                           V3& Q3, uint4& rec)
 {
-    const PairView pv = a.pairs[bvtt_pair(c)];
-    const TreeView& TA = a.trees[pv.a];
-    const TreeView& TB = a.trees[pv.b];
+    const PairView& pv = a.pairs[bvtt_pair(c)];
+    const TreeView& TA = pv.ta;
+    const TreeView& TB = pv.tb;
     const uint4 fa = __ldg(TA.face + bvtt_a(c));
     const uint4 fb = __ldg(TB.face + bvtt_b(c));
     P1 = load_vertex(TA.pos, fa.x);

@@ -200,6 +200,17 @@ void list_pairs(const oibvh_scene_s* s, std::vector<uint32_t>& out)
     }
 }
 
+TreeView view_of(const oibvh_tree_t t)
+{
+    TreeView v{};
+    v.box = t->box.p;
+    v.face = t->face.p;
+    v.pos = t->cur_pos;
+    v.shape = t->shape;
+    v.nV = t->nV;
+    return v;
+}
+
 // Start level of each pair: the reference's entry level, deepened so that
 // the start cross product holds about 2^tune_start_log2 (default 2^16) node
 // pairs over the pass (the
@@ -218,6 +229,8 @@ int plan_pass(const oibvh_scene_s* s, const uint32_t* pr, uint32_t n, uint32_t e
         PairView v{};
         v.a = pr[2 * p];
         v.b = pr[2 * p + 1];
+        v.ta = view_of(s->trees[v.a]);
+        v.tb = view_of(s->trees[v.b]);
         const uint32_t start = std::max(entry, auto_level);
         v.entry_a = std::min(start, A.L);
         v.entry_b = std::min(start, B.L);

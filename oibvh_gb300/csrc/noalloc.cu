@@ -118,6 +118,8 @@ extern "C" __attribute__((visibility("default"))) int oibvh_pair_detect_noalloc(
         const uint32_t start = entry_level > 8u ? entry_level : 8u;
         h.pair.a = 0;
         h.pair.b = 1;
+        h.pair.ta = h.trees[0];
+        h.pair.tb = h.trees[1];
         h.pair.front_off = 0;
         h.pair.entry_a = start < A.L ? start : A.L;
         h.pair.entry_b = start < B.L ? start : B.L;

@@ -114,7 +114,9 @@ struct TreeView {
     uint32_t pad0;
 };
 
-// One mesh pair of a detection pass.
+// One mesh pair of a detection pass. The two tree views are copied in, so a
+// traversal step reads its pair's record and then the boxes (one dependent
+// load fewer than going through the TreeView table).
 struct PairView {
     uint32_t a, b;            // tree ids (index into the TreeView table)
     uint32_t front_off;       // first initial-front node of this pair
@@ -122,6 +124,7 @@ struct PairView {
     uint32_t front_cnt_b;     // real nodes of B at the entry level
     uint32_t entry_a, entry_b;
     uint32_t pad0;
+    TreeView ta, tb;          // copies of views a and b
 };
 
 // Status bits a kernel can raise (the host turns them into status codes).

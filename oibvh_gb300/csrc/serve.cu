@@ -244,6 +244,8 @@ int oibvh_server_s::launch(Lane& L, std::vector<Query*>& batch)
         PairView pv{};
         pv.a = 2 * i;
         pv.b = 2 * i + 1;
+        pv.ta = va;
+        pv.tb = vb;
         const uint32_t start = std::max(entry_level, auto_level);
         pv.entry_a = std::min(start, A->shape.L);
         pv.entry_b = std::min(start, B->shape.L);
