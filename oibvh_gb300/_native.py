@@ -74,6 +74,7 @@ class Tuning(ctypes.Structure):
         ("walk_blocks_per_sm", ctypes.c_uint32),
         ("front_capacity", ctypes.c_uint32),
         ("hit_capacity", ctypes.c_uint32),
+        ("walk_front", ctypes.c_uint32),
     ]
 
 

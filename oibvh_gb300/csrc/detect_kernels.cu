@@ -375,7 +375,8 @@ constexpr int kCandBuf = 64;  // <= 31 left over + 32 added per round
 constexpr uint32_t kTopThreads = 1024;  // the single CTA of the top levels
 constexpr uint32_t kTopCap = 8192;      // its front capacity (two buffers: 128 KB)
 constexpr uint32_t kHandoff = 2048;     // front width at which the walkers take over
-constexpr uint32_t kWalkCap = 128;      // per-warp front capacity of the walkers
+constexpr uint32_t kWalkCap = 128;      // default per-warp front capacity of the walkers
+constexpr uint32_t kWalkCapMax = 512;
 
 struct WarpCands {
     uint64_t* buf;       // kCandBuf entries
@@ -641,7 +642,7 @@ __global__ void __launch_bounds__(kTopThreads) k_top(DetectArgs a)
 // buffer spills the excess to the next round's list.
 __global__ void __launch_bounds__(kDetectThreads) k_walk(DetectArgs a, uint32_t round)
 {
-    __shared__ uint64_t s_front[kDetectThreads / 32][2][kWalkCap];
+    extern __shared__ uint64_t s_front[];  // [warp][2][cap]
     __shared__ uint64_t s_cand[kDetectThreads / 32][kCandBuf];
     __shared__ uint32_t s_cnt[kDetectThreads / 32][2];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -652,8 +653,9 @@ __global__ void __launch_bounds__(kDetectThreads) k_walk(DetectArgs a, uint32_t 
     const uint32_t n_src = min(*(volatile uint32_t*)(a.counts + kCountWork0 + round), a.work_cap);
     const uint32_t W = (gridDim.x * blockDim.x) >> 5;
     const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint64_t* f0 = s_front[wib][0];
-    uint64_t* f1 = s_front[wib][1];
+    const uint32_t cap = a.walk_cap ? a.walk_cap : kWalkCap;
+    uint64_t* f0 = s_front + (size_t)wib * 2 * cap;
+    uint64_t* f1 = f0 + cap;
     uint32_t* cnt = s_cnt[wib];
     uint32_t tested = 0;
 
@@ -673,10 +675,10 @@ __global__ void __launch_bounds__(kDetectThreads) k_walk(DetectArgs a, uint32_t 
                 const uint32_t i = base + lane;
                 const bool valid = i < c;
                 const uint64_t node = valid ? fc[i] : 0ull;
-                tested += expand_pair(a, wc, valid, node, fn, &cnt[cur ^ 1], kWalkCap, spill, spill_cnt, lane);
+                tested += expand_pair(a, wc, valid, node, fn, &cnt[cur ^ 1], cap, spill, spill_cnt, lane);
             }
             __syncwarp();
-            c = min(cnt[cur ^ 1], kWalkCap);
+            c = min(cnt[cur ^ 1], cap);
             cur ^= 1;
         }
     }
@@ -833,18 +835,37 @@ cudaError_t launch_top(const DetectArgs& a, cudaStream_t s)
     return cudaGetLastError();
 }
 
+static size_t walk_smem(uint32_t cap) { return (size_t)(kDetectThreads / 32) * 2 * (cap ? cap : kWalkCap) * 8; }
+
+static cudaError_t walk_configure()
+{
+    static bool configured[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && configured[dev]) return cudaSuccess;
+    const cudaError_t e =
+        cudaFuncSetAttribute(k_walk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)walk_smem(kWalkCapMax));
+    if (e == cudaSuccess && dev >= 0 && dev < 64) configured[dev] = true;
+    return e;
+}
+
 cudaError_t launch_walk(const DetectArgs& a, uint32_t round, cudaStream_t s)
 {
     if (fused_precision(a)) return cudaErrorInvalidValue;
+    if (a.walk_cap > kWalkCapMax || (a.walk_cap % 32) != 0) return cudaErrorInvalidValue;
+    cudaError_t e = walk_configure();
+    if (e != cudaSuccess) return e;
     note_launches(1);
-    k_walk<<<a.grid, kDetectThreads, 0, s>>>(a, round);
+    k_walk<<<a.grid, kDetectThreads, walk_smem(a.walk_cap), s>>>(a, round);
     return cudaGetLastError();
 }
 
-int walk_blocks_per_sm()
+int walk_blocks_per_sm(uint32_t walk_cap)
 {
+    if (walk_configure() != cudaSuccess) return 1;
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_walk, kDetectThreads, 0) != cudaSuccess) return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_walk, kDetectThreads, walk_smem(walk_cap)) != cudaSuccess)
+        return 1;
     return n > 0 ? n : 1;
 }
 

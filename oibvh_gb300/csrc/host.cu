@@ -154,6 +154,7 @@ struct oibvh_scene_s {
     uint32_t tune_handoff = 2048;   // front width at which k_top hands over to the walkers
     uint32_t precision = 0;         // OIBVH_PRECISION_*
     uint32_t tune_walk_per_sm = 0;  // walker CTAs per SM, 0 = as many as fit
+    uint32_t tune_walk_cap = 128;   // per-warp front entries of the walkers
 
     // captured frame (CUDA graph): [transform] + refit + detect
     cudaGraphExec_t frame_exec = nullptr;
@@ -274,7 +275,7 @@ int upload_views(oibvh_scene_s* s, cudaStream_t st)
 
 int walk_grid(const oibvh_scene_s* s)
 {
-    const int fit = walk_blocks_per_sm();
+    const int fit = walk_blocks_per_sm(s->tune_walk_cap);
     const int per = s->tune_walk_per_sm ? std::min<int>(fit, (int)s->tune_walk_per_sm) : fit;
     return sm_count(s->device) * std::max(1, per);
 }
@@ -367,6 +368,7 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
             a.fuse_narrow = narrow ? 1u : 0u;
             a.grid = grid;
             a.handoff = s->tune_handoff;
+    a.walk_cap = s->tune_walk_cap;
             a.precision = s->precision;
             CUDA_TRY(launch_init_front(a, (uint32_t)plan.front0, st));
             CUDA_TRY(launch_top(a, st));
@@ -1062,6 +1064,9 @@ API int oibvh_scene_set_tuning(oibvh_scene_t s, const oibvh_tuning* t)
     if (!s || !t) return fail(OIBVH_ERR_ARG, "scene or tuning is NULL");
     if (t->start_pairs_log2 < 8 || t->start_pairs_log2 > 24) return fail(OIBVH_ERR_ARG, "start_pairs_log2 in 8..24");
     if (t->handoff < 32 || t->handoff > 8192) return fail(OIBVH_ERR_ARG, "handoff in 32..8192");
+    if (t->walk_front && (t->walk_front % 32 || t->walk_front > 512))
+        return fail(OIBVH_ERR_ARG, "walk_front: a multiple of 32 up to 512 (0 keeps the value)");
+    if (t->walk_front) s->tune_walk_cap = t->walk_front;
     s->tune_start_log2 = t->start_pairs_log2;
     s->tune_handoff = t->handoff;
     s->tune_walk_per_sm = t->walk_blocks_per_sm;
@@ -1077,64 +1082,80 @@ API int oibvh_scene_get_tuning(oibvh_scene_t s, oibvh_tuning* t)
     t->start_pairs_log2 = s->tune_start_log2;
     t->handoff = s->tune_handoff;
     t->walk_blocks_per_sm = s->tune_walk_per_sm;
+    t->walk_front = s->tune_walk_cap;
     t->front_capacity = s->front_cap;
     t->hit_capacity = s->hit_cap;
     return OIBVH_OK;
 }
 
 // Times `reps` detects per candidate setting with CUDA events and keeps the
-// fastest; queue capacities are set from the observed peaks with headroom so
-// that timed frames never regrow.
+// fastest. Coordinate descent: the start size x handoff grid first, then the
+// walkers' front capacity, then walker CTAs per SM, each with the others at
+// their best so far.
 API int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t reps, oibvh_tuning* chosen)
 {
     GUARD_BEGIN
     if (!s) return fail(OIBVH_ERR_ARG, "scene is NULL");
     if (reps == 0) reps = 3;
     DeviceGuard g(s->device);
-    const uint32_t starts[] = {12, 14, 16, 18, 20};
-    const uint32_t handoffs[] = {512, 2048, 8192};
-    const int fit = walk_blocks_per_sm();
     cudaEvent_t e0, e1;
     CUDA_TRY(cudaEventCreate(&e0));
     CUDA_TRY(cudaEventCreate(&e1));
-    float best = 1e30f;
-    oibvh_tuning bt{};
     int st = OIBVH_OK;
-    // warm-up sizes the queues
-    st = detect_impl(s, s->device, entry_level, 1, full_detect_mode(s), 0);
-    for (uint32_t sl : starts) {
-        for (uint32_t h : handoffs) {
-            for (int per = std::max(1, fit / 2); per <= fit && st == OIBVH_OK; per += std::max(1, fit / 2)) {
-                s->tune_start_log2 = sl;
-                s->tune_handoff = h;
-                s->tune_walk_per_sm = (uint32_t)per;
-                st = detect_impl(s, s->device, entry_level, 1, full_detect_mode(s), 0);
-                if (st != OIBVH_OK) break;
-                float tot = 0.0f;
-                for (uint32_t r = 0; r < reps && st == OIBVH_OK; ++r) {
-                    cudaEventRecord(e0, 0);
-                    st = detect_impl(s, s->device, entry_level, 1, full_detect_mode(s), 0);
-                    cudaEventRecord(e1, 0);
-                    cudaEventSynchronize(e1);
-                    float ms = 0.0f;
-                    cudaEventElapsedTime(&ms, e0, e1);
-                    tot += ms;
-                }
-                if (st == OIBVH_OK && tot < best) {
-                    best = tot;
-                    bt.start_pairs_log2 = sl;
-                    bt.handoff = h;
-                    bt.walk_blocks_per_sm = (uint32_t)per;
-                }
-            }
+    // one setting: a warm-up detect (sizes the queues), then `reps` timed ones
+    auto time_setting = [&](float& ms_out) {
+        st = detect_impl(s, s->device, entry_level, 1, full_detect_mode(s), 0);
+        float tot = 0.0f;
+        for (uint32_t r = 0; r < reps && st == OIBVH_OK; ++r) {
+            cudaEventRecord(e0, 0);
+            st = detect_impl(s, s->device, entry_level, 1, full_detect_mode(s), 0);
+            cudaEventRecord(e1, 0);
+            cudaEventSynchronize(e1);
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            tot += ms;
         }
+        ms_out = tot;
+        return st == OIBVH_OK;
+    };
+    float best = 1e30f;
+    uint32_t b_start = s->tune_start_log2, b_handoff = s->tune_handoff, b_cap = 128, b_per = 0;
+    s->tune_walk_cap = 128;
+    s->tune_walk_per_sm = 0;
+    for (uint32_t sl : {12u, 14u, 16u, 18u, 20u})
+        for (uint32_t h : {512u, 2048u, 8192u}) {
+            s->tune_start_log2 = sl;
+            s->tune_handoff = h;
+            float ms;
+            if (!time_setting(ms)) break;
+            if (ms < best) best = ms, b_start = sl, b_handoff = h;
+        }
+    s->tune_start_log2 = b_start;
+    s->tune_handoff = b_handoff;
+    for (uint32_t cap : {64u, 256u}) {
+        if (st != OIBVH_OK) break;
+        s->tune_walk_cap = cap;
+        float ms;
+        if (!time_setting(ms)) break;
+        if (ms < best) best = ms, b_cap = cap;
     }
+    s->tune_walk_cap = b_cap;
+    const int fit = walk_blocks_per_sm(b_cap);
+    for (int per = 1; per < fit && st == OIBVH_OK; ++per) {
+        s->tune_walk_per_sm = (uint32_t)per;
+        float ms;
+        if (!time_setting(ms)) break;
+        if (ms < best) best = ms, b_per = (uint32_t)per;
+    }
+    s->tune_walk_per_sm = b_per;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (st != OIBVH_OK) return st;
-    s->tune_start_log2 = bt.start_pairs_log2;
-    s->tune_handoff = bt.handoff;
-    s->tune_walk_per_sm = bt.walk_blocks_per_sm;
+    oibvh_tuning bt{};
+    bt.start_pairs_log2 = b_start;
+    bt.handoff = b_handoff;
+    bt.walk_blocks_per_sm = b_per ? b_per : (uint32_t)fit;
+    bt.walk_front = b_cap;
     // capacities: the largest work list and hit count seen, doubled
     st = detect_impl(s, s->device, entry_level, 1, full_detect_mode(s), 0);
     if (st != OIBVH_OK) return st;
@@ -1214,6 +1235,7 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
     a.cand_cap = s->precision ? s->cand_cap : 0u;
     a.grid = walk_grid(s);
     a.handoff = s->tune_handoff;
+    a.walk_cap = s->tune_walk_cap;
     a.precision = s->precision;
 
     // capture on a private non-blocking stream (the legacy default stream

@@ -83,11 +83,13 @@ struct DetectArgs {
     int grid;              // CTAs of the grid-stride / persistent kernels
     uint32_t handoff;      // front width at which k_top hands over to the walkers (<= 8192)
     uint32_t precision;    // 0: float triangle test (reference arithmetic); 1: FP64-filtered
+    uint32_t walk_cap;     // per-warp front entries of the walkers (multiple of 32, <= 512; 0: 128)
 };
 cudaError_t launch_init_front(const DetectArgs& a, uint32_t total0, cudaStream_t s);
 cudaError_t launch_top(const DetectArgs& a, cudaStream_t s);
 cudaError_t launch_walk(const DetectArgs& a, uint32_t round, cudaStream_t s);
-int walk_blocks_per_sm();
+// walker CTAs that fit on one SM with fronts of `walk_cap` entries (0: default)
+int walk_blocks_per_sm(uint32_t walk_cap = 0);
 cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s);
 
 // counts[]: hits, flags, candidates found, candidate slots used (broad-only),

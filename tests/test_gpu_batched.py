@@ -118,8 +118,26 @@ def test_autotune_keeps_the_pair_set(gpu):
     sc.detectCollision(DeviceType.GPU0, 0, 1)
     before = sc.int_tri_pairs()
     chosen = sc.autotune(0, 2)
-    assert chosen["handoff"] in (512, 2048, 8192)
+    assert chosen["handoff"] in (512, 2048, 8192) and chosen["walk_front"] in (64, 128, 256)
     sc.detectCollision(DeviceType.GPU0, 0, 1)
     assert np.array_equal(sc.int_tri_pairs(), before)
     want, _ = _oracle(w.positions(0), [m.tri for m in w.rest], w.pairs)
     assert np.array_equal(before, want)
+
+
+def test_walker_front_capacity_keeps_the_pair_set(gpu):
+    from oibvh_gb300 import DeviceType, OibvhError
+
+    w = _workload(8, seed=17)
+    sc, trees = _scene_from(w, build_with_scene=False)
+    for t, x in zip(trees, w.positions(0)):
+        t.refit(x)
+    want, wc = _oracle(w.positions(0), [m.tri for m in w.rest], w.pairs)
+    for cap in (32, 64, 256, 512):
+        sc.set_tuning(walk_front=cap)
+        assert sc.tuning()["walk_front"] == cap
+        sc.detectCollision(DeviceType.GPU0, 0, 1)
+        assert np.array_equal(sc.int_tri_pairs(), want), cap
+        assert sc.candidate_count() == wc
+    with pytest.raises(OibvhError):
+        sc.set_tuning(walk_front=48)
