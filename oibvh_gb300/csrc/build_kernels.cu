@@ -469,25 +469,42 @@ __global__ void __launch_bounds__(256) k_gather_faces_multi(const BuildJob* __re
 
 // Rigid transforms of every tree: pos = M * rest, M a row-major 3x4 matrix per
 // tree, each product and sum rounded on its own: x' = ((m0 x + m1 y) + m2 z) + m3.
+// Four 256-vertex blocks per CTA (vertex v of block k at thread v): the four
+// loads are issued before any arithmetic, for more bytes in flight.
+constexpr uint32_t kTransformUnroll = 4;
+
 __global__ void __launch_bounds__(256) k_transform_multi(const BuildJob* __restrict__ jobs, uint32_t n_jobs,
                                                          const uint32_t* __restrict__ vjob,
                                                          const float4* __restrict__ rest,
-                                                         const float* __restrict__ mats)
+                                                         const float* __restrict__ mats, uint32_t v_blocks)
 {
-    const uint32_t j = find_job(jobs, n_jobs, blockIdx.x, false, vjob);
-    const BuildJob& job = jobs[j];
-    const uint32_t v = (blockIdx.x - job.vblock_begin) * blockDim.x + threadIdx.x;
-    if (v >= job.nV) return;
-    // packed rest positions of all jobs, or (rest == nullptr) each job's own source
-    const float4 p = __ldg(rest ? rest + job.vert_off + v : job.pos + v);
-    const float* m = mats + 12 * (size_t)j;
-    float o[3];
+    float4 p[kTransformUnroll];
+    uint32_t jj[kTransformUnroll], vv[kTransformUnroll];
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
-        o[r] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(__ldg(m + 4 * r), p.x), __fmul_rn(__ldg(m + 4 * r + 1), p.y)),
-                                   __fmul_rn(__ldg(m + 4 * r + 2), p.z)),
-                         __ldg(m + 4 * r + 3));
-    job.pos_out[v] = make_float4(o[0], o[1], o[2], 0.0f);
+    for (uint32_t k = 0; k < kTransformUnroll; ++k) {
+        const uint32_t vb = blockIdx.x * kTransformUnroll + k;
+        jj[k] = 0xffffffffu;
+        if (vb >= v_blocks) continue;
+        const uint32_t j = find_job(jobs, n_jobs, vb, false, vjob);
+        const uint32_t v = (vb - jobs[j].vblock_begin) * 256u + threadIdx.x;
+        if (v >= jobs[j].nV) continue;
+        jj[k] = j;
+        vv[k] = v;
+        // packed rest positions of all jobs, or (rest == nullptr) each job's own source
+        p[k] = __ldg(rest ? rest + jobs[j].vert_off + v : jobs[j].pos + v);
+    }
+#pragma unroll
+    for (uint32_t k = 0; k < kTransformUnroll; ++k) {
+        if (jj[k] == 0xffffffffu) continue;
+        const float* m = mats + 12 * (size_t)jj[k];
+        float o[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+            o[r] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(__ldg(m + 4 * r), p[k].x), __fmul_rn(__ldg(m + 4 * r + 1), p[k].y)),
+                                       __fmul_rn(__ldg(m + 4 * r + 2), p[k].z)),
+                             __ldg(m + 4 * r + 3));
+        jobs[jj[k]].pos_out[vv[k]] = make_float4(o[0], o[1], o[2], 0.0f);
+    }
 }
 
 cudaError_t launch_build_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, uint32_t f_blocks,
@@ -525,7 +542,8 @@ cudaError_t launch_transform_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint
                                    const float4* rest, const float* mats, cudaStream_t s)
 {
     note_launches(1);
-    k_transform_multi<<<v_blocks, 256, 0, s>>>(d_jobs, n_jobs, vjob, rest, mats);
+    k_transform_multi<<<(v_blocks + kTransformUnroll - 1) / kTransformUnroll, 256, 0, s>>>(d_jobs, n_jobs, vjob, rest,
+                                                                                            mats, v_blocks);
     return cudaGetLastError();
 }
 
