@@ -413,30 +413,41 @@ __device__ __forceinline__ void test_candidates(const DetectArgs& a, const uint6
 }
 
 // Queue (or, in broad-only mode, store) one candidate per lane where `pred`.
+// Broad phase only: `count` buffered candidates (one per lane) to the global
+// candidate queue with one atomic for the warp.
+__device__ __forceinline__ void store_candidates(const DetectArgs& a, const uint64_t* buf, uint32_t count,
+                                                 uint32_t lane)
+{
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(a.counts + kCountCandSlots, count);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (lane < count) {
+        if (base + lane < a.cand_cap) a.cand[base + lane] = buf[lane];
+        else atomicOr(a.counts + kCountFlags, (uint32_t)kFlagCandOverflow);
+    }
+}
+
+// The warp's buffered candidates: tested (fused narrow phase) or stored.
+__device__ __forceinline__ void flush_candidates(const DetectArgs& a, const uint64_t* buf, uint32_t count,
+                                                 uint32_t lane)
+{
+    if (a.fuse_narrow) test_candidates(a, buf, count, lane);
+    else store_candidates(a, buf, count, lane);
+}
+
+// Queue one candidate per lane where `pred`; every 32 queued candidates are
+// tested (fused narrow phase) or stored (broad phase only) at once.
 __device__ __forceinline__ void push_candidate(const DetectArgs& a, WarpCands& wc, bool pred, uint64_t cval,
                                                uint32_t lane)
 {
     const uint32_t mask = __ballot_sync(0xffffffffu, pred);
     if (mask == 0) return;
     wc.found += __popc(mask);
-    if (!a.fuse_narrow) {
-        // broad phase only: candidates go to the global queue
-        uint32_t base = 0;
-        const int leader = __ffs(mask) - 1;
-        if ((int)lane == leader) base = atomicAdd(a.counts + kCountCandSlots, (uint32_t)__popc(mask));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (pred) {
-            const uint32_t pos = base + __popc(mask & ((1u << lane) - 1u));
-            if (pos < a.cand_cap) a.cand[pos] = cval;
-            else atomicOr(a.counts + kCountFlags, (uint32_t)kFlagCandOverflow);
-        }
-        return;
-    }
     if (pred) wc.buf[wc.n + __popc(mask & ((1u << lane) - 1u))] = cval;
     wc.n += __popc(mask);
     __syncwarp();
     if (wc.n >= 32) {
-        test_candidates(a, wc.buf + wc.n - 32, 32, lane);
+        flush_candidates(a, wc.buf + wc.n - 32, 32, lane);
         wc.n -= 32;
         __syncwarp();
     }
@@ -576,7 +587,7 @@ __global__ void __launch_bounds__(kDetectThreads) k_init_front(DetectArgs a, uin
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.counts + kCountTested, total0);
     flush_found(a, wc, lane);
-    if (a.fuse_narrow && wc.n > 0) test_candidates(a, wc.buf, wc.n, lane);
+    if (wc.n > 0) flush_candidates(a, wc.buf, wc.n, lane);
 }
 
 // The narrow top of the traversal: ONE CTA of kTopThreads walks the start
@@ -631,7 +642,7 @@ __global__ void __launch_bounds__(kTopThreads) k_top(DetectArgs a)
     }
     if (lane == 0 && tested) atomicAdd(a.counts + kCountTested, tested);
     flush_found(a, wc, lane);
-    if (a.fuse_narrow && wc.n > 0) test_candidates(a, wc.buf, wc.n, lane);
+    if (wc.n > 0) flush_candidates(a, wc.buf, wc.n, lane);
 }
 
 // The wide bottom of the traversal, round `round` (>= 1): every warp takes
@@ -684,7 +695,7 @@ __global__ void __launch_bounds__(kDetectThreads) k_walk(DetectArgs a, uint32_t 
     }
     if (lane == 0 && tested) atomicAdd(a.counts + kCountTested, tested);
     flush_found(a, wc, lane);
-    if (a.fuse_narrow && wc.n > 0) test_candidates(a, wc.buf, wc.n, lane);
+    if (wc.n > 0) flush_candidates(a, wc.buf, wc.n, lane);
 }
 
 // Narrow phase over stored candidates (the split broad/narrow API):
@@ -758,7 +769,48 @@ __device__ __forceinline__ void settle_fp64(const DetectArgs& a, const uint64_t*
     }
 }
 
-__global__ void __launch_bounds__(kDetectThreads) k_narrow_prec(DetectArgs a)
+// Pass 1 in lockstep: every lane holds one candidate and evaluates ONE axis
+// of it per iteration with the same instructions (the axis is chosen by
+// selects, not branches); a lane whose candidate is decided takes the next
+// one from the warp's range. Axis order: the two face normals, the six
+// in-plane axes, then the nine edge-edge axes (coplanar neighbours separate
+// early on the in-plane ones).
+struct LaneTri {
+    V3 p2, p3, q1, q2, q3;  // relative vertices (p1 = 0); their bound is u|x|
+    EV3 n1, m1;             // face normals with error bounds
+};
+
+__device__ __forceinline__ EV3 ev_rel(const V3& v)
+{
+    return EV3{v, V3{kU * fabsf(v.x), kU * fabsf(v.y), kU * fabsf(v.z)}};
+}
+__device__ __forceinline__ V3 vsel(bool c, const V3& a, const V3& b)
+{
+    return V3{c ? a.x : b.x, c ? a.y : b.y, c ? a.z : b.z};
+}
+__device__ __forceinline__ EV3 esel(bool c, const EV3& a, const EV3& b) { return EV3{vsel(c, a.v, b.v), vsel(c, a.e, b.e)}; }
+
+// Axis `k` (0..16, the reference numbering) of the lane's candidate, built
+// with selects only (no divergence between lanes on different axes).
+__device__ __forceinline__ EV3 axis_of(uint32_t k, const LaneTri& t)
+{
+    const EV3 zero{V3{0.0f, 0.0f, 0.0f}, V3{0.0f, 0.0f, 0.0f}};
+    const EV3 p2 = ev_rel(t.p2), p3 = ev_rel(t.p3), q1 = ev_rel(t.q1), q2 = ev_rel(t.q2), q3 = ev_rel(t.q3);
+    // edges as the reference forms them: e1 = p2 - p1, e2 = p3 - p2, e3 = p1 - p3,
+    // f1 = q2 - q1, f2 = q3 - q2, f3 = q1 - q3
+    const uint32_t ei = k < 11 ? (k - 2) / 3 : k - 11;  // edge of A (axes 2..13)
+    const uint32_t fj = k < 11 ? (k - 2) % 3 : k - 14;  // edge of B (axes 2..10, 14..16)
+    const EV3 E = esub(esel(ei == 0, p2, esel(ei == 1, p3, zero)), esel(ei == 0, zero, esel(ei == 1, p2, p3)));
+    const EV3 F = esub(esel(fj == 0, q2, esel(fj == 1, q3, q1)), esel(fj == 0, q1, esel(fj == 1, q2, q3)));
+    const bool ef = k >= 2 && k < 11, en = k >= 11 && k < 14;
+    const EV3 X = esel(ef || en, E, F);
+    const EV3 Y = esel(ef, F, esel(en, t.n1, t.m1));
+    return esel(k == 0, t.n1, esel(k == 1, t.m1, ecross(X, Y)));
+}
+
+__constant__ uint8_t c_axis_order[17] = {0, 1, 11, 12, 13, 14, 15, 16, 2, 3, 4, 5, 6, 7, 8, 9, 10};
+
+__global__ void __launch_bounds__(kDetectThreads, 2) k_narrow_prec(DetectArgs a)
 {
     __shared__ uint64_t s_qc[kDetectThreads / 32][kFp64Queue];
     __shared__ uint32_t s_qm[kDetectThreads / 32][kFp64Queue];
@@ -766,25 +818,86 @@ __global__ void __launch_bounds__(kDetectThreads) k_narrow_prec(DetectArgs a)
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+    // this warp's contiguous range of candidates
+    const uint32_t per = (n + n_warps - 1) / n_warps;
+    const uint32_t lo = min(n, warp * per), hi = min(n, lo + per);
     uint64_t* qc = s_qc[wib];
     uint32_t* qm = s_qm[wib];
-    uint32_t qn = 0;  // warp-uniform
-    for (uint32_t base = warp * 32; base < n; base += n_warps * 32) {
-        const uint32_t i = base + lane;
+    uint32_t qn = 0;    // FP64 queue fill (warp-uniform)
+    uint32_t next = lo; // next candidate of the range (warp-uniform)
+
+    bool busy = false;  // this lane holds a candidate in pass 1
+    uint64_t c = 0;
+    LaneTri t;
+    uint32_t step = 0, undecided = 0;
+    bool sep32 = false;
+    for (;;) {
+        // ---- refill idle lanes, decide what needs no axis at all ----
         bool hit = false, queue = false;
-        uint32_t mask = 0;
         uint4 rec = make_uint4(0, 0, 0, 0);
-        uint64_t c = 0;
-        if (i < n) {
-            c = a.cand[i];
+        uint32_t mask = 0;
+        const uint32_t idle = __ballot_sync(0xffffffffu, !busy);
+        const uint32_t take = min((uint32_t)__popc(idle), hi - next);
+        const uint32_t rank = __popc(idle & ((1u << lane) - 1u));
+        if (!busy && rank < take) {
+            c = a.cand[next + rank];
             V3 P1, P2, P3, Q1, Q2, Q3;
             load_tris(a, c, P1, P2, P3, Q1, Q2, Q3, rec);
-            bool hit32 = false;
-            const uint32_t st = tri_pass1(P1, P2, P3, Q1, Q2, Q3, mask, hit32);
-            hit = st == kPass1Hit;
-            queue = st == kPass1Undecided;
-            mask |= hit32 ? 0x80000000u : 0u;
+            const V3 p2v = vsub(P2, P1), p3v = vsub(P3, P1);
+            const V3 q1v = vsub(Q1, P1), q2v = vsub(Q2, P1), q3v = vsub(Q3, P1);
+            float A = fmaxf(fmaxf(fmaxf(fabsf(p2v.x), fabsf(p2v.y)), fmaxf(fabsf(p2v.z), fabsf(p3v.x))),
+                            fmaxf(fmaxf(fabsf(p3v.y), fabsf(p3v.z)), fmaxf(fabsf(q1v.x), fabsf(q1v.y))));
+            A = fmaxf(A, fmaxf(fmaxf(fabsf(q1v.z), fabsf(q2v.x)), fmaxf(fabsf(q2v.y), fabsf(q2v.z))));
+            A = fmaxf(A, fmaxf(fmaxf(fabsf(q3v.x), fabsf(q3v.y)), fabsf(q3v.z)));
+            if (!(A >= 0x1p-20f && A <= 0x1p20f)) {
+                // the bounds could under- or overflow: every axis in FP64
+                queue = true;
+                mask = ((1u << 17) - 1u) | (tri_intersect_exact(P1, P2, P3, Q1, Q2, Q3) ? 0x80000000u : 0u);
+            } else if (veq(P1, Q1) || veq(P1, Q2) || veq(P1, Q3) || veq(P2, Q1) || veq(P2, Q2) || veq(P2, Q3) ||
+                       veq(P3, Q1) || veq(P3, Q2) || veq(P3, Q3)) {
+                hit = true;  // a shared vertex: never separated
+            } else {
+                const EV3 zero{V3{0.0f, 0.0f, 0.0f}, V3{0.0f, 0.0f, 0.0f}};
+                t.p2 = p2v;
+                t.p3 = p3v;
+                t.q1 = q1v;
+                t.q2 = q2v;
+                t.q3 = q3v;
+                t.n1 = ecross(esub(ev_rel(p2v), zero), esub(ev_rel(p3v), ev_rel(p2v)));
+                t.m1 = ecross(esub(ev_rel(q2v), ev_rel(q1v)), esub(ev_rel(q3v), ev_rel(q2v)));
+                busy = true;
+                step = 0;
+                undecided = 0;
+                sep32 = false;
+            }
         }
+        next += take;
+        // ---- one axis per busy lane ----
+        if (busy) {
+            const uint32_t k = c_axis_order[step];
+            const EV3 zero{V3{0.0f, 0.0f, 0.0f}, V3{0.0f, 0.0f, 0.0f}};
+            bool s32;
+            const uint32_t r = project6_bounded(axis_of(k, t), zero, ev_rel(t.p2), ev_rel(t.p3), ev_rel(t.q1),
+                                                ev_rel(t.q2), ev_rel(t.q3), s32);
+            if (r == 0u) {
+                busy = false;  // separates in every arithmetic: no hit
+            } else {
+                sep32 |= s32;
+                if (r == 2u) undecided |= 1u << k;
+                if (++step == 17) {
+                    busy = false;
+                    if (undecided == 0) {
+                        hit = true;
+                        const PairView& pv = a.pairs[bvtt_pair(c)];
+                        rec = make_uint4(pv.a, pv.b, __ldg(pv.ta.face + bvtt_a(c)).w, __ldg(pv.tb.face + bvtt_b(c)).w);
+                    } else {
+                        queue = true;
+                        mask = undecided | (sep32 ? 0u : 0x80000000u);
+                    }
+                }
+            }
+        }
+        // ---- results: hits out, undecided candidates to the FP64 queue ----
         append_hit(a, hit, rec, lane);
         const uint32_t qmask = __ballot_sync(0xffffffffu, queue);
         if (queue) {
@@ -799,6 +912,7 @@ __global__ void __launch_bounds__(kDetectThreads) k_narrow_prec(DetectArgs a)
             qn -= 32;
             __syncwarp();
         }
+        if (!__any_sync(0xffffffffu, busy) && next >= hi) break;
     }
     if (qn > 0) settle_fp64(a, qc, qm, qn, lane);
 }
