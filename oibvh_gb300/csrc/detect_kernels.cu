@@ -149,10 +149,6 @@ __device__ __forceinline__ bool project6_d(const D3& ax, const D3& p1, const D3&
     if (mn2 > mx1) return false;
     return true;
 }
-__device__ __forceinline__ const D3& pick3(uint32_t i, const D3& a, const D3& b, const D3& c)
-{
-    return i == 0 ? a : (i == 1 ? b : c);
-}
 
 // Relative vertices of the FP64 formula: p_i = P_i - P1, q_j = Q_j - P1.
 struct D6 {
@@ -172,14 +168,15 @@ __device__ __forceinline__ D6 fp64_relative(const V3& P1, const V3& P2, const V3
 __device__ __forceinline__ bool axis_overlaps_fp64(uint32_t k, const D6& r)
 {
     const D3 p1{0.0, 0.0, 0.0};
-    const D3 e1 = dsub(r.p2, p1), e2 = dsub(r.p3, r.p2), e3 = dsub(p1, r.p3);
-    const D3 f1 = dsub(r.q2, r.q1), f2 = dsub(r.q3, r.q2), f3 = dsub(r.q1, r.q3);
+    // only the edges this axis needs, each formed as the FP64 formula forms it
+    auto e = [&](uint32_t i) { return i == 0 ? dsub(r.p2, p1) : (i == 1 ? dsub(r.p3, r.p2) : dsub(p1, r.p3)); };
+    auto f = [&](uint32_t j) { return j == 0 ? dsub(r.q2, r.q1) : (j == 1 ? dsub(r.q3, r.q2) : dsub(r.q1, r.q3)); };
     D3 ax;
-    if (k == 0) ax = dcross(e1, e2);
-    else if (k == 1) ax = dcross(f1, f2);
-    else if (k < 11) ax = dcross(pick3((k - 2) / 3, e1, e2, e3), pick3((k - 2) % 3, f1, f2, f3));
-    else if (k < 14) ax = dcross(pick3(k - 11, e1, e2, e3), dcross(e1, e2));
-    else ax = dcross(pick3(k - 14, f1, f2, f3), dcross(f1, f2));
+    if (k == 0) ax = dcross(e(0), e(1));
+    else if (k == 1) ax = dcross(f(0), f(1));
+    else if (k < 11) ax = dcross(e((k - 2) / 3), f((k - 2) % 3));
+    else if (k < 14) ax = dcross(e(k - 11), dcross(e(0), e(1)));
+    else ax = dcross(f(k - 14), dcross(f(0), f(1)));
     return project6_d(ax, p1, r.p2, r.p3, r.q1, r.q2, r.q3);
 }
 
