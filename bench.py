@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["batched", "precision", "serving", "deforming", "plain"], default="batched")
-    ap.add_argument("--rates", default="1000,3000,10000,30000,100000", help="serving: offered query rates (1/s)")
+    ap.add_argument("--rates", default="1000,3000,10000,30000,60000,100000", help="serving: offered query rates (1/s)")
     ap.add_argument("--pool", type=int, default=2000, help="serving: resident meshes")
     ap.add_argument("--budget-gb", type=float, default=16.0, help="serving: device memory budget for query slots")
     ap.add_argument("--pairs", type=int, default=512, help="mesh pairs of the batched workload")
@@ -1162,7 +1162,7 @@ def run_ours_serving(args, rank, world, local):
                 "mean_batch": round(float(sizes.mean()), 2), "pairs": int(pairs)}
 
     # warm-up stream (lane buffers grow to their working sizes)
-    run_stream(2000.0, 2000, seed=99)
+    run_stream(30000.0, 6000, seed=99)
     sweep = []
     for i, rate in enumerate(rates):
         n = int(min(max(2000, rate * 0.4), 40000))

@@ -319,6 +319,11 @@ int oibvh_server_set_entry_level(oibvh_server_t s, uint32_t entry_level);
 /* Starting capacities (entries) of each lane's BVTT work lists and hit
  * queue; they grow on demand (the batch is redone). 0 keeps a value. */
 int oibvh_server_set_queue_capacity(oibvh_server_t s, uint32_t front, uint32_t hits);
+/* Largest batch, in triangles of A + B summed over its queries (default
+ * 32 Mi; 0 = no limit). A batch completes as a whole, so this bounds how
+ * long one query can wait for the others of its batch; a single query
+ * larger than the limit still runs, alone. */
+int oibvh_server_set_batch_cost(oibvh_server_t s, uint64_t max_triangles);
 int oibvh_server_add_mesh(oibvh_server_t s, oibvh_tree_t t, uint32_t* id);
 int oibvh_server_start(oibvh_server_t s);
 int oibvh_server_submit(oibvh_server_t s, uint32_t mesh_a, uint32_t mesh_b, const float* mat_b, uint64_t* ticket);

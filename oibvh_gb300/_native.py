@@ -126,6 +126,7 @@ SIGNATURES = [
     ("oibvh_server_create", ctypes.c_int, [ctypes.c_int, _u64, _u32, _u32, ctypes.POINTER(_vp)]),
     ("oibvh_server_set_entry_level", ctypes.c_int, [_vp, _u32]),
     ("oibvh_server_set_queue_capacity", ctypes.c_int, [_vp, _u32, _u32]),
+    ("oibvh_server_set_batch_cost", ctypes.c_int, [_vp, _u64]),
     ("oibvh_server_add_mesh", ctypes.c_int, [_vp, _vp, _u32p]),
     ("oibvh_server_start", ctypes.c_int, [_vp]),
     ("oibvh_server_submit", ctypes.c_int, [_vp, _u32, _u32, _f32p, ctypes.POINTER(_u64)]),

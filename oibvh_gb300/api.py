@@ -353,6 +353,9 @@ class Server:
         N.check(N.lib().oibvh_server_set_queue_capacity(self._h, int(front), int(hits)),
                 "oibvh_server_set_queue_capacity")
 
+    def set_batch_cost(self, max_triangles: int) -> None:
+        N.check(N.lib().oibvh_server_set_batch_cost(self._h, int(max_triangles)), "oibvh_server_set_batch_cost")
+
     def add_mesh(self, tree: "OibvhTree") -> int:
         i = ctypes.c_uint32()
         N.check(N.lib().oibvh_server_add_mesh(self._h, tree.handle, ctypes.byref(i)), "oibvh_server_add_mesh")

@@ -129,8 +129,8 @@ struct Lane {
     DevBuf<uint32_t> counts;
     PinnedBuf<uint32_t> h_counts;
     PinnedBuf<uint4> h_hits;
-    uint32_t front_cap = 1u << 20, hit_cap = 1u << 18;
-    uint32_t cap_gen = 0;  // queue capacities follow the server's settings of this generation
+    uint32_t front_cap = 0, hit_cap = 0;  // set from the server's capacities at the first batch
+    uint32_t cap_gen = ~0u;  // queue capacities follow the server's settings of this generation
     uint32_t rounds = kServeWalkRoundsInit;
     uint64_t front0_count = 0;
     uint32_t n_pairs = 0;
@@ -142,6 +142,16 @@ struct Lane {
         if (st) cudaStreamDestroy(st);
     }
 };
+
+// Staging buffers grow to powers of two: allocating (cudaMallocHost,
+// cudaMalloc/cudaFree) stalls the device, so it must stay rare in the loop.
+template <class Buf>
+int ensure_pow2(Buf& b, size_t want, const char* what)
+{
+    size_t n = 64;
+    while (n < want) n <<= 1;
+    return b.ensure(n, what);
+}
 
 uint32_t grow(uint64_t need, uint32_t cur)
 {
@@ -157,7 +167,11 @@ struct oibvh_server_s {
     uint32_t max_batch = 0;
     uint32_t entry_level = 4;
     uint32_t start_log2 = 16;
-    uint32_t init_front_cap = 1u << 20, init_hit_cap = 1u << 18, cap_gen = 0;
+    // lane queue capacities: generous from the start (a regrowth redoes a
+    // batch synchronously), and shared: a lane that had to grow raises them
+    // for every lane before its next batch
+    uint32_t init_front_cap = 1u << 22, init_hit_cap = 1u << 21, cap_gen = 0;
+    uint64_t max_batch_cost = 32ull << 20;  // triangles (A + B) per batch, 0 = no limit
     std::vector<oibvh_tree_t> pool;
     DevBuf<uint8_t> arena_mem;
     Arena arena;
@@ -203,17 +217,17 @@ int oibvh_server_s::launch(Lane& L, std::vector<Query*>& batch)
 {
     const uint32_t n = (uint32_t)batch.size();
     const uint32_t per = refit_counters_per_tree();
-    OK_TRY(L.h_views.ensure(2 * n, "cudaMallocHost(views)"));
-    OK_TRY(L.views.ensure(2 * n, "cudaMalloc(views)"));
-    OK_TRY(L.h_pairs.ensure(n, "cudaMallocHost(pairs)"));
-    OK_TRY(L.pairv.ensure(n, "cudaMalloc(pairs)"));
-    OK_TRY(L.h_jobs.ensure(n, "cudaMallocHost(jobs)"));
-    OK_TRY(L.jobs.ensure(n, "cudaMalloc(jobs)"));
-    OK_TRY(L.h_rjobs.ensure(n, "cudaMallocHost(refit jobs)"));
-    OK_TRY(L.rjobs.ensure(n, "cudaMalloc(refit jobs)"));
-    OK_TRY(L.h_mats.ensure(12 * (size_t)n, "cudaMallocHost(matrices)"));
-    OK_TRY(L.mats.ensure(12 * (size_t)n, "cudaMalloc(matrices)"));
-    OK_TRY(L.rcount.ensure((size_t)per * n, "cudaMalloc(refit counters)"));
+    OK_TRY(ensure_pow2(L.h_views, 2 * n, "cudaMallocHost(views)"));
+    OK_TRY(ensure_pow2(L.views, 2 * n, "cudaMalloc(views)"));
+    OK_TRY(ensure_pow2(L.h_pairs, n, "cudaMallocHost(pairs)"));
+    OK_TRY(ensure_pow2(L.pairv, n, "cudaMalloc(pairs)"));
+    OK_TRY(ensure_pow2(L.h_jobs, n, "cudaMallocHost(jobs)"));
+    OK_TRY(ensure_pow2(L.jobs, n, "cudaMalloc(jobs)"));
+    OK_TRY(ensure_pow2(L.h_rjobs, n, "cudaMallocHost(refit jobs)"));
+    OK_TRY(ensure_pow2(L.rjobs, n, "cudaMalloc(refit jobs)"));
+    OK_TRY(ensure_pow2(L.h_mats, 12 * (size_t)n, "cudaMallocHost(matrices)"));
+    OK_TRY(ensure_pow2(L.mats, 12 * (size_t)n, "cudaMalloc(matrices)"));
+    OK_TRY(ensure_pow2(L.rcount, (size_t)per * n, "cudaMalloc(refit counters)"));
     OK_TRY(L.counts.ensure(kCountTotal, "cudaMalloc(counts)"));
     OK_TRY(L.h_counts.ensure(kCountTotal, "cudaMallocHost(counts)"));
 
@@ -280,12 +294,15 @@ int oibvh_server_s::launch(Lane& L, std::vector<Query*>& batch)
     {
         std::lock_guard<std::mutex> lk(mu);
         if (L.cap_gen != cap_gen) {
+            // adopt the server's capacities (set by the caller, or raised by a lane that grew)
+            if (L.front_cap != init_front_cap) {
+                L.front0.release();
+                L.front1.release();
+            }
+            if (L.hit_cap != init_hit_cap) L.hits.release();
             L.front_cap = init_front_cap;
             L.hit_cap = init_hit_cap;
             L.cap_gen = cap_gen;
-            L.front0.release();
-            L.front1.release();
-            L.hits.release();
         }
     }
     cudaStream_t st = L.st;
@@ -378,6 +395,13 @@ int oibvh_server_s::advance(Lane& L)
             {
                 std::lock_guard<std::mutex> lk(mu);
                 stats.redos++;
+                // the other lanes take the grown capacities before their next batch
+                if (L.front_cap > init_front_cap || L.hit_cap > init_hit_cap) {
+                    init_front_cap = std::max(init_front_cap, L.front_cap);
+                    init_hit_cap = std::max(init_hit_cap, L.hit_cap);
+                    cap_gen++;
+                    L.cap_gen = cap_gen;
+                }
             }
             return enqueue_detect(L);
         }
@@ -387,7 +411,7 @@ int oibvh_server_s::advance(Lane& L)
             stats.candidates += c[kCountCands];
             stats.hits += L.n_hits;
         }
-        OK_TRY(L.h_hits.ensure(std::max<uint64_t>(1, L.n_hits), "cudaMallocHost(hits)"));
+        OK_TRY(ensure_pow2(L.h_hits, std::max<uint64_t>(L.n_hits, L.hit_cap), "cudaMallocHost(hits)"));
         if (L.n_hits)
             CUDA_TRY(cudaMemcpyAsync(L.h_hits.p, L.hits.p, L.n_hits * sizeof(uint4), cudaMemcpyDeviceToHost, L.st));
         CUDA_TRY(cudaEventRecord(L.ev, L.st));
@@ -433,10 +457,15 @@ void oibvh_server_s::loop()
             std::vector<Query*> batch;
             {
                 std::lock_guard<std::mutex> lk(mu);
+                uint64_t cost = 0;
                 while (!pending.empty() && batch.size() < max_batch) {
                     Query* q = pending.front();
+                    // a batch completes as a whole: bound its work (the first query always goes)
+                    const uint64_t qc = (uint64_t)pool[q->a]->nT + pool[q->b]->nT;
+                    if (!batch.empty() && max_batch_cost && cost + qc > max_batch_cost) break;
                     size_t off = 0;
                     if (!arena.alloc(q->slot_bytes, off)) break;  // FIFO: the head waits for memory
+                    cost += qc;
                     q->slot_off = off;
                     q->pos = (float4*)(arena_mem.p + off);
                     q->box = (float4*)(arena_mem.p + off + align_up((size_t)pool[q->b]->nV * sizeof(float4)));
@@ -539,6 +568,14 @@ API int oibvh_server_set_queue_capacity(oibvh_server_t s, uint32_t front, uint32
     if (front) s->init_front_cap = front;
     if (hits) s->init_hit_cap = hits;
     s->cap_gen++;
+    return OIBVH_OK;
+}
+
+API int oibvh_server_set_batch_cost(oibvh_server_t s, uint64_t max_triangles)
+{
+    if (!s) return fail(OIBVH_ERR_ARG, "server is NULL");
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->max_batch_cost = max_triangles;
     return OIBVH_OK;
 }
 

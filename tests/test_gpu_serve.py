@@ -164,3 +164,17 @@ def test_concurrent_submitters(gpu):
     for k, q in enumerate(qs):
         assert np.array_equal(results[k], _oracle(meshes, q)), k
     srv.close()
+
+
+def test_batch_cost_limit(gpu):
+    """With a one-triangle batch budget every query runs alone, and results
+    stay those of the oracle."""
+    meshes = _pool(6, seed=14)
+    qs = _queries(len(meshes), 20, seed=8)
+    srv = _server(meshes, lanes=2)
+    srv.set_batch_cost(1)
+    mix, sizes = _run_mix(srv, qs)
+    assert max(sizes) == 1
+    for k, q in enumerate(qs):
+        assert np.array_equal(mix[k], _oracle(meshes, q))
+    srv.close()
