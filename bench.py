@@ -65,6 +65,23 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(values, dist, device):
+    """The max over ranks of each value (the job's time is its slowest
+    replica's); `dist` None means a single process."""
+    import torch
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
+def replicas_value(units_per_rank, world, ms_max):
+    """Whole-job throughput of N independent replicas: every rank processed
+    `units_per_rank` units; the job took the slowest rank's time."""
+    return units_per_rank * world / (ms_max / 1e3)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -341,10 +358,7 @@ def run_ours(args, rank, world, local):
     refit_ms = statistics.mean(s.elapsed_time(e) for s, e in zip(rf_s, rf_e))
 
     # max over ranks
-    t_dev = torch.tensor([ms_dev, ms_e2e], dtype=torch.float64, device=f"cuda:{dev}")
-    if dist is not None:
-        dist.all_reduce(t_dev, op=dist.ReduceOp.MAX)
-    ms_dev, ms_e2e = float(t_dev[0]), float(t_dev[1])
+    ms_dev, ms_e2e = max_over_ranks([ms_dev, ms_e2e], dist, f"cuda:{dev}")
     if dist is not None:
         dist.destroy_process_group()
     if rank != 0:
@@ -352,7 +366,7 @@ def run_ours(args, rank, world, local):
 
     K = args.steps
     queries = K * world
-    value = queries / (ms_dev / 1e3)
+    value = replicas_value(K, world, ms_dev)
     e2e = queries / (ms_e2e / 1e3)
     tri_total = sum(m.n_triangles for m in w.meshes)
     V = sum(m.n_vertices for m in w.meshes)
@@ -662,18 +676,16 @@ def run_ours_batched(args, rank, world, local):
         rf.append(e0.elapsed_time(e1))
     refit_ms = statistics.median(rf)
 
-    t_dev = torch.tensor([ms_dev, ms_e2e], dtype=torch.float64, device=f"cuda:{dev}")
+    ms_dev, ms_e2e = max_over_ranks([ms_dev, ms_e2e], dist, f"cuda:{dev}")
     if dist is not None:
-        dist.all_reduce(t_dev, op=dist.ReduceOp.MAX)
         dist.destroy_process_group()
-    ms_dev, ms_e2e = float(t_dev[0]), float(t_dev[1])
     if rank != 0:
         return None
 
     K = args.steps
     n_pairs = len(w.pairs)
     queries = K * n_pairs * world
-    value = queries / (ms_dev / 1e3)
+    value = replicas_value(K * n_pairs, world, ms_dev)
 
     def tree_size(T):
         p2 = 1 << (T - 1).bit_length()
@@ -970,15 +982,13 @@ def run_ours_precision(args, rank, world, local):
     plain_s = (time.perf_counter() - tp0) / 3
     plain_hits = sum(ps.getIntTriPairCount() for ps in plain)
 
-    t_dev = torch.tensor([ms_f, ms_e2e], dtype=torch.float64, device=f"cuda:{dev}")
+    ms_f, ms_e2e = max_over_ranks([ms_f, ms_e2e], dist, f"cuda:{dev}")
     if dist is not None:
-        dist.all_reduce(t_dev, op=dist.ReduceOp.MAX)
         dist.destroy_process_group()
-    ms_f, ms_e2e = float(t_dev[0]), float(t_dev[1])
     if rank != 0:
         return None
     K = args.steps
-    value = K * n_pairs * world / (ms_f / 1e3)
+    value = replicas_value(K * n_pairs, world, ms_f)
     line = {
         "metric": "collision queries/s (mesh pairs through refit + broad + narrow), FP64-filtered triangle test",
         "value": round(value, 1), "unit": "queries/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
