@@ -31,6 +31,8 @@ __all__ = [
     "rigid_transform",
     "jitter",
     "mesh_digest",
+    "load_obj",
+    "save_obj",
 ]
 
 
@@ -259,3 +261,49 @@ def mesh_digest(*arrays: np.ndarray) -> str:
         h.update(str(a.shape).encode())
         h.update(a.tobytes())
     return h.hexdigest()
+
+
+def load_obj(path: str) -> Mesh:
+    """Minimal Wavefront OBJ reader for the collision path: `v x y z [w]`
+    positions and `f` faces (`i`, `i/t`, `i//n`, `i/t/n`, 1-based or negative
+    relative indices); polygons are split into fans (v0, vi, vi+1), the
+    triangulation the reference's loader asks assimp for (aiProcess_Triangulate,
+    src/utils/model.cpp:49-51). Normals, texture coordinates, groups and
+    materials are ignored: collision reads positions and index triples only.
+    Positions are parsed as float64 and rounded once to float32."""
+    xyz: list = []
+    tri: list = []
+    with open(path, "r", encoding="utf-8", errors="replace") as fh:
+        for ln, line in enumerate(fh, 1):
+            parts = line.split("#", 1)[0].split()
+            if not parts:
+                continue
+            if parts[0] == "v":
+                if len(parts) < 4:
+                    raise ValueError(f"{path}:{ln}: vertex needs three coordinates")
+                xyz.append((float(parts[1]), float(parts[2]), float(parts[3])))
+            elif parts[0] == "f":
+                idx = []
+                for tok in parts[1:]:
+                    k = int(tok.split("/", 1)[0])
+                    k = k - 1 if k > 0 else len(xyz) + k
+                    if not 0 <= k < len(xyz):
+                        raise ValueError(f"{path}:{ln}: face refers to vertex {tok} of {len(xyz)}")
+                    idx.append(k)
+                if len(idx) < 3:
+                    raise ValueError(f"{path}:{ln}: a face needs three vertices")
+                for i in range(1, len(idx) - 1):
+                    tri.append((idx[0], idx[i], idx[i + 1]))
+    if not tri:
+        raise ValueError(f"{path}: no faces")
+    return Mesh(np.asarray(xyz, dtype=np.float64).astype(np.float32), np.asarray(tri, dtype=np.uint32))
+
+
+def save_obj(mesh: Mesh, path: str) -> None:
+    """Write positions and triangles as OBJ (positions with float32 round-trip precision)."""
+    with open(path, "w", encoding="utf-8") as fh:
+        # 9 significant digits identify a float32 exactly
+        for x, y, z in mesh.xyz.astype(np.float32).astype(np.float64).tolist():
+            fh.write(f"v {x:.9g} {y:.9g} {z:.9g}\n")
+        for a, b, c in (mesh.tri.astype(np.int64) + 1).tolist():
+            fh.write(f"f {a} {b} {c}\n")

@@ -169,3 +169,31 @@ def test_positions_xyzw_in_place(gpu):
 
     with pytest.raises(OibvhError):
         trees[0].set_positions4_device(dev[0].data_ptr() + 4)
+
+
+def test_obj_meshes_through_the_pipeline(gpu, tmp_path):
+    """A mesh read from an OBJ file collides exactly as the oracle says."""
+    import numpy as np
+
+    from oibvh_gb300 import DeviceType, OibvhTree, Scene
+    from oibvh_gb300 import meshes as M
+    from oracle.oracle import Port, sort_pairs
+
+    a = M.noise_displace(M.icosphere(4), 0.05, seed=1)
+    b = M.rigid_transform(M.noise_displace(M.icosphere(4), 0.05, seed=2), np.eye(3), (0.9, 0.1, 0.0))
+    paths = [str(tmp_path / "a.obj"), str(tmp_path / "b.obj")]
+    for m, p in zip((a, b), paths):
+        M.save_obj(m, p)
+    meshes = [M.load_obj(p) for p in paths]
+    trees = [OibvhTree(m) for m in meshes]
+    sc = Scene()
+    for t in trees:
+        t.build()
+        sc.addOibvhTree(t)
+    sc.detectCollision(DeviceType.GPU0, 4, 3)
+    port = Port()
+    for m in meshes:
+        port.add_mesh(m.xyz, m.tri)
+    want, _ = port.detect()
+    assert np.array_equal(sc.int_tri_pairs(), sort_pairs(want))
+    assert want.shape[0] > 0
