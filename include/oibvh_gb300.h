@@ -107,6 +107,12 @@ int oibvh_tree_set_positions_device(oibvh_tree_t t, const float* d_xyz, void* st
 int oibvh_tree_set_positions4_device(oibvh_tree_t t, const float* d_xyzw);
 
 /* OibvhTree::getDepth() (src/cuda/oibvhTree.cu:46-49) = floor(log2(size)). */
+/* Morton key width of the next build (OibvhTree::build, src/cuda/oibvh.cu:17-22
+ * uses 30 bits: 10 per axis). 63 (21 bits per axis) orders the leaves of
+ * large meshes more finely; the pair set does not depend on it. Default 30;
+ * a scene build needs the same width for all its trees. */
+int oibvh_tree_set_morton_bits(oibvh_tree_t t, uint32_t bits);
+uint32_t oibvh_tree_get_morton_bits(oibvh_tree_t t);
 uint32_t oibvh_tree_get_depth(oibvh_tree_t t);
 /* OibvhTree::getPrimCount() (src/cuda/oibvhTree.cu:51-54). */
 uint32_t oibvh_tree_get_prim_count(oibvh_tree_t t);

@@ -92,6 +92,8 @@ SIGNATURES = [
     ("oibvh_tree_set_positions", ctypes.c_int, [_vp, _f32p, _vp]),
     ("oibvh_tree_set_positions_device", ctypes.c_int, [_vp, _vp, _vp]),
     ("oibvh_tree_set_positions4_device", ctypes.c_int, [_vp, _vp]),
+    ("oibvh_tree_set_morton_bits", ctypes.c_int, [_vp, _u32]),
+    ("oibvh_tree_get_morton_bits", _u32, [_vp]),
     ("oibvh_tree_get_depth", _u32, [_vp]),
     ("oibvh_tree_get_prim_count", _u32, [_vp]),
     ("oibvh_tree_get_size", _u32, [_vp]),

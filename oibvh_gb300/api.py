@@ -108,6 +108,13 @@ class OibvhTree:
     def build(self, stream=None) -> None:
         N.check(N.lib().oibvh_tree_build(self._h, _stream_handle(stream)), "oibvh_tree_build")
 
+    def set_morton_bits(self, bits: int) -> None:
+        """Key width of the next build: 30 (the reference's) or 63."""
+        N.check(N.lib().oibvh_tree_set_morton_bits(self._h, int(bits)), "oibvh_tree_set_morton_bits")
+
+    def morton_bits(self) -> int:
+        return int(N.lib().oibvh_tree_get_morton_bits(self._h))
+
     def refit(self, xyz=None, stream=None) -> None:
         """Refit to host positions `xyz` (float32[V,3]), or to the positions
         already held when None. Stream-ordered."""

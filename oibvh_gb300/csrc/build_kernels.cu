@@ -102,6 +102,33 @@ __device__ __forceinline__ uint32_t stretch3(uint32_t x)
     return x;
 }
 
+// 21 bits -> every third bit of 63 (the wide key: 21 bits per axis)
+__device__ __forceinline__ uint64_t stretch3_21(uint32_t v)
+{
+    uint64_t x = v & 0x1fffffu;
+    x = (x | (x << 32)) & 0x1f00000000ffffull;
+    x = (x | (x << 16)) & 0x1f0000ff0000ffull;
+    x = (x | (x << 8)) & 0x100f00f00f00f00full;
+    x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+// The wide key's quantisation: as quant1024 with 2^21 cells per axis (the
+// scaling by 2^21 is exact, the clamp bound 2^21 - 1 is a float).
+__device__ __forceinline__ uint32_t quant2m(float u)
+{
+    float v = __fmul_rn(u, 2097152.0f);
+    v = (v < 0.0f) ? 0.0f : v;
+    v = (2097151.0f < v) ? 2097151.0f : v;
+    return __float2uint_rz(v);  // NaN -> 0
+}
+
+// The key of a leaf from its three cell coordinates: 30 bits (the
+// reference's morton3D, x << 2 | y << 1 | z) in `lo`, or 63 bits (same
+// interleave, 21 bits per axis) split into `lo` (bits 0..31) and `hi`.
+__device__ __forceinline__ void morton_key(const float u[3], bool wide, uint32_t& lo, uint32_t& hi);
+
 __device__ __forceinline__ uint32_t quant1024(float u)
 {
     float v = __fmul_rn(u, 1024.0f);
@@ -110,9 +137,22 @@ __device__ __forceinline__ uint32_t quant1024(float u)
     return __float2uint_rz(v);        // NaN -> 0
 }
 
+__device__ __forceinline__ void morton_key(const float u[3], bool wide, uint32_t& lo, uint32_t& hi)
+{
+    if (!wide) {
+        lo = (stretch3(quant1024(u[0])) << 2) | (stretch3(quant1024(u[1])) << 1) | stretch3(quant1024(u[2]));
+        hi = 0;
+        return;
+    }
+    const uint64_t k = (stretch3_21(quant2m(u[0])) << 2) | (stretch3_21(quant2m(u[1])) << 1) | stretch3_21(quant2m(u[2]));
+    lo = (uint32_t)k;
+    hi = (uint32_t)(k >> 32);
+}
+
 __global__ void __launch_bounds__(256) k_leaf_morton(const uint32_t* __restrict__ tri, const float4* __restrict__ pos,
                                                      uint32_t nT, const uint32_t* __restrict__ bound_keys,
-                                                     uint32_t* __restrict__ codes, uint32_t* __restrict__ idx)
+                                                     uint32_t* __restrict__ codes, uint32_t* __restrict__ idx,
+                                                     uint32_t* __restrict__ codes_hi)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nT) return;
@@ -126,7 +166,7 @@ __global__ void __launch_bounds__(256) k_leaf_morton(const uint32_t* __restrict_
                    f2 = __ldg(tri + 3 * (size_t)i + 2);
     const float4 p0 = __ldg(pos + f0), p1 = __ldg(pos + f1), p2 = __ldg(pos + f2);
     const float va[3] = {p0.x, p0.y, p0.z}, vb[3] = {p1.x, p1.y, p1.z}, vc[3] = {p2.x, p2.y, p2.z};
-    uint32_t q[3];
+    float u[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const float a = va[k], b = vb[k], c = vc[k];
@@ -134,9 +174,12 @@ __global__ void __launch_bounds__(256) k_leaf_morton(const uint32_t* __restrict_
         const float centroid = __fmul_rn(__fadd_rn(mn, mx), 0.5f);
         const float off = __fsub_rn(centroid, bmin[k]);
         const float len = __fsub_rn(bmax[k], bmin[k]);
-        q[k] = quant1024(__fdiv_rn(off, len));
+        u[k] = __fdiv_rn(off, len);
     }
-    codes[i] = (stretch3(q[0]) << 2) | (stretch3(q[1]) << 1) | stretch3(q[2]);
+    uint32_t lo, hi;
+    morton_key(u, codes_hi != nullptr, lo, hi);
+    codes[i] = lo;
+    if (codes_hi) codes_hi[i] = hi;
     idx[i] = i;
 }
 
@@ -309,10 +352,10 @@ cudaError_t launch_mesh_bounds(const float4* xyz, uint32_t nV, uint32_t* bound_k
 }
 
 cudaError_t launch_leaf_morton(const uint32_t* tri, const float4* xyz, uint32_t nT, const uint32_t* bound_keys,
-                               uint32_t* codes, uint32_t* idx, cudaStream_t s)
+                               uint32_t* codes, uint32_t* idx, uint32_t* codes_hi, cudaStream_t s)
 {
     note_launches(1);
-    k_leaf_morton<<<(nT + 255) / 256, 256, 0, s>>>(tri, xyz, nT, bound_keys, codes, idx);
+    k_leaf_morton<<<(nT + 255) / 256, 256, 0, s>>>(tri, xyz, nT, bound_keys, codes, idx, codes_hi);
     return cudaGetLastError();
 }
 
@@ -417,7 +460,7 @@ __global__ void __launch_bounds__(256) k_mesh_bounds_multi(const BuildJob* __res
 __global__ void __launch_bounds__(256) k_leaf_morton_multi(const BuildJob* __restrict__ jobs, uint32_t n_jobs,
                                                            const uint32_t* __restrict__ fjob,
                                                            uint32_t* __restrict__ codes, uint32_t* __restrict__ idx,
-                                                           uint32_t* __restrict__ tree_of)
+                                                           uint32_t* __restrict__ tree_of, uint32_t* __restrict__ codes_hi)
 {
     const uint32_t j = find_job(jobs, n_jobs, blockIdx.x, true, fjob);
     const BuildJob job = jobs[j];
@@ -433,15 +476,18 @@ __global__ void __launch_bounds__(256) k_leaf_morton_multi(const BuildJob* __res
                    f2 = __ldg(job.tri + 3 * (size_t)i + 2);
     const float4 p0 = __ldg(job.pos + f0), p1 = __ldg(job.pos + f1), p2 = __ldg(job.pos + f2);
     const float va[3] = {p0.x, p0.y, p0.z}, vb[3] = {p1.x, p1.y, p1.z}, vc[3] = {p2.x, p2.y, p2.z};
-    uint32_t q[3];
+    float u[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const float mn = gmin(gmin(va[k], vb[k]), vc[k]), mx = gmax(gmax(va[k], vb[k]), vc[k]);
         const float centroid = __fmul_rn(__fadd_rn(mn, mx), 0.5f);
-        q[k] = quant1024(__fdiv_rn(__fsub_rn(centroid, bmin[k]), __fsub_rn(bmax[k], bmin[k])));
+        u[k] = __fdiv_rn(__fsub_rn(centroid, bmin[k]), __fsub_rn(bmax[k], bmin[k]));
     }
     const uint32_t g = job.face_off + i;
-    codes[g] = (stretch3(q[0]) << 2) | (stretch3(q[1]) << 1) | stretch3(q[2]);
+    uint32_t lo, hi;
+    morton_key(u, codes_hi != nullptr, lo, hi);
+    codes[g] = lo;
+    if (codes_hi) codes_hi[g] = hi;
     idx[g] = g;
     tree_of[g] = j;
 }
@@ -509,20 +555,28 @@ __global__ void __launch_bounds__(256) k_transform_multi(const BuildJob* __restr
 
 cudaError_t launch_build_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, uint32_t f_blocks,
                                const uint32_t* vjob, const uint32_t* fjob, uint32_t n_faces, uint32_t tree_bits,
-                               void* scratch, cudaStream_t s)
+                               bool wide, void* scratch, cudaStream_t s)
 {
-    // scratch: codes, idx, tree_of, keys2 (4 x n_faces u32), then the sort scratch
+    // scratch: codes, idx, tree_of, keys2, codes_hi (5 x n_faces u32), then the sort scratch
     uint32_t* codes = (uint32_t*)scratch;
     uint32_t* idx = codes + n_faces;
     uint32_t* tree_of = idx + n_faces;
     uint32_t* keys2 = tree_of + n_faces;
-    void* sort_scratch = keys2 + n_faces;
+    uint32_t* codes_hi = keys2 + n_faces;
+    void* sort_scratch = codes_hi + n_faces;
     note_launches(4);
     k_bounds_init_multi<<<(n_jobs + 255) / 256, 256, 0, s>>>(d_jobs, n_jobs);
     k_mesh_bounds_multi<<<v_blocks, 256, 0, s>>>(d_jobs, n_jobs, vjob);
-    k_leaf_morton_multi<<<f_blocks, 256, 0, s>>>(d_jobs, n_jobs, fjob, codes, idx, tree_of);
-    cudaError_t e = launch_radix_sort(codes, idx, n_faces, 30, sort_scratch, s);
+    k_leaf_morton_multi<<<f_blocks, 256, 0, s>>>(d_jobs, n_jobs, fjob, codes, idx, tree_of, wide ? codes_hi : nullptr);
+    // stable LSD order: low key bits, [high key bits,] then the tree id
+    cudaError_t e = launch_radix_sort(codes, idx, n_faces, wide ? 32 : 30, sort_scratch, s);
     if (e != cudaSuccess) return e;
+    if (wide) {
+        note_launches(1);
+        k_gather_u32<<<(n_faces + 255) / 256, 256, 0, s>>>(codes_hi, idx, n_faces, keys2);
+        e = launch_radix_sort(keys2, idx, n_faces, 31, sort_scratch, s);
+        if (e != cudaSuccess) return e;
+    }
     k_gather_u32<<<(n_faces + 255) / 256, 256, 0, s>>>(tree_of, idx, n_faces, keys2);
     if (tree_bits > 0) {
         e = launch_radix_sort(keys2, idx, n_faces, (int)tree_bits, sort_scratch, s);
@@ -535,7 +589,7 @@ cudaError_t launch_build_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t
 
 size_t build_multi_scratch_bytes(uint32_t n_faces)
 {
-    return 4 * (size_t)n_faces * sizeof(uint32_t) + radix_sort_scratch_bytes(n_faces);
+    return 5 * (size_t)n_faces * sizeof(uint32_t) + radix_sort_scratch_bytes(n_faces);
 }
 
 cudaError_t launch_transform_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, const uint32_t* vjob,
@@ -544,6 +598,15 @@ cudaError_t launch_transform_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint
     note_launches(1);
     k_transform_multi<<<(v_blocks + kTransformUnroll - 1) / kTransformUnroll, 256, 0, s>>>(d_jobs, n_jobs, vjob, rest,
                                                                                             mats, v_blocks);
+    return cudaGetLastError();
+}
+
+
+cudaError_t launch_gather_u32(const uint32_t* src, const uint32_t* idx, uint32_t n, uint32_t* out, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    note_launches(1);
+    k_gather_u32<<<(n + 255) / 256, 256, 0, s>>>(src, idx, n, out);
     return cudaGetLastError();
 }
 

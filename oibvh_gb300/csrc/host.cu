@@ -95,16 +95,25 @@ static int tree_build_impl(oibvh_tree_t t, cudaStream_t s)
     const uint32_t nT = t->nT;
     // scratch: bounds keys, codes, indices, sort buffers
     DevBuf<uint8_t> scratch;
+    const bool wide = t->morton_bits == 63;
     const size_t sort_bytes = radix_sort_scratch_bytes(nT);
-    const size_t codes_off = 256, idx_off = codes_off + ((size_t)nT * 4 + 255) / 256 * 256;
-    const size_t sort_off = idx_off + ((size_t)nT * 4 + 255) / 256 * 256;
+    const size_t arr = ((size_t)nT * 4 + 255) / 256 * 256;
+    const size_t codes_off = 256, idx_off = codes_off + arr, hi_off = idx_off + arr, gath_off = hi_off + arr;
+    const size_t sort_off = gath_off + arr;
     OK_TRY(scratch.ensure(sort_off + sort_bytes, "cudaMalloc(build scratch)"));
     uint32_t* keys6 = (uint32_t*)scratch.p;
     uint32_t* codes = (uint32_t*)(scratch.p + codes_off);
     uint32_t* idx = (uint32_t*)(scratch.p + idx_off);
+    uint32_t* hi = (uint32_t*)(scratch.p + hi_off);
+    uint32_t* hi_sorted = (uint32_t*)(scratch.p + gath_off);
     CUDA_TRY(launch_mesh_bounds(t->cur_pos, t->nV, keys6, sm_count(t->device), s));
-    CUDA_TRY(launch_leaf_morton(t->tri.p, t->cur_pos, nT, keys6, codes, idx, s));
-    CUDA_TRY(launch_radix_sort(codes, idx, nT, 30, scratch.p + sort_off, s));
+    CUDA_TRY(launch_leaf_morton(t->tri.p, t->cur_pos, nT, keys6, codes, idx, wide ? hi : nullptr, s));
+    // stable LSD order by (key, original index): low key bits first, then the high ones
+    CUDA_TRY(launch_radix_sort(codes, idx, nT, wide ? 32 : 30, scratch.p + sort_off, s));
+    if (wide) {
+        CUDA_TRY(launch_gather_u32(hi, idx, nT, hi_sorted, s));
+        CUDA_TRY(launch_radix_sort(hi_sorted, idx, nT, 31, scratch.p + sort_off, s));
+    }
     CUDA_TRY(launch_gather_faces(t->tri.p, idx, nT, t->face.p, s));
     CUDA_TRY(launch_refit_one(t->job(), s));
     CUDA_TRY(cudaStreamSynchronize(s));
@@ -650,6 +659,16 @@ API int oibvh_tree_set_positions4_device(oibvh_tree_t t, const float* d_xyzw)
     GUARD_END
 }
 
+API int oibvh_tree_set_morton_bits(oibvh_tree_t t, uint32_t bits)
+{
+    if (!t) return fail(OIBVH_ERR_ARG, "tree is NULL");
+    if (bits != 30 && bits != 63) return fail(OIBVH_ERR_ARG, "Morton key width must be 30 or 63 bits");
+    t->morton_bits = bits;
+    return OIBVH_OK;
+}
+
+API uint32_t oibvh_tree_get_morton_bits(oibvh_tree_t t) { return t ? t->morton_bits : 0; }
+
 API uint32_t oibvh_tree_get_depth(oibvh_tree_t t) { return t ? ilog2(t->shape.size) : 0; }
 API uint32_t oibvh_tree_get_prim_count(oibvh_tree_t t) { return t ? t->nT : 0; }
 API uint32_t oibvh_tree_get_size(oibvh_tree_t t) { return t ? t->shape.size : 0; }
@@ -1032,8 +1051,12 @@ API int oibvh_scene_build(oibvh_scene_t s, void* stream)
     OK_TRY(scratch.ensure(build_multi_scratch_bytes(s->n_faces), "cudaMalloc(build scratch)"));
     const uint32_t n = (uint32_t)s->trees.size();
     const uint32_t tree_bits = n <= 1 ? 0u : ilog2(next_pow2(n));
+    const bool wide = s->trees[0]->morton_bits == 63;
+    for (auto t : s->trees)
+        if ((t->morton_bits == 63) != wide)
+            return fail(OIBVH_ERR_UNSUPPORTED, "a scene build needs the same Morton key width for every tree");
     CUDA_TRY(launch_build_multi(s->build_jobs.p, n, s->v_blocks, s->f_blocks, s->vblock_job.p, s->fblock_job.p,
-                                s->n_faces, tree_bits, scratch.p, st));
+                                s->n_faces, tree_bits, wide, scratch.p, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     for (auto t : s->trees) t->built = true;
     const int r = oibvh_scene_refit(s, stream);

@@ -174,6 +174,7 @@ struct oibvh_tree_s {
     DevBuf<float4> box;         // 2 * (size - nT): internal nodes only
     DevBuf<uint32_t> counters;  // refit climbing counters
     bool built = false;
+    uint32_t morton_bits = 30;  // 30 (the reference's key) or 63 (21 bits per axis)
 
     RefitJob job() const
     {

@@ -43,17 +43,21 @@ size_t radix_sort_scratch_bytes(uint32_t n);
 size_t build_multi_scratch_bytes(uint32_t n_faces);
 // vjob / fjob: optional host-built maps from a 256-vertex / 256-face block
 // to its job (nullptr: each CTA binary-searches the job table).
+// wide: 63-bit Morton keys (21 bits per axis) instead of the reference's 30.
 cudaError_t launch_build_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, uint32_t f_blocks,
                                const uint32_t* vjob, const uint32_t* fjob, uint32_t n_faces, uint32_t tree_bits,
-                               void* scratch, cudaStream_t s);
+                               bool wide, void* scratch, cudaStream_t s);
 cudaError_t launch_transform_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, const uint32_t* vjob,
                                    const float4* rest, const float* mats, cudaStream_t s);
 cudaError_t launch_xyz_to_pos4(const float* xyz, uint32_t nV, float4* pos, cudaStream_t s);
 cudaError_t launch_mesh_bounds(const float4* pos, uint32_t nV, uint32_t* bound_keys, int num_sms, cudaStream_t s);
+// codes_hi != nullptr: 63-bit keys, low 32 bits in codes and high 31 in codes_hi
 cudaError_t launch_leaf_morton(const uint32_t* tri, const float4* pos, uint32_t nT, const uint32_t* bound_keys,
-                               uint32_t* codes, uint32_t* idx, cudaStream_t s);
+                               uint32_t* codes, uint32_t* idx, uint32_t* codes_hi, cudaStream_t s);
 cudaError_t launch_radix_sort(uint32_t* keys, uint32_t* vals, uint32_t n, int key_bits, void* scratch,
                               cudaStream_t s);
+// out[i] = src[idx[i]]
+cudaError_t launch_gather_u32(const uint32_t* src, const uint32_t* idx, uint32_t n, uint32_t* out, cudaStream_t s);
 cudaError_t launch_gather_faces(const uint32_t* tri, const uint32_t* perm, uint32_t nT, uint4* out, cudaStream_t s);
 
 // refit_kernels.cu

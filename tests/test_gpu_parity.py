@@ -148,3 +148,42 @@ def test_scene_refit_one_launch_bit_exact(gpu):
     sc.detectCollision(DeviceType.GPU0, 4, 1)
     want, wc = _oracle_pairs([type(g["meshes"][0])(x, m.tri) for x, m in zip(moved, g["meshes"])])
     assert np.array_equal(sc.int_tri_pairs(), want) and sc.candidate_count() == wc
+
+
+def test_wide_morton_keys_order_and_pair_set(gpu):
+    """63-bit keys (21 bits per axis): the leaf order is the restated one, a
+    scene build agrees with per-tree builds, and the pair set is unchanged."""
+    from oibvh_gb300 import DeviceType, OibvhTree, Scene
+    from oibvh_gb300 import meshes as M
+    from oibvh_gb300 import workloads as W
+    from tests_support import morton63_order
+
+    meshes = [W.noise_displace_mesh(5, 0.05, 11), W.noise_displace_mesh(4, 0.05, 12)]
+    meshes[1] = M.rigid_transform(meshes[1], np.eye(3), (0.8, 0.2, 0.1))
+    trees = [OibvhTree(m) for m in meshes]
+    for t, m in zip(trees, meshes):
+        t.set_morton_bits(63)
+        assert t.morton_bits() == 63
+        t.build()
+        _, perm = t.sorted_faces()
+        assert np.array_equal(perm, morton63_order(m.xyz, m.tri))
+    sc = Scene()
+    for t in trees:
+        sc.addOibvhTree(t)
+    sc.detectCollision(DeviceType.GPU0, 4, 3)
+    port = Port()
+    for m in meshes:
+        port.add_mesh(m.xyz, m.tri)
+    want, wc = port.detect()
+    assert np.array_equal(sc.int_tri_pairs(), sort_pairs(want)) and want.shape[0] > 0
+    assert sc.candidate_count() == wc
+    # the same trees built together
+    trees2 = [OibvhTree(m) for m in meshes]
+    sc2 = Scene()
+    for t in trees2:
+        t.set_morton_bits(63)
+        sc2.addOibvhTree(t)
+    sc2.build()
+    for t, t2 in zip(trees, trees2):
+        assert np.array_equal(t.sorted_faces()[1], t2.sorted_faces()[1])
+        assert np.array_equal(t.aabb_tree().view(np.uint32), t2.aabb_tree().view(np.uint32))

@@ -69,3 +69,30 @@ def near_degenerate_pair(seed, n_tri=2000):
     ma = M.Mesh(A.reshape(-1, 3).astype(np.float32), np.arange(3 * n_tri, dtype=np.uint32).reshape(-1, 3))
     mb = M.Mesh(B.reshape(-1, 3).astype(np.float32), np.arange(3 * len(out), dtype=np.uint32).reshape(-1, 3))
     return ma, mb
+
+
+def morton63_order(xyz, tri):
+    """Face order of a 63-bit-key build, restated in numpy: per face the
+    centroid of its box, normalised by the mesh box (float32 operations in
+    the build's order), 2^21 cells per axis, keys interleaved x << 2 | y << 1
+    | z, then a stable sort by (key, face index)."""
+    x = np.asarray(xyz, dtype=np.float32)
+    t = np.asarray(tri, dtype=np.int64)
+    bmin, bmax = x.min(0), x.max(0)
+    v = x[t]                                      # [T, 3 vertices, 3 axes]
+    mn, mx = v.min(1), v.max(1)
+    centroid = (mn + mx) * np.float32(0.5)
+    u = (centroid - bmin) / (bmax - bmin)
+    q = np.clip(u * np.float32(2097152.0), np.float32(0.0), np.float32(2097151.0)).astype(np.uint64)
+
+    def stretch(a):
+        a = a & np.uint64(0x1FFFFF)
+        a = (a | (a << np.uint64(32))) & np.uint64(0x1F00000000FFFF)
+        a = (a | (a << np.uint64(16))) & np.uint64(0x1F0000FF0000FF)
+        a = (a | (a << np.uint64(8))) & np.uint64(0x100F00F00F00F00F)
+        a = (a | (a << np.uint64(4))) & np.uint64(0x10C30C30C30C30C3)
+        a = (a | (a << np.uint64(2))) & np.uint64(0x1249249249249249)
+        return a
+
+    key = (stretch(q[:, 0]) << np.uint64(2)) | (stretch(q[:, 1]) << np.uint64(1)) | stretch(q[:, 2])
+    return np.argsort(key, kind="stable").astype(np.uint32)
