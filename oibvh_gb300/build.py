@@ -72,7 +72,9 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
             if log.strip():
                 print(f"--- {os.path.basename(obj)}\n{log}", file=sys.stderr)
     tmp = LIB + f".{os.getpid()}.tmp"
-    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *[o for o, _ in results]]
+    # --no-undefined: a symbol missing from the library fails the build here,
+    # not the first load on a GPU host
+    cmd = [nvcc, *ARCH, "-shared", "-Xlinker", "--no-undefined", "-o", tmp, *[o for o, _ in results]]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
