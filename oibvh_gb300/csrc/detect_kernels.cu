@@ -425,15 +425,20 @@ __device__ __forceinline__ void store_candidates(const DetectArgs& a, const uint
 }
 
 // The warp's buffered candidates: tested (fused narrow phase) or stored.
+// kFused: the narrow phase is compiled into the traversal kernel (tested
+// here); otherwise the candidates are stored, and the kernel carries no
+// triangle-test code (fewer registers, more warps per SM).
+template <bool kFused>
 __device__ __forceinline__ void flush_candidates(const DetectArgs& a, const uint64_t* buf, uint32_t count,
                                                  uint32_t lane)
 {
-    if (a.fuse_narrow) test_candidates(a, buf, count, lane);
+    if constexpr (kFused) test_candidates(a, buf, count, lane);
     else store_candidates(a, buf, count, lane);
 }
 
 // Queue one candidate per lane where `pred`; every 32 queued candidates are
 // tested (fused narrow phase) or stored (broad phase only) at once.
+template <bool kFused>
 __device__ __forceinline__ void push_candidate(const DetectArgs& a, WarpCands& wc, bool pred, uint64_t cval,
                                                uint32_t lane)
 {
@@ -444,7 +449,7 @@ __device__ __forceinline__ void push_candidate(const DetectArgs& a, WarpCands& w
     wc.n += __popc(mask);
     __syncwarp();
     if (wc.n >= 32) {
-        flush_candidates(a, wc.buf + wc.n - 32, 32, lane);
+        flush_candidates<kFused>(a, wc.buf + wc.n - 32, 32, lane);
         wc.n -= 32;
         __syncwarp();
     }
@@ -457,6 +462,7 @@ __device__ __forceinline__ void push_candidate(const DetectArgs& a, WarpCands& w
 // (one shared atomic per warp); what does not fit goes to the spill list
 // of the next round.
 // Returns the number of child pairs tested (lane 0 only, else 0).
+template <bool kFused>
 __device__ __forceinline__ uint32_t expand_pair(const DetectArgs& a, WarpCands& wc, bool valid, uint64_t node,
                                                 uint64_t* next, uint32_t* next_cnt, uint32_t next_cap,
                                                 uint64_t* __restrict__ spill, uint32_t* spill_cnt, uint32_t lane)
@@ -501,7 +507,7 @@ __device__ __forceinline__ uint32_t expand_pair(const DetectArgs& a, WarpCands& 
             cm &= cm - 1;
             c = bvtt_pack(pair, leaf_a + (k >> 1), leaf_b + (k & 1));
         }
-        push_candidate(a, wc, pred, c, lane);
+        push_candidate<kFused>(a, wc, pred, c, lane);
     }
     // the overlapping internal pairs: reserve slots for the whole warp at once
     const uint32_t cnt = leaves ? 0u : (uint32_t)__popc(m);
@@ -545,6 +551,7 @@ __device__ __forceinline__ uint32_t expand_pair(const DetectArgs& a, WarpCands& 
 // reference's Scene::expandBvttNodes cross product, src/cuda/scene.cu:192-223)
 // is tested here; overlapping internal pairs go to work list 0, overlapping
 // leaf pairs straight to the candidates.
+template <bool kFused>
 __global__ void __launch_bounds__(kDetectThreads) k_init_front(DetectArgs a, uint32_t total0)
 {
     __shared__ uint64_t s_cand[kDetectThreads / 32][kCandBuf];
@@ -574,7 +581,7 @@ __global__ void __launch_bounds__(kDetectThreads) k_init_front(DetectArgs a, uin
             node = bvtt_pack(lo, ia, ib);
             cval = bvtt_pack(lo, x, y);
         }
-        push_candidate(a, wc, leafpair, cval, lane);
+        push_candidate<kFused>(a, wc, leafpair, cval, lane);
         const bool push = ov && !leafpair;
         const uint32_t pos = warp_append(a.counts + kCountWork0, push, lane);
         if (push) {
@@ -584,7 +591,7 @@ __global__ void __launch_bounds__(kDetectThreads) k_init_front(DetectArgs a, uin
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.counts + kCountTested, total0);
     flush_found(a, wc, lane);
-    if (wc.n > 0) flush_candidates(a, wc.buf, wc.n, lane);
+    if (wc.n > 0) flush_candidates<kFused>(a, wc.buf, wc.n, lane);
 }
 
 // The narrow top of the traversal: ONE CTA of kTopThreads walks the start
@@ -593,6 +600,7 @@ __global__ void __launch_bounds__(kDetectThreads) k_init_front(DetectArgs a, uin
 // the next work list. The first levels hold a few hundred pairs at most, so
 // one CTA covers them with one round of loads per level and no grid-wide
 // synchronisation.
+template <bool kFused>
 __global__ void __launch_bounds__(kTopThreads) k_top(DetectArgs a)
 {
     extern __shared__ uint64_t s_dyn[];  // two front buffers of kTopCap
@@ -631,7 +639,7 @@ __global__ void __launch_bounds__(kTopThreads) k_top(DetectArgs a)
             const bool valid = i < c;
             const uint64_t node = valid ? fc[i] : 0ull;
             // what outgrows the buffer goes to the walkers' list directly
-            tested += expand_pair(a, wc, valid, node, fn, &s_cnt[cur ^ 1], kTopCap, out, out_cnt, lane);
+            tested += expand_pair<kFused>(a, wc, valid, node, fn, &s_cnt[cur ^ 1], kTopCap, out, out_cnt, lane);
         }
         __syncthreads();
         c = min(s_cnt[cur ^ 1], kTopCap);
@@ -639,7 +647,7 @@ __global__ void __launch_bounds__(kTopThreads) k_top(DetectArgs a)
     }
     if (lane == 0 && tested) atomicAdd(a.counts + kCountTested, tested);
     flush_found(a, wc, lane);
-    if (wc.n > 0) flush_candidates(a, wc.buf, wc.n, lane);
+    if (wc.n > 0) flush_candidates<kFused>(a, wc.buf, wc.n, lane);
 }
 
 // The wide bottom of the traversal, round `round` (>= 1): every warp takes
@@ -648,6 +656,7 @@ __global__ void __launch_bounds__(kTopThreads) k_top(DetectArgs a)
 // walks them to the leaves level by level with a private front in shared
 // memory: warps never wait for each other. A warp whose front outgrows its
 // buffer spills the excess to the next round's list.
+template <bool kFused>
 __global__ void __launch_bounds__(kDetectThreads) k_walk(DetectArgs a, uint32_t round)
 {
     extern __shared__ uint64_t s_front[];  // [warp][2][cap]
@@ -683,7 +692,7 @@ __global__ void __launch_bounds__(kDetectThreads) k_walk(DetectArgs a, uint32_t 
                 const uint32_t i = base + lane;
                 const bool valid = i < c;
                 const uint64_t node = valid ? fc[i] : 0ull;
-                tested += expand_pair(a, wc, valid, node, fn, &cnt[cur ^ 1], cap, spill, spill_cnt, lane);
+                tested += expand_pair<kFused>(a, wc, valid, node, fn, &cnt[cur ^ 1], cap, spill, spill_cnt, lane);
             }
             __syncwarp();
             c = min(cnt[cur ^ 1], cap);
@@ -692,7 +701,7 @@ __global__ void __launch_bounds__(kDetectThreads) k_walk(DetectArgs a, uint32_t 
     }
     if (lane == 0 && tested) atomicAdd(a.counts + kCountTested, tested);
     flush_found(a, wc, lane);
-    if (wc.n > 0) flush_candidates(a, wc.buf, wc.n, lane);
+    if (wc.n > 0) flush_candidates<kFused>(a, wc.buf, wc.n, lane);
 }
 
 // Narrow phase over stored candidates (the split broad/narrow API):
@@ -925,7 +934,8 @@ cudaError_t launch_init_front(const DetectArgs& a, uint32_t total0, cudaStream_t
     if (blocks > (uint32_t)a.grid) blocks = (uint32_t)a.grid;
     if (blocks == 0) blocks = 1;
     note_launches(1);
-    k_init_front<<<blocks, kDetectThreads, 0, s>>>(a, total0);
+    if (a.fuse_narrow) k_init_front<true><<<blocks, kDetectThreads, 0, s>>>(a, total0);
+    else k_init_front<false><<<blocks, kDetectThreads, 0, s>>>(a, total0);
     return cudaGetLastError();
 }
 
@@ -937,12 +947,14 @@ cudaError_t launch_top(const DetectArgs& a, cudaStream_t s)
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64 || !configured[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(k_top, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaError_t e = cudaFuncSetAttribute(k_top<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_top<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
         if (dev >= 0 && dev < 64) configured[dev] = true;
     }
     note_launches(1);
-    k_top<<<1, kTopThreads, smem, s>>>(a);
+    if (a.fuse_narrow) k_top<true><<<1, kTopThreads, smem, s>>>(a);
+    else k_top<false><<<1, kTopThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -954,8 +966,10 @@ static cudaError_t walk_configure()
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev >= 0 && dev < 64 && configured[dev]) return cudaSuccess;
-    const cudaError_t e =
-        cudaFuncSetAttribute(k_walk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)walk_smem(kWalkCapMax));
+    cudaError_t e =
+        cudaFuncSetAttribute(k_walk<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)walk_smem(kWalkCapMax));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_walk<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)walk_smem(kWalkCapMax));
     if (e == cudaSuccess && dev >= 0 && dev < 64) configured[dev] = true;
     return e;
 }
@@ -967,16 +981,19 @@ cudaError_t launch_walk(const DetectArgs& a, uint32_t round, cudaStream_t s)
     cudaError_t e = walk_configure();
     if (e != cudaSuccess) return e;
     note_launches(1);
-    k_walk<<<a.grid, kDetectThreads, walk_smem(a.walk_cap), s>>>(a, round);
+    if (a.fuse_narrow) k_walk<true><<<a.grid, kDetectThreads, walk_smem(a.walk_cap), s>>>(a, round);
+    else k_walk<false><<<a.grid, kDetectThreads, walk_smem(a.walk_cap), s>>>(a, round);
     return cudaGetLastError();
 }
 
-int walk_blocks_per_sm(uint32_t walk_cap)
+int walk_blocks_per_sm(uint32_t walk_cap, bool fused)
 {
     if (walk_configure() != cudaSuccess) return 1;
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_walk, kDetectThreads, walk_smem(walk_cap)) != cudaSuccess)
-        return 1;
+    const cudaError_t e =
+        fused ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_walk<true>, kDetectThreads, walk_smem(walk_cap))
+              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_walk<false>, kDetectThreads, walk_smem(walk_cap));
+    if (e != cudaSuccess) return 1;
     return n > 0 ? n : 1;
 }
 

@@ -282,9 +282,9 @@ int upload_views(oibvh_scene_s* s, cudaStream_t st)
     return OIBVH_OK;
 }
 
-int walk_grid(const oibvh_scene_s* s)
+int walk_grid(const oibvh_scene_s* s, bool fused = true)
 {
-    const int fit = walk_blocks_per_sm(s->tune_walk_cap);
+    const int fit = walk_blocks_per_sm(s->tune_walk_cap, fused);
     const int per = s->tune_walk_per_sm ? std::min<int>(fit, (int)s->tune_walk_per_sm) : fit;
     return sm_count(s->device) * std::max(1, per);
 }
@@ -338,7 +338,7 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
     OK_TRY(upload_views(s, st));
     OK_TRY(s->hits.ensure(s->hit_cap, "cudaMalloc(hits)"));
 
-    const int grid = walk_grid(s);
+    const int grid = walk_grid(s, narrow);
     for (uint32_t p0 = 0; p0 < n_pairs; p0 += kMaxPairsPerPass) {
         const uint32_t np = std::min(kMaxPairsPerPass, n_pairs - p0);
         PassPlan plan;
@@ -1256,7 +1256,7 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
     a.fuse_narrow = s->precision ? 0u : 1u;
     a.cand = s->precision ? s->cand.p : nullptr;
     a.cand_cap = s->precision ? s->cand_cap : 0u;
-    a.grid = walk_grid(s);
+    a.grid = walk_grid(s, !s->precision);
     a.handoff = s->tune_handoff;
     a.walk_cap = s->tune_walk_cap;
     a.precision = s->precision;

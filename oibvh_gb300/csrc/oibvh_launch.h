@@ -92,8 +92,9 @@ struct DetectArgs {
 cudaError_t launch_init_front(const DetectArgs& a, uint32_t total0, cudaStream_t s);
 cudaError_t launch_top(const DetectArgs& a, cudaStream_t s);
 cudaError_t launch_walk(const DetectArgs& a, uint32_t round, cudaStream_t s);
-// walker CTAs that fit on one SM with fronts of `walk_cap` entries (0: default)
-int walk_blocks_per_sm(uint32_t walk_cap = 0);
+// walker CTAs that fit on one SM with fronts of `walk_cap` entries (0:
+// default), for the fused (narrow phase inside) or the broad-only walker
+int walk_blocks_per_sm(uint32_t walk_cap = 0, bool fused = true);
 cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s);
 
 // counts[]: hits, flags, candidates found, candidate slots used (broad-only),
