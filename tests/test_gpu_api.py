@@ -197,3 +197,59 @@ def test_obj_meshes_through_the_pipeline(gpu, tmp_path):
     want, _ = port.detect()
     assert np.array_equal(sc.int_tri_pairs(), sort_pairs(want))
     assert want.shape[0] > 0
+
+
+def test_empty_and_single_tree_scenes(gpu):
+    """A scene with no trees, or one tree (no pair), detects nothing, and an
+    explicit empty pair list detects nothing either."""
+    import numpy as np
+
+    from oibvh_gb300 import DeviceType, OibvhTree, Scene
+    from oibvh_gb300 import meshes as M
+
+    sc = Scene()
+    sc.detectCollision(DeviceType.GPU0, 0, 1)
+    assert sc.getIntTriPairCount() == 0
+    t = OibvhTree(M.icosphere(2))
+    t.build()
+    sc.addOibvhTree(t)
+    sc.detectCollision(DeviceType.GPU0, 4, 3)
+    assert sc.getIntTriPairCount() == 0 and sc.int_tri_pairs().shape == (0, 4)
+    u = OibvhTree(M.icosphere(2, 1.0, (0.5, 0.0, 0.0)))
+    u.build()
+    sc.addOibvhTree(u)
+    sc.set_pairs(np.zeros((0, 2), dtype=np.uint32))
+    sc.detectCollision(DeviceType.GPU0, 0, 1)
+    assert sc.getIntTriPairCount() == 0
+
+
+def test_maximum_tree_size(gpu):
+    """2^23 triangles, the largest mesh a tree takes (24-bit node indices in
+    the BVTT records), against a small sphere crossing it: the oracle's pair
+    set; one more triangle is refused."""
+    import numpy as np
+
+    from oibvh_gb300 import DeviceType, OibvhError, OibvhTree, Scene
+    from oibvh_gb300 import meshes as M
+    from oracle.oracle import Port, sort_pairs
+
+    sheet = M.grid_sheet(2048, 2.0, 0.0, 1.0, origin=(-1.0, -1.0, 0.0))
+    assert sheet.n_triangles == 1 << 23
+    ball = M.icosphere(3, 0.3, (0.1, -0.2, 0.05))
+    trees = [OibvhTree(sheet), OibvhTree(ball)]
+    sc = Scene()
+    for t in trees:
+        t.build()
+        sc.addOibvhTree(t)
+    assert trees[0].getPrimCount() == 1 << 23
+    sc.detectCollision(DeviceType.GPU0, 4, 3)
+    port = Port()
+    port.add_mesh(sheet.xyz, sheet.tri)
+    port.add_mesh(ball.xyz, ball.tri)
+    want, wc = port.detect()
+    assert want.shape[0] > 0
+    assert np.array_equal(sc.int_tri_pairs(), sort_pairs(want))
+    assert sc.candidate_count() == wc
+    big = M.Mesh(np.zeros((3, 3), np.float32), np.zeros(((1 << 23) + 1, 3), np.uint32))
+    with pytest.raises(OibvhError):
+        OibvhTree(big)
