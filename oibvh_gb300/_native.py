@@ -75,6 +75,7 @@ class Tuning(ctypes.Structure):
         ("front_capacity", ctypes.c_uint32),
         ("hit_capacity", ctypes.c_uint32),
         ("walk_front", ctypes.c_uint32),
+        ("refit_group_log2", ctypes.c_uint32),
     ]
 
 

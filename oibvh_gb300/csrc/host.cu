@@ -164,6 +164,7 @@ struct oibvh_scene_s {
     uint32_t precision = 0;         // OIBVH_PRECISION_*
     uint32_t tune_walk_per_sm = 0;  // walker CTAs per SM, 0 = as many as fit
     uint32_t tune_walk_cap = 128;   // per-warp front entries of the walkers
+    uint32_t tune_refit_log = 10;   // refit level-group depth (levels per CTA: 9, 10 or 11)
 
     // captured frame (CUDA graph): [transform] + refit + detect
     cudaGraphExec_t frame_exec = nullptr;
@@ -825,6 +826,7 @@ API int oibvh_scene_refit(oibvh_scene_t s, void* stream)
         const oibvh_tree_t t = s->trees[i];
         if (!t->built) return fail(OIBVH_ERR_STATE, "every tree must be built before refit");
         RefitJob j = t->job();
+        j.n_blocks = refit_blocks_for(t->nT, s->tune_refit_log);
         j.block_begin = blocks;
         j.counters = nullptr;  // filled below
         blocks += j.n_blocks;
@@ -853,7 +855,7 @@ API int oibvh_scene_refit(oibvh_scene_t s, void* stream)
     }
     s->refit_blocks = blocks;
     CUDA_TRY(launch_refit(s->refit_jobs.p, (uint32_t)n, blocks, s->refit_block_job.p, s->refit_counters.p, per * n,
-                          st));
+                          s->tune_refit_log, st));
     return OIBVH_OK;
     GUARD_END
 }
@@ -1090,6 +1092,9 @@ API int oibvh_scene_set_tuning(oibvh_scene_t s, const oibvh_tuning* t)
     if (t->walk_front && (t->walk_front % 32 || t->walk_front > 512))
         return fail(OIBVH_ERR_ARG, "walk_front: a multiple of 32 up to 512 (0 keeps the value)");
     if (t->walk_front) s->tune_walk_cap = t->walk_front;
+    if (t->refit_group_log2 && (t->refit_group_log2 < 9 || t->refit_group_log2 > 11))
+        return fail(OIBVH_ERR_ARG, "refit_group_log2: 9, 10 or 11 (0 keeps the value)");
+    if (t->refit_group_log2) s->tune_refit_log = t->refit_group_log2;
     s->tune_start_log2 = t->start_pairs_log2;
     s->tune_handoff = t->handoff;
     s->tune_walk_per_sm = t->walk_blocks_per_sm;
@@ -1106,6 +1111,7 @@ API int oibvh_scene_get_tuning(oibvh_scene_t s, oibvh_tuning* t)
     t->handoff = s->tune_handoff;
     t->walk_blocks_per_sm = s->tune_walk_per_sm;
     t->walk_front = s->tune_walk_cap;
+    t->refit_group_log2 = s->tune_refit_log;
     t->front_capacity = s->front_cap;
     t->hit_capacity = s->hit_cap;
     return OIBVH_OK;
@@ -1141,6 +1147,29 @@ API int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t rep
         ms_out = tot;
         return st == OIBVH_OK;
     };
+    // the refit's level-group depth: the scene refit timed alone
+    uint32_t b_group = s->tune_refit_log;
+    {
+        float best_refit = 1e30f;
+        for (uint32_t gl : {9u, 10u, 11u}) {
+            s->tune_refit_log = gl;
+            st = oibvh_scene_refit(s, 0);  // warm-up (uploads the job table)
+            float tot = 0.0f;
+            for (uint32_t r = 0; r < reps && st == OIBVH_OK; ++r) {
+                cudaEventRecord(e0, 0);
+                st = oibvh_scene_refit(s, 0);
+                cudaEventRecord(e1, 0);
+                cudaEventSynchronize(e1);
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                tot += ms;
+            }
+            if (st != OIBVH_OK) break;
+            if (tot < best_refit) best_refit = tot, b_group = gl;
+        }
+        s->tune_refit_log = b_group;
+        if (st == OIBVH_OK) st = oibvh_scene_refit(s, 0);
+    }
     float best = 1e30f;
     uint32_t b_start = s->tune_start_log2, b_handoff = s->tune_handoff, b_cap = 128, b_per = 0;
     s->tune_walk_cap = 128;
@@ -1179,6 +1208,7 @@ API int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t rep
     bt.handoff = b_handoff;
     bt.walk_blocks_per_sm = b_per ? b_per : (uint32_t)fit;
     bt.walk_front = b_cap;
+    bt.refit_group_log2 = b_group;
     // capacities: the largest work list and hit count seen, doubled
     st = detect_impl(s, s->device, entry_level, 1, full_detect_mode(s), 0);
     if (st != OIBVH_OK) return st;
@@ -1276,7 +1306,7 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
     }
     if (s->frame_refit && e == cudaSuccess) {
         e = launch_refit(s->refit_jobs.p, (uint32_t)s->trees.size(), s->refit_blocks, s->refit_block_job.p,
-                         s->refit_counters.p, refit_counters_per_tree() * s->trees.size(), st);
+                         s->refit_counters.p, refit_counters_per_tree() * s->trees.size(), s->tune_refit_log, st);
         ++kernels;
     }
     if (e == cudaSuccess) e = cudaMemsetAsync(s->counts.p, 0, kCountTotal * sizeof(uint32_t), st);

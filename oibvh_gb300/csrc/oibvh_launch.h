@@ -61,14 +61,16 @@ cudaError_t launch_gather_u32(const uint32_t* src, const uint32_t* idx, uint32_t
 cudaError_t launch_gather_faces(const uint32_t* tri, const uint32_t* perm, uint32_t nT, uint4* out, cudaStream_t s);
 
 // refit_kernels.cu
-uint32_t refit_blocks_for(uint32_t nT);
+// refit CTAs of a tree of nT leaves with level groups of group_log2 levels
+// (9, 10 or 11; 0 = 10, the single-tree refit's)
+uint32_t refit_blocks_for(uint32_t nT, uint32_t group_log2 = 0);
 uint32_t refit_counters_per_tree();
 cudaError_t launch_refit_one(const RefitJob& job, cudaStream_t s);
 cudaError_t launch_leaf_boxes(const uint4* face, const float4* pos, uint32_t nT, float4* out, cudaStream_t s);
 // block_job: optional host-built map from a refit CTA to its job (nullptr:
 // each CTA binary-searches the job table).
 cudaError_t launch_refit(const RefitJob* d_jobs, uint32_t n_jobs, uint32_t total_blocks, const uint32_t* block_job,
-                         uint32_t* d_counters, size_t n_counters, cudaStream_t s);
+                         uint32_t* d_counters, size_t n_counters, uint32_t group_log2, cudaStream_t s);
 
 // detect_kernels.cu
 struct DetectArgs {

@@ -24,11 +24,10 @@
 
 namespace oibvh {
 
-constexpr int kRefitThreads = 256;
-constexpr int kRefitLog = 10;
-constexpr int kRefitChunk = 1 << kRefitLog;  // leaves per CTA, and nodes per climbing group
-constexpr int kStageCounters = 16;           // counters per climbing stage and tree
-static_assert(kRefitThreads * 4 == kRefitChunk, "four nodes per thread");
+// Level groups: a CTA reduces 2^kLog nodes by kLog levels (four nodes per
+// thread), kLog = 9, 10 (default) or 11; the group depth is a tuning knob.
+constexpr uint32_t kRefitLogDefault = 10;
+constexpr int kStageCounters = 64;  // counters per climbing stage and tree (groups of the widest stage, kLog 9)
 
 __device__ __forceinline__ Box shfl_down(const Box& b, int d)
 {
@@ -50,10 +49,11 @@ __device__ __forceinline__ Box load_node_cg(const float4* box, uint32_t real)
     return Box{a.x, a.y, a.z, c.x, c.y, c.z};
 }
 
-// Reduce the 1024-node block whose four nodes per thread are v[0..3] (level
-// `lvl`, global indices base + 4*tid + k, real when < level_count(lvl)) by
-// `levels` levels, writing each produced node. Thread 0 ends holding the
+// Reduce the 2^kLog-node block whose four nodes per thread are v[0..3]
+// (level `lvl`, global indices base + 4*tid + k, real when < level_count(lvl))
+// by `levels` levels, writing each produced node. Thread 0 ends holding the
 // block root (level lvl - levels, index base >> levels).
+template <int kLog>
 __device__ __forceinline__ void reduce_block(Box v[4], const TreeShape& S, float4* box, uint32_t lvl, uint32_t base,
                                              uint32_t levels, Box* sm8)
 {
@@ -100,19 +100,20 @@ __device__ __forceinline__ void reduce_block(Box v[4], const TreeShape& S, float
             ++done;
         }
     }
-    // three levels across the CTA: the 8 warp roots
+    // the last kLog - 7 levels across the CTA: one root per warp
+    constexpr int kWarpLog = kLog - 7, kWarps = 1 << kWarpLog;
     if (done < levels) {
         if (lane == 0) sm8[warp] = v[0];
         __syncthreads();
         if (warp == 0) {
-            if (lane < 8) v[0] = sm8[lane];
+            if (lane < kWarps) v[0] = sm8[lane];
             const uint32_t b0 = base >> 7;  // index of warp 0's root
 #pragma unroll
-            for (int s = 0; s < 3; ++s) {
+            for (int s = 0; s < kWarpLog; ++s) {
                 if (done < levels) {
                     const Box r = shfl_down(v[0], 1 << s);
                     const uint32_t j = (b0 + lane) >> s;
-                    if (lane < 8 && (lane & ((2u << s) - 1u)) == 0) {
+                    if (lane < kWarps && (lane & ((2u << s) - 1u)) == 0) {
                         if (j + 1 < cnt) v[0] = merge(v[0], r);
                         if (j < cnt) store_node(box, S.level_offset(lvl - 1) + (j >> 1), v[0]);
                     }
@@ -126,10 +127,13 @@ __device__ __forceinline__ void reduce_block(Box v[4], const TreeShape& S, float
 }
 
 // `jobs` == nullptr: a single tree passed by value in `one`.
-__global__ void __launch_bounds__(kRefitThreads, 5) k_refit(const RefitJob* __restrict__ jobs, uint32_t n_jobs,
-                                                         const uint32_t* __restrict__ block_job, const RefitJob one)
+template <int kLog>
+__global__ void __launch_bounds__((1 << kLog) / 4, 1280 / ((1 << kLog) / 4))
+    k_refit(const RefitJob* __restrict__ jobs, uint32_t n_jobs, const uint32_t* __restrict__ block_job,
+            const RefitJob one)
 {
-    __shared__ Box sm8[8];
+    constexpr uint32_t kRefitLog = kLog, kRefitChunk = 1u << kLog;
+    __shared__ Box sm8[(1 << kLog) / 128];
     __shared__ uint32_t s_last;
 
     RefitJob job = one;
@@ -158,7 +162,7 @@ __global__ void __launch_bounds__(kRefitThreads, 5) k_refit(const RefitJob* __re
     for (int k = 0; k < 4; ++k) v[k] = leaf_box(job.pos, f[k]);
 
     uint32_t levels = min((uint32_t)kRefitLog, S.L);
-    reduce_block(v, S, job.box, S.L, chunk << kRefitLog, levels, sm8);
+    reduce_block<kLog>(v, S, job.box, S.L, chunk << kRefitLog, levels, sm8);
     uint32_t lvl = S.L - levels;
     if (lvl == 0) return;
 
@@ -166,7 +170,7 @@ __global__ void __launch_bounds__(kRefitThreads, 5) k_refit(const RefitJob* __re
     uint32_t idx = chunk;
     for (int stage = 0;; ++stage) {
         const uint32_t g = idx >> kRefitLog;
-        const uint32_t gcnt = min((uint32_t)kRefitChunk, S.level_count(lvl) - (g << kRefitLog));
+        const uint32_t gcnt = min(kRefitChunk, S.level_count(lvl) - (g << kRefitLog));
         if (threadIdx.x == 0) {
             __threadfence();
             const uint32_t old = atomicAdd(job.counters + stage * kStageCounters + g, 1u);
@@ -184,7 +188,7 @@ __global__ void __launch_bounds__(kRefitThreads, 5) k_refit(const RefitJob* __re
             v[k] = (j < cnt) ? load_node_cg(job.box, off + j) : Box{0, 0, 0, 0, 0, 0};
         }
         levels = min((uint32_t)kRefitLog, lvl);
-        reduce_block(v, S, job.box, lvl, base, levels, sm8);
+        reduce_block<kLog>(v, S, job.box, lvl, base, levels, sm8);
         lvl -= levels;
         if (lvl == 0) return;
         idx = g;
@@ -203,28 +207,49 @@ __global__ void __launch_bounds__(256) k_leaf_boxes(const uint4* __restrict__ fa
     out[2 * (size_t)i + 1] = make_float4(b.xx, b.xy, b.xz, 0.0f);
 }
 
-uint32_t refit_blocks_for(uint32_t nT) { return (nT + kRefitChunk - 1) / kRefitChunk; }
+uint32_t refit_blocks_for(uint32_t nT, uint32_t group_log2)
+{
+    const uint32_t g = group_log2 ? group_log2 : kRefitLogDefault;
+    return (nT + (1u << g) - 1) >> g;
+}
 uint32_t refit_counters_per_tree() { return 4 * kStageCounters; }
+
+template <int kLog>
+static void refit_launch(uint32_t blocks, const RefitJob* jobs, uint32_t n_jobs, const uint32_t* block_job,
+                         const RefitJob& one, cudaStream_t s)
+{
+    k_refit<kLog><<<blocks, (1 << kLog) / 4, 0, s>>>(jobs, n_jobs, block_job, one);
+}
+
+static cudaError_t refit_dispatch(uint32_t group_log2, uint32_t blocks, const RefitJob* jobs, uint32_t n_jobs,
+                                  const uint32_t* block_job, const RefitJob& one, cudaStream_t s)
+{
+    switch (group_log2 ? group_log2 : kRefitLogDefault) {
+    case 9: refit_launch<9>(blocks, jobs, n_jobs, block_job, one, s); break;
+    case 10: refit_launch<10>(blocks, jobs, n_jobs, block_job, one, s); break;
+    case 11: refit_launch<11>(blocks, jobs, n_jobs, block_job, one, s); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
 
 cudaError_t launch_refit_one(const RefitJob& job, cudaStream_t s)
 {
     cudaError_t e = cudaMemsetAsync(job.counters, 0, refit_counters_per_tree() * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     note_launches(1);
-    k_refit<<<job.n_blocks, kRefitThreads, 0, s>>>(nullptr, 1, nullptr, job);
-    return cudaGetLastError();
+    return refit_dispatch(kRefitLogDefault, job.n_blocks, nullptr, 1, nullptr, job, s);
 }
 
 cudaError_t launch_refit(const RefitJob* d_jobs, uint32_t n_jobs, uint32_t total_blocks, const uint32_t* block_job,
-                         uint32_t* d_counters, size_t n_counters, cudaStream_t s)
+                         uint32_t* d_counters, size_t n_counters, uint32_t group_log2, cudaStream_t s)
 {
     if (n_jobs == 0 || total_blocks == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(d_counters, 0, n_counters * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     RefitJob none{};
     note_launches(1);
-    k_refit<<<total_blocks, kRefitThreads, 0, s>>>(d_jobs, n_jobs, block_job, none);
-    return cudaGetLastError();
+    return refit_dispatch(group_log2, total_blocks, d_jobs, n_jobs, block_job, none, s);
 }
 
 cudaError_t launch_leaf_boxes(const uint4* face, const float4* xyz, uint32_t nT, float4* out, cudaStream_t s)

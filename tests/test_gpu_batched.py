@@ -141,3 +141,34 @@ def test_walker_front_capacity_keeps_the_pair_set(gpu):
         assert sc.candidate_count() == wc
     with pytest.raises(OibvhError):
         sc.set_tuning(walk_front=48)
+
+
+def test_refit_level_group_depths_agree(gpu):
+    """The scene refit with level groups of 9, 10 and 11 levels per CTA (two
+    climbing stages for the deep tree) writes the oracle's boxes bit for bit."""
+    import torch
+
+    from oibvh_gb300 import OibvhTree, Scene
+    from oibvh_gb300 import workloads as W
+
+    meshes = [W.noise_displace_mesh(7, 0.05, 3), W.noise_displace_mesh(2, 0.05, 4),
+              W.noise_displace_mesh(5, 0.05, 5)]
+    trees = [OibvhTree(m) for m in meshes]
+    sc = Scene()
+    for t in trees:
+        sc.addOibvhTree(t)
+    sc.build()
+    rest = torch.from_numpy(np.concatenate([np.pad(m.xyz, ((0, 0), (0, 1))) for m in meshes], 0)).cuda()
+    mats = torch.tensor([[0.6, -0.8, 0.0, 0.1, 0.8, 0.6, 0.0, -0.2, 0.0, 0.0, 1.0, 0.3]] * 3, dtype=torch.float32).cuda()
+    sc.transform(rest.data_ptr(), mats.data_ptr())
+    want = None
+    for gl in (9, 10, 11):
+        sc.set_tuning(refit_group_log2=gl)
+        assert sc.tuning()["refit_group_log2"] == gl
+        sc.refit()
+        got = [t.aabb_tree().view(np.uint32).copy() for t in trees]
+        if want is None:
+            pos = [W.rigid_apply(m.xyz, mats[0].cpu().numpy()) for m in meshes]
+            want = [Port.oibvh_refit(x, t.sorted_faces()[0]).view(np.uint32) for x, t in zip(pos, trees)]
+        for g, wv in zip(got, want):
+            assert np.array_equal(g, wv), gl
