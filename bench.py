@@ -52,7 +52,8 @@ REFIT_DRAM_BYTES_PER_TRIANGLE = (372.686592e6 + 445.836544e6) / 15520000
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: the config's frame count, 60 batched, 100 deforming, else 30)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["batched", "precision", "serving", "deforming", "plain"], default="batched")
@@ -62,7 +63,10 @@ def parse():
     ap.add_argument("--pairs", type=int, default=512, help="mesh pairs of the batched workload")
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.steps is None:
+        args.steps = {"batched": 60, "deforming": 100}.get(args.workload, 30)
+    return args
 
 
 def max_over_ranks(values, dist, device):
@@ -955,8 +959,16 @@ def run_ours_precision(args, rank, world, local):
     ms_e2e, lat_e2e, _, _, d2h = measure(_native.PRECISION_FP64_FILTERED, args.steps, e2e=True)
     clocks = sampler.stop() if sampler else None
     got_f = sc.int_tri_pairs() if not args.no_cpu_baseline else None
+    got_f_all = sc.int_tri_pairs() if got_f is None else got_f
     ms_32, lat_32, _, st_32, _ = measure(_native.PRECISION_FP32, max(3, args.steps // 2))
     hits32 = sc.getIntTriPairCount()
+    got_32 = sc.int_tri_pairs()
+    # float vs FP64 disagreements per pair: symmetric difference of the two pair sets
+    def keyed(recs, a_, b_):
+        r = recs[(recs[:, 0] == a_) & (recs[:, 1] == b_)]
+        return (r[:, 2].astype(np.int64) << 32) | r[:, 3].astype(np.int64)
+
+    per_pair = [int(np.setxor1d(keyed(got_f_all, a_, b_), keyed(got_32, a_, b_)).size) for a_, b_ in w.pairs]
 
     # the plain path: one pair per call (refit both trees + detect), each query alone
     plain = []
@@ -1003,7 +1015,9 @@ def run_ours_precision(args, rank, world, local):
                              "every query of a frame completes with it"},
         "fp64_filter": {"candidates": st_f["candidates"], "fp64_candidates": st_f["fp64_candidates"],
                         "fp64_axes": st_f["fp64_axes"], "fp32_disagreements": st_f["fp32_disagreements"],
-                        "hits_fp64": hits, "hits_fp32": hits32},
+                        "hits_fp64": hits, "hits_fp32": hits32,
+                        "fp32_vs_fp64_disagreements_per_pair": per_pair,
+                        "pairs_with_disagreements": sum(1 for x in per_pair if x)},
         "fp32_frame": {"queries_per_s": round(max(3, K // 2) * n_pairs / (ms_32 / 1e3), 1),
                        "ms_per_frame": round(ms_32 / max(3, K // 2), 4),
                        "latency_p99_ms": round(_pctl(lat_32, 99), 4)},
