@@ -185,8 +185,6 @@ struct oibvh_server_s {
     bool running = false, stop = false;
     std::thread worker;
     oibvh_server_stats stats{};
-    int fatal = OIBVH_OK;
-    std::string fatal_msg;
 
     ~oibvh_server_s();
     void loop();
