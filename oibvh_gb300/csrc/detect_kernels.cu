@@ -814,6 +814,7 @@ __device__ __forceinline__ EV3 axis_of(uint32_t k, const LaneTri& t)
     return esel(k == 0, t.n1, esel(k == 1, t.m1, ecross(X, Y)));
 }
 
+constexpr int kRefillBatch = 16;
 __constant__ uint8_t c_axis_order[17] = {0, 1, 11, 12, 13, 14, 15, 16, 2, 3, 4, 5, 6, 7, 8, 9, 10};
 
 __global__ void __launch_bounds__(kDetectThreads, 2) k_narrow_prec(DetectArgs a)
@@ -842,8 +843,11 @@ __global__ void __launch_bounds__(kDetectThreads, 2) k_narrow_prec(DetectArgs a)
         bool hit = false, queue = false;
         uint4 rec = make_uint4(0, 0, 0, 0);
         uint32_t mask = 0;
+        // a refill costs the warp three dependent loads (candidate, faces,
+        // vertices): refill only once kRefillBatch lanes are idle (or none is busy)
         const uint32_t idle = __ballot_sync(0xffffffffu, !busy);
-        const uint32_t take = min((uint32_t)__popc(idle), hi - next);
+        const bool refill = __popc(idle) >= kRefillBatch || idle == 0xffffffffu;
+        const uint32_t take = refill ? min((uint32_t)__popc(idle), hi - next) : 0u;
         const uint32_t rank = __popc(idle & ((1u << lane) - 1u));
         if (!busy && rank < take) {
             c = a.cand[next + rank];
