@@ -1194,9 +1194,13 @@ def run_ours_serving(args, rank, world, local):
     # warm-up stream (lane buffers grow to their working sizes)
     run_stream(30000.0, 6000, seed=99)
     sweep = []
+    launches0 = L.oibvh_get_launch_count()
     for i, rate in enumerate(rates):
         n = int(min(max(2000, rate * 0.4), 40000))
         sweep.append(run_stream(rate, n, seed=1000 + i))
+    sweep_launches = L.oibvh_get_launch_count() - launches0
+    sweep_queries = sum(r["queries"] for r in sweep)
+    sweep_pairs = sum(r["pairs"] for r in sweep)
     clocks = sampler.stop() if sampler else None
 
     # plain: the same kind of queries one at a time, each alone on the GPU
@@ -1233,8 +1237,11 @@ def run_ours_serving(args, rank, world, local):
         "served_over_plain": round(top["throughput_per_s"] / plain_qps, 2),
         "server_stats": st,
         "e2e": {"value": top["throughput_per_s"], "unit": "queries/s", "h2d_bytes_per_step": 48,
-                "d2h_bytes_per_step": None, "note": "every served query is end to end: host submit -> host pairs"},
-        "gpu_launches": None,
+                "d2h_bytes_per_step": round(16 * sweep_pairs / max(1, sweep_queries), 1),
+                "note": "every served query is end to end: host submit -> host pairs; a step is one query "
+                        "(48 B of transform in, its hit records out)"},
+        "gpu_launches": int(sweep_launches),
+        "gpu_launches_note": f"this library's kernels over the {sweep_queries} queries of the sweep",
         "clocks": clocks,
         "setup_s": round(setup_s, 2),
     }
