@@ -1,12 +1,15 @@
 // Build-time kernels: mesh bounds, leaf boxes + Morton codes, the stable
-// LSD radix sort of the codes, and the gather of Morton-ordered faces.
+// LSD radix sort of the codes, and the gather of Morton-ordered faces; the
+// same stages for any number of trees in one launch each (scene builds);
+// and the rigid transform of every tree's vertices in one launch.
 //
 // Reference: src/cuda/oibvh.cu:6-70 (strech_by_3, morton3D,
 // calculate_aabb_and_morton_kernel) and src/cuda/oibvhTree.cu:253-299
 // (mesh bounds from Mesh::m_aabb, two thrust::stable_sort_by_key calls).
 // Here one stable sort of (code, face index) replaces the two payload sorts
 // and the permutation is kept, so faces are gathered once into a 16-byte
-// record (v0, v1, v2, original index).
+// record (v0, v1, v2, original index). Keys are the reference's 30 bits, or
+// 63 bits (21 per axis) as an option, sorted as two stable 32-bit passes.
 #include "oibvh_common.cuh"
 #include "oibvh_launch.h"
 

@@ -10,14 +10,19 @@
 // the node pairs at a start level and lists the overlapping ones; k_top (one
 // CTA) walks the narrow top levels until the front is wide; in k_walk every
 // warp takes an interleaved share of that front and walks it to the leaves
-// with a private front in shared memory, so no grid-wide synchronisation is
-// needed. The host enqueues everything and reads the counters back once.
-// Appends (next front, candidates, hits) are warp-aggregated: one atomicAdd
-// per warp, positions from ballot/shuffle prefix sums. The narrow phase is
-// fused: overlapping leaf pairs are buffered per warp in shared memory and
-// tested 32 at a time.
+// with a private front in shared memory (its capacity a tuning parameter);
+// what outgrows it spills to the next round's list, so no grid-wide
+// synchronisation is needed. The host enqueues the rounds and reads the
+// counters back once. Appends (next front, spills, hits) are warp-aggregated:
+// one atomic per warp, positions from ballot/shuffle prefix sums.
 //
-// The triangle test reproduces the reference's CPU arithmetic
+// Narrow phase: overlapping leaf pairs are buffered per warp in shared memory
+// and, 32 at a time, tested inside the traversal (the kernels' <true>
+// instantiation, the float test) or stored for a separate kernel (<false>,
+// fewer registers): k_narrow (float test, split API) or k_narrow_prec
+// (precision mode: the FP64-filtered test).
+//
+// The float triangle test reproduces the reference's CPU arithmetic
 // (src/utils/utils.cpp:71-169, glm scalar dot/cross): every product, sum and
 // difference is rounded on its own (__fmul_rn/__fadd_rn/__fsub_rn, never
 // contracted to FMA), so the GPU pair set is the CPU pair set bit for bit.

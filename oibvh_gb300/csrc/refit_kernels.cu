@@ -5,15 +5,16 @@
 // (src/cuda/oibvhTree.cu:193-235,338-357) after calculate_aabb_kernel
 // (src/cuda/oibvh.cu:24-40). Here one kernel does all of it, for any number
 // of trees at once:
-//   * a CTA of 256 threads owns 1024 consecutive Morton-ordered leaves, four
+//   * a CTA owns 2^g consecutive Morton-ordered leaves (a level group of g
+//     levels, g = 9, 10 or 11, chosen by the tuning; 2^g / 4 threads), four
 //     per thread: it loads the four 16-byte face records and the twelve
 //     vertices with independent loads, builds the leaf boxes in registers,
 //     reduces two levels inside the thread, five across the warp (shuffles)
-//     and three across the CTA (eight boxes through shared memory), writing
-//     every internal node it produces;
-//   * the CTA finishing last among a group of 1024 sibling subtree roots
-//     (one atomic counter per group, threadfence-reduction pattern) loads
-//     the group and climbs the next 10 levels the same way, up to the root.
+//     and g - 7 across the CTA (one box per warp through shared memory),
+//     writing every internal node it produces;
+//   * the CTA finishing last among a group of 2^g sibling subtree roots (one
+//     atomic counter per group, threadfence-reduction pattern) loads the
+//     group and climbs the next g levels the same way, up to the root.
 // No CTA waits for another (no spin loop).
 //
 // Leaf boxes are not stored: a leaf's box is min/max of its three vertices
