@@ -59,3 +59,34 @@ def test_argument_errors_need_no_gpu():
     assert L.oibvh_tree_create(f32(xyz), 3, u32(tri), 1, 0, None) == N.ERR_ARG
     assert L.oibvh_scene_detect(None, 0, 0, 1, None) == N.ERR_ARG
     assert L.oibvh_status_string(N.ERR_OVERFLOW) == b"queue overflow"
+
+
+def test_extension_argument_errors_need_no_gpu():
+    """Serving, precision, tuning and Morton-width entry points reject bad
+    arguments before any CUDA call."""
+    from oibvh_gb300 import _native as N
+
+    L = N.lib()
+    h = ctypes.c_void_p()
+    # server: null out, a budget under 1 MiB, no batch, no lane, too many lanes
+    assert L.oibvh_server_create(0, 1 << 30, 64, 4, None) == N.ERR_ARG
+    assert L.oibvh_server_create(0, 1 << 10, 64, 4, ctypes.byref(h)) == N.ERR_ARG
+    assert L.oibvh_server_create(0, 1 << 30, 0, 4, ctypes.byref(h)) == N.ERR_ARG
+    assert L.oibvh_server_create(0, 1 << 30, 64, 0, ctypes.byref(h)) == N.ERR_ARG
+    assert L.oibvh_server_create(0, 1 << 30, 64, 17, ctypes.byref(h)) == N.ERR_ARG
+    mat = np.eye(3, 4, dtype=np.float32)
+    t = ctypes.c_uint64()
+    assert L.oibvh_server_submit(None, 0, 1, mat.ctypes.data_as(N._f32p), ctypes.byref(t)) == N.ERR_ARG
+    assert L.oibvh_server_wait(None, 1, 10, None) == N.ERR_ARG
+    assert L.oibvh_server_release(None, 1) == N.ERR_ARG
+    assert L.oibvh_server_destroy(None) == N.OK
+    # scene-level knobs on a null scene
+    assert L.oibvh_scene_set_precision(None, 1) == N.ERR_ARG
+    assert L.oibvh_scene_get_precision(None) == -1
+    assert L.oibvh_scene_set_tuning(None, None) == N.ERR_ARG
+    assert L.oibvh_scene_autotune(None, 0, 1, None) == N.ERR_ARG
+    assert L.oibvh_scene_capture_frame(None, 0, 1, 1, None, None, None) == N.ERR_ARG
+    assert L.oibvh_tree_set_morton_bits(None, 63) == N.ERR_ARG
+    # the allocation-free detect
+    n = ctypes.c_uint32()
+    assert L.oibvh_pair_detect_noalloc(None, None, 0, None, 0, ctypes.byref(n), None) == N.ERR_ARG
