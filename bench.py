@@ -614,7 +614,7 @@ def run_ours_batched(args, rank, world, local):
     build_s = time.perf_counter() - tb
     sc.transform(rest.data_ptr(), mats.data_ptr(), stream=sh)
     sc.refit(stream=sh)
-    tuning = sc.autotune(ENTRY_LEVEL, 2)
+    tuning = sc.autotune(ENTRY_LEVEL, 3)
     sc.capture_frame(ENTRY_LEVEL, EXPAND_LEVELS, True, rest.data_ptr(), mats.data_ptr(), stream=sh)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
     setup_s = time.perf_counter() - t_setup
