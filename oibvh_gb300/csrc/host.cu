@@ -1200,13 +1200,35 @@ API int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t rep
         if (ms < best) best = ms, b_per = (uint32_t)per;
     }
     s->tune_walk_per_sm = b_per;
+    // confirmation: the descent follows noisy timings, so the chosen detect
+    // setting is timed again against the defaults (twice the repetitions)
+    // and the faster one is kept
+    if (st == OIBVH_OK) {
+        const uint32_t reps0 = reps;
+        reps = 2 * reps0;
+        float ms_chosen = 0.0f, ms_default = 0.0f;
+        if (time_setting(ms_chosen)) {
+            s->tune_start_log2 = 16;
+            s->tune_handoff = 2048;
+            s->tune_walk_cap = 128;
+            s->tune_walk_per_sm = 0;
+            if (time_setting(ms_default) && ms_default < ms_chosen) {
+                b_start = 16, b_handoff = 2048, b_cap = 128, b_per = 0;
+            }
+        }
+        reps = reps0;
+        s->tune_start_log2 = b_start;
+        s->tune_handoff = b_handoff;
+        s->tune_walk_cap = b_cap;
+        s->tune_walk_per_sm = b_per;
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (st != OIBVH_OK) return st;
     oibvh_tuning bt{};
     bt.start_pairs_log2 = b_start;
     bt.handoff = b_handoff;
-    bt.walk_blocks_per_sm = b_per ? b_per : (uint32_t)fit;
+    bt.walk_blocks_per_sm = b_per ? b_per : (uint32_t)walk_blocks_per_sm(b_cap);
     bt.walk_front = b_cap;
     bt.refit_group_log2 = b_group;
     // capacities: the largest work list and hit count seen, doubled
