@@ -129,7 +129,7 @@ __device__ __forceinline__ void reduce_block(Box v[4], const TreeShape& S, float
 
 // `jobs` == nullptr: a single tree passed by value in `one`.
 template <int kLog>
-__global__ void __launch_bounds__((1 << kLog) / 4, 1280 / ((1 << kLog) / 4))
+__global__ void __launch_bounds__((1 << kLog) / 4, 1536 / ((1 << kLog) / 4))
     k_refit(const RefitJob* __restrict__ jobs, uint32_t n_jobs, const uint32_t* __restrict__ block_job,
             const RefitJob one)
 {
