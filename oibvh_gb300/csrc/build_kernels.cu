@@ -522,7 +522,7 @@ __global__ void __launch_bounds__(256) k_gather_faces_multi(const BuildJob* __re
 // loads are issued before any arithmetic, for more bytes in flight.
 constexpr uint32_t kTransformUnroll = 4;
 
-__global__ void __launch_bounds__(256) k_transform_multi(const BuildJob* __restrict__ jobs, uint32_t n_jobs,
+__global__ void __launch_bounds__(256, 8) k_transform_multi(const BuildJob* __restrict__ jobs, uint32_t n_jobs,
                                                          const uint32_t* __restrict__ vjob,
                                                          const float4* __restrict__ rest,
                                                          const float* __restrict__ mats, uint32_t v_blocks)
