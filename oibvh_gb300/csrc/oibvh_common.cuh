@@ -162,14 +162,43 @@ __device__ __forceinline__ Box leaf_box(const float4* __restrict__ pos, uint4 f)
                gmax(gmax(a.x, b.x), c.x), gmax(gmax(a.y, b.y), c.y), gmax(gmax(a.z, b.z), c.z)};
 }
 
+// Internal nodes are 32 bytes, (min.xyz, 0, max.xyz, 0), and 32-byte
+// aligned (node arrays start at cudaMalloc or 256-byte arena boundaries), so
+// one node moves as ONE 256-bit access (the .v8 forms of ld/st, sm_100 and
+// later) instead of two 128-bit ones: half the load/store instructions and
+// L1 requests per node.
+// Read-only path: for nodes written by an earlier kernel.
+__device__ __forceinline__ Box load_node_nc(const float4* p)
+{
+    float a, b, c, d, e, f, g, h;
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a), "=f"(b), "=f"(c), "=f"(d), "=f"(e), "=f"(f), "=f"(g), "=f"(h)
+        : "l"(p));
+    return Box{a, b, c, e, f, g};
+}
+// L2 path (no L1): for nodes written by other CTAs of the same kernel.
+__device__ __forceinline__ Box load_node_cg(const float4* p)
+{
+    float a, b, c, d, e, f, g, h;
+    asm volatile("ld.global.cg.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=f"(a), "=f"(b), "=f"(c), "=f"(d), "=f"(e), "=f"(f), "=f"(g), "=f"(h)
+                 : "l"(p)
+                 : "memory");
+    return Box{a, b, c, e, f, g};
+}
+__device__ __forceinline__ void store_node_v8(float4* p, const Box& v)
+{
+    asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(v.nx), "f"(v.ny),
+                 "f"(v.nz), "f"(0.0f), "f"(v.xx), "f"(v.xy), "f"(v.xz), "f"(0.0f)
+                 : "memory");
+}
+
 // Box of a node given by implicit index and level: internal nodes are read
-// from the tree (32 B, two float4), leaves are rebuilt from their face.
+// from the tree (one 32-byte load), leaves are rebuilt from their face.
 __device__ __forceinline__ Box node_box(const TreeView& T, uint32_t implicit, uint32_t level)
 {
     if (level == T.shape.L) return leaf_box(T.pos, __ldg(T.face + implicit - ((1u << level) - 1u)));
-    const float4* p = T.box + 2 * (size_t)T.shape.real_index(implicit);
-    const float4 a = __ldg(p), b = __ldg(p + 1);
-    return Box{a.x, a.y, a.z, b.x, b.y, b.z};
+    return load_node_nc(T.box + 2 * (size_t)T.shape.real_index(implicit));
 }
 
 // aabb_box_t::overlap (include/utils/utils.h:39-44; src/cuda/collide.cu:12-17)

@@ -39,15 +39,7 @@ __device__ __forceinline__ Box shfl_down(const Box& b, int d)
 
 __device__ __forceinline__ void store_node(float4* box, uint32_t real, const Box& b)
 {
-    box[2 * (size_t)real] = make_float4(b.nx, b.ny, b.nz, 0.0f);
-    box[2 * (size_t)real + 1] = make_float4(b.xx, b.xy, b.xz, 0.0f);
-}
-
-__device__ __forceinline__ Box load_node_cg(const float4* box, uint32_t real)
-{
-    const float4 a = __ldcg(box + 2 * (size_t)real);
-    const float4 c = __ldcg(box + 2 * (size_t)real + 1);
-    return Box{a.x, a.y, a.z, c.x, c.y, c.z};
+    store_node_v8(box + 2 * (size_t)real, b);
 }
 
 // Reduce the 2^kLog-node block whose four nodes per thread are v[0..3]
@@ -186,7 +178,7 @@ __global__ void __launch_bounds__((1 << kLog) / 4, 1536 / ((1 << kLog) / 4))
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const uint32_t j = base + 4 * threadIdx.x + k;
-            v[k] = (j < cnt) ? load_node_cg(job.box, off + j) : Box{0, 0, 0, 0, 0, 0};
+            v[k] = (j < cnt) ? load_node_cg(job.box + 2 * (size_t)(off + j)) : Box{0, 0, 0, 0, 0, 0};
         }
         levels = min((uint32_t)kRefitLog, lvl);
         reduce_block<kLog>(v, S, job.box, lvl, base, levels, sm8);

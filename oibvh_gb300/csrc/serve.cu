@@ -44,6 +44,7 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 constexpr size_t kArenaAlign = 256;
+static_assert(kArenaAlign % 32 == 0, "node arrays in the arena must be 32-byte aligned (256-bit node loads)");
 constexpr uint32_t kServeWalkRoundsInit = 8;
 
 size_t align_up(size_t x) { return (x + kArenaAlign - 1) / kArenaAlign * kArenaAlign; }
