@@ -193,6 +193,15 @@ __device__ __forceinline__ void store_node_v8(float4* p, const Box& v)
                  : "memory");
 }
 
+// Two consecutive 16-byte face records as one 256-bit read-only load
+// (face arrays start at cudaMalloc boundaries; p must be 32-byte aligned).
+__device__ __forceinline__ void load_face_pair(const uint4* p, uint4& f0, uint4& f1)
+{
+    asm("ld.global.nc.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(f0.x), "=r"(f0.y), "=r"(f0.z), "=r"(f0.w), "=r"(f1.x), "=r"(f1.y), "=r"(f1.z), "=r"(f1.w)
+        : "l"(p));
+}
+
 // Box of a node given by implicit index and level: internal nodes are read
 // from the tree (one 32-byte load), leaves are rebuilt from their face.
 __device__ __forceinline__ Box node_box(const TreeView& T, uint32_t implicit, uint32_t level)

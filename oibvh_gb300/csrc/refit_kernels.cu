@@ -148,8 +148,13 @@ __global__ void __launch_bounds__((1 << kLog) / 4, 1536 / ((1 << kLog) / 4))
     // ---- leaves: calculate_aabb_kernel (src/cuda/oibvh.cu:24-40), in registers ----
     const uint32_t leaf0 = (chunk << kRefitLog) + 4 * threadIdx.x;
     uint4 f[4];
+    if (leaf0 + 3 < S.nT) {  // leaf0 is a multiple of 4: 64-byte aligned, two 256-bit loads
+        load_face_pair(job.face + leaf0, f[0], f[1]);
+        load_face_pair(job.face + leaf0 + 2, f[2], f[3]);
+    } else {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) f[k] = (leaf0 + k < S.nT) ? __ldg(job.face + leaf0 + k) : make_uint4(0, 0, 0, 0);
+        for (int k = 0; k < 4; ++k) f[k] = (leaf0 + k < S.nT) ? __ldg(job.face + leaf0 + k) : make_uint4(0, 0, 0, 0);
+    }
     Box v[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) v[k] = leaf_box(job.pos, f[k]);
