@@ -399,8 +399,8 @@ __device__ __forceinline__ void test_candidates(const DetectArgs& a, const uint6
     if (lane < count) {
         const uint64_t c = buf[lane];
         const PairView& pv = a.pairs[bvtt_pair(c)];
-        const TreeView& TA = pv.ta;
-        const TreeView& TB = pv.tb;
+        const TreeRef TA = load_tree_ref(pv.ta);
+        const TreeRef TB = load_tree_ref(pv.tb);
         const uint4 fa = __ldg(TA.face + bvtt_a(c));
         const uint4 fb = __ldg(TB.face + bvtt_b(c));
         hit = tri_intersect_exact(load_vertex(TA.pos, fa.x), load_vertex(TA.pos, fa.y), load_vertex(TA.pos, fa.z),
@@ -479,13 +479,13 @@ __device__ __forceinline__ uint32_t expand_pair(const DetectArgs& a, WarpCands& 
         pair = bvtt_pair(node);
         const uint32_t ia = bvtt_a(node), ib = bvtt_b(node);
         const PairView& pv = a.pairs[pair];
-        const TreeView& TA = pv.ta;
-        const TreeView& TB = pv.tb;
+        const TreeRef TA = load_tree_ref(pv.ta);
+        const TreeRef TB = load_tree_ref(pv.tb);
         const uint32_t la = ilog2(ia + 1u), lb = ilog2(ib + 1u);
-        expand_side(TA.shape, ia, la, 1, fa, na);
-        expand_side(TB.shape, ib, lb, 1, fb, nb);
+        expand_side(TA.shape(), ia, la, 1, fa, na);
+        expand_side(TB.shape(), ib, lb, 1, fb, nb);
         const uint32_t lca = ilog2(fa + 1u), lcb = ilog2(fb + 1u);
-        leaves = lca == TA.shape.L && lcb == TB.shape.L;
+        leaves = lca == TA.L && lcb == TB.L;
         leaf_a = fa - ((1u << lca) - 1u);  // Morton-order leaf index when lca is the leaf level
         leaf_b = fb - ((1u << lcb) - 1u);
         A0 = node_box(TA, fa, lca);

@@ -15,6 +15,7 @@
 // the three vertices when it is needed.
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -65,9 +66,9 @@ __host__ __device__ __forceinline__ uint32_t popc(uint32_t x)
 
 // Static shape of one tree (everything derives from T).
 struct TreeShape {
-    uint32_t nT;   // real leaves
     uint32_t L;    // leaf level
     uint32_t vl;   // virtual leaves
+    uint32_t nT;   // real leaves
     uint32_t size; // real nodes, oibvh_get_size (include/cuda/oibvh.cuh:56-59)
 
     __host__ __device__ static TreeShape of(uint32_t nT)
@@ -104,14 +105,35 @@ struct TreeShape {
     }
 };
 
-// Device view of one tree.
-struct TreeView {
+// Device view of one tree. 32-byte aligned: its first 32 bytes (the three
+// arrays, the leaf level and the virtual-leaf count: all that a traversal
+// step needs) are read as one 256-bit load (TreeRef).
+struct alignas(32) TreeView {
     float4* box;        // 2*(size-nT) float4: level-ordered real internal nodes
     const uint4* face;  // Morton-sorted faces: (v0, v1, v2, original face index)
     const float4* pos;  // vertex positions, (x, y, z, unused) per vertex
     TreeShape shape;
     uint32_t nV;
     uint32_t pad0;
+};
+static_assert(offsetof(TreeView, shape) == 24 && offsetof(TreeShape, vl) == 4, "TreeRef is TreeView's first 32 bytes");
+
+// The first 32 bytes of a TreeView, in registers.
+struct TreeRef {
+    float4* box;
+    const uint4* face;
+    const float4* pos;
+    uint32_t L, vl;
+    // index arithmetic only needs L and vl
+    __device__ __forceinline__ TreeShape shape() const
+    {
+        TreeShape s;
+        s.L = L;
+        s.vl = vl;
+        s.nT = 0;
+        s.size = 0;
+        return s;
+    }
 };
 
 // One mesh pair of a detection pass. The two tree views are copied in, so a
@@ -208,6 +230,28 @@ __device__ __forceinline__ Box node_box(const TreeView& T, uint32_t implicit, ui
 {
     if (level == T.shape.L) return leaf_box(T.pos, __ldg(T.face + implicit - ((1u << level) - 1u)));
     return load_node_nc(T.box + 2 * (size_t)T.shape.real_index(implicit));
+}
+__device__ __forceinline__ Box node_box(const TreeRef& T, uint32_t implicit, uint32_t level)
+{
+    if (level == T.L) return leaf_box(T.pos, __ldg(T.face + implicit - ((1u << level) - 1u)));
+    return load_node_nc(T.box + 2 * (size_t)T.shape().real_index(implicit));
+}
+
+// A tree view's first 32 bytes as one 256-bit read-only load (the views are
+// written by the host before the kernels that read them run).
+__device__ __forceinline__ TreeRef load_tree_ref(const TreeView& T)
+{
+    uint32_t r[8];
+    asm("ld.global.nc.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+        : "l"(&T));
+    TreeRef t;
+    t.box = (float4*)(((uint64_t)r[1] << 32) | r[0]);
+    t.face = (const uint4*)(((uint64_t)r[3] << 32) | r[2]);
+    t.pos = (const float4*)(((uint64_t)r[5] << 32) | r[4]);
+    t.L = r[6];
+    t.vl = r[7];
+    return t;
 }
 
 // aabb_box_t::overlap (include/utils/utils.h:39-44; src/cuda/collide.cu:12-17)
