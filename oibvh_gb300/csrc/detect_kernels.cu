@@ -488,10 +488,8 @@ __device__ __forceinline__ uint32_t expand_pair(const DetectArgs& a, WarpCands& 
         leaves = lca == TA.L && lcb == TB.L;
         leaf_a = fa - ((1u << lca) - 1u);  // Morton-order leaf index when lca is the leaf level
         leaf_b = fb - ((1u << lcb) - 1u);
-        A0 = node_box(TA, fa, lca);
-        if (na > 1) A1 = node_box(TA, fa + 1, lca);
-        B0 = node_box(TB, fb, lcb);
-        if (nb > 1) B1 = node_box(TB, fb + 1, lcb);
+        node_boxes(TA, fa, lca, na > 1, A0, A1);
+        node_boxes(TB, fb, lcb, nb > 1, B0, B1);
     }
     // bit (2x + y): child pair (fa + x, fb + y) overlaps
     uint32_t m = 0;
@@ -579,10 +577,10 @@ __global__ void __launch_bounds__(kDetectThreads) k_init_front(DetectArgs a, uin
             const uint32_t k = i - pv.front_off;
             const uint32_t x = k / pv.front_cnt_b, y = k - x * pv.front_cnt_b;
             const uint32_t ia = (1u << pv.entry_a) - 1u + x, ib = (1u << pv.entry_b) - 1u + y;
-            const TreeView& TA = pv.ta;
-            const TreeView& TB = pv.tb;
+            const TreeRef TA = load_tree_ref(pv.ta);
+            const TreeRef TB = load_tree_ref(pv.tb);
             ov = overlap(node_box(TA, ia, pv.entry_a), node_box(TB, ib, pv.entry_b));
-            leafpair = ov && pv.entry_a == TA.shape.L && pv.entry_b == TB.shape.L;
+            leafpair = ov && pv.entry_a == TA.L && pv.entry_b == TB.L;
             node = bvtt_pack(lo, ia, ib);
             cval = bvtt_pack(lo, x, y);
         }
@@ -733,8 +731,8 @@ __device__ __forceinline__ void load_tris(const DetectArgs& a, uint64_t c, V3& P
                                           V3& Q3, uint4& rec)
 {
     const PairView& pv = a.pairs[bvtt_pair(c)];
-    const TreeView& TA = pv.ta;
-    const TreeView& TB = pv.tb;
+    const TreeRef TA = load_tree_ref(pv.ta);
+    const TreeRef TB = load_tree_ref(pv.tb);
     const uint4 fa = __ldg(TA.face + bvtt_a(c));
     const uint4 fb = __ldg(TB.face + bvtt_b(c));
     P1 = load_vertex(TA.pos, fa.x);

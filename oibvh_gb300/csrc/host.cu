@@ -42,7 +42,9 @@ static int tree_alloc(oibvh_tree_t t)
     OK_TRY(t->xyz.ensure(3 * (size_t)t->nV, "cudaMalloc(positions)"));
     OK_TRY(t->pos4.ensure((size_t)t->nV, "cudaMalloc(positions)"));
     OK_TRY(t->tri.ensure(3 * (size_t)t->nT, "cudaMalloc(faces)"));
-    OK_TRY(t->face.ensure(t->nT, "cudaMalloc(sorted faces)"));
+    // one record more than the faces: traversal reads two sibling leaves' faces as one
+    // 32-byte load, and the last leaf's sibling may be virtual (past the end)
+    OK_TRY(t->face.ensure((size_t)t->nT + 1, "cudaMalloc(sorted faces)"));
     OK_TRY(t->box.ensure(2 * (size_t)std::max(1u, t->shape.size - t->nT), "cudaMalloc(tree)"));
     OK_TRY(t->counters.ensure(refit_counters_per_tree(), "cudaMalloc(counters)"));
     return OIBVH_OK;

@@ -237,6 +237,32 @@ __device__ __forceinline__ Box node_box(const TreeRef& T, uint32_t implicit, uin
     return load_node_nc(T.box + 2 * (size_t)T.shape().real_index(implicit));
 }
 
+// Boxes of `first` and, when `two`, its right neighbour on the same level.
+// Leaves: sibling leaves 2j and 2j+1 have adjacent 16-byte face records, read
+// as one 32-byte load (face arrays hold one record past the last face, so the
+// load stays inside the array when the sibling is virtual); an odd leaf index
+// only occurs for a leaf that stays put, read on its own.
+__device__ __forceinline__ void node_boxes(const TreeRef& T, uint32_t first, uint32_t level, bool two, Box& b0,
+                                           Box& b1)
+{
+    if (level == T.L) {
+        const uint32_t i = first - ((1u << level) - 1u);
+        uint4 f0, f1;
+        if ((i & 1u) == 0) {
+            load_face_pair(T.face + i, f0, f1);
+        } else {
+            f0 = __ldg(T.face + i);
+            f1 = two ? __ldg(T.face + i + 1) : f0;
+        }
+        b0 = leaf_box(T.pos, f0);
+        if (two) b1 = leaf_box(T.pos, f1);
+    } else {
+        const float4* p = T.box + 2 * (size_t)T.shape().real_index(first);
+        b0 = load_node_nc(p);
+        if (two) b1 = load_node_nc(p + 2);  // same level: the next real node
+    }
+}
+
 // A tree view's first 32 bytes as one 256-bit read-only load (the views are
 // written by the host before the kernels that read them run).
 __device__ __forceinline__ TreeRef load_tree_ref(const TreeView& T)
