@@ -938,6 +938,8 @@ def run_ours_precision(args, rank, world, local):
     sc.build(stream=sh)
     sc.transform(rest.data_ptr(), mats.data_ptr(), stream=sh)
     sc.refit(stream=sh)
+    sc.set_precision(_native.PRECISION_FP64_FILTERED)
+    tuning = sc.autotune(ENTRY_LEVEL, 3)  # the library's autotuner, on the first frame (FP64-filtered)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
     hit_buf = torch.empty((1 << 24, 4), dtype=torch.int32).pin_memory()
 
@@ -1033,6 +1035,7 @@ def run_ours_precision(args, rank, world, local):
         "dtype": "f32 + f64 (filtered)", "data": "synthetic (seeded sine sheets)",
         "config": {"workload": w.name, **w.info, "entry_level": ENTRY_LEVEL, "expand_levels": EXPAND_LEVELS,
                    "frame": "one captured CUDA graph: identity transforms + refit all sheets + detect all pairs",
+                   "tuning": tuning,
                    "l2": "flushed between steps (256 MiB write, outside the timed events)",
                    "parallelism": f"replicas{world}"},
         "frame_latency_ms": {"p50": round(_pctl(lat_f, 50), 4), "p99": round(_pctl(lat_f, 99), 4),

@@ -10,8 +10,8 @@
 // the node pairs at a start level and lists the overlapping ones; k_top (one
 // CTA) walks the narrow top levels until the front is wide; in k_walk every
 // warp takes an interleaved share of that front and walks it to the leaves
-// with a private front in shared memory (its capacity a tuning parameter);
-// what outgrows it spills to the next round's list, so no grid-wide
+// through a private FIFO ring in shared memory (its capacity a tuning
+// parameter); what outgrows it spills to the next round's list, so no grid-wide
 // synchronisation is needed. The host enqueues the rounds and reads the
 // counters back once. Appends (next front, spills, hits) are warp-aggregated:
 // one atomic per warp, positions from ballot/shuffle prefix sums.
@@ -377,8 +377,15 @@ constexpr int kCandBuf = 64;  // <= 31 left over + 32 added per round
 constexpr uint32_t kTopThreads = 1024;  // the single CTA of the top levels
 constexpr uint32_t kTopCap = 8192;      // its front capacity (two buffers: 128 KB)
 constexpr uint32_t kHandoff = 2048;     // front width at which the walkers take over
-constexpr uint32_t kWalkCap = 128;      // default per-warp front capacity of the walkers
+constexpr uint32_t kWalkCap = 128;      // default per-warp ring capacity of the walkers (node pairs)
 constexpr uint32_t kWalkCapMax = 512;
+// Ring entries per warp for a requested capacity (0: the default): at least
+// 64, so that a top-up of 32 list items always fits beside up to 31 queued.
+__host__ __device__ __forceinline__ uint32_t walk_ring(uint32_t cap)
+{
+    cap = cap ? cap : kWalkCap;
+    return cap < 64u ? 64u : cap;
+}
 
 struct WarpCands {
     uint64_t* buf;       // kCandBuf entries
@@ -462,15 +469,15 @@ __device__ __forceinline__ void push_candidate(const DetectArgs& a, WarpCands& w
 
 // One BVTT pair per lane, one level down on both sides (a leaf stays put):
 // all child boxes are loaded first (independent loads), the up to 4 child
-// pairs are tested, overlapping leaf pairs become candidates and the other
-// overlapping pairs are appended to the CTA's next front in shared memory
-// (one shared atomic per warp); what does not fit goes to the spill list
-// of the next round.
-// Returns the number of child pairs tested (lane 0 only, else 0).
+// pairs are tested and overlapping leaf pairs become candidates. Returns the
+// overlapping internal child pairs (bit 2x + y: child pair (fa + x, fb + y));
+// `tested` gets the warp's number of child pairs tested (lane 0 only).
+struct Expansion {
+    uint32_t pair, fa, fb, m;
+};
 template <bool kFused>
-__device__ __forceinline__ uint32_t expand_pair(const DetectArgs& a, WarpCands& wc, bool valid, uint64_t node,
-                                                uint64_t* next, uint32_t* next_cnt, uint32_t next_cap,
-                                                uint64_t* __restrict__ spill, uint32_t* spill_cnt, uint32_t lane)
+__device__ __forceinline__ Expansion expand_test(const DetectArgs& a, WarpCands& wc, bool valid, uint64_t node,
+                                                 uint32_t lane, uint32_t& tested)
 {
     uint32_t pair = 0, fa = 0, fb = 0, na = 0, nb = 0, leaf_a = 0, leaf_b = 0;
     bool leaves = false;
@@ -499,7 +506,8 @@ __device__ __forceinline__ uint32_t expand_pair(const DetectArgs& a, WarpCands& 
         if (na > 1) m |= overlap(A1, B0) ? 4u : 0u;
         if (na > 1 && nb > 1) m |= overlap(A1, B1) ? 8u : 0u;
     }
-    const uint32_t tested = __reduce_add_sync(0xffffffffu, na * nb);
+    const uint32_t t = __reduce_add_sync(0xffffffffu, na * nb);
+    tested = lane == 0 ? t : 0u;
     // candidates, one bit per round (at most 4 rounds); every lane joins each round
     uint32_t cm = leaves ? m : 0u;
     while (__any_sync(0xffffffffu, cm != 0)) {
@@ -512,16 +520,60 @@ __device__ __forceinline__ uint32_t expand_pair(const DetectArgs& a, WarpCands& 
         }
         push_candidate<kFused>(a, wc, pred, c, lane);
     }
-    // the overlapping internal pairs: reserve slots for the whole warp at once
-    const uint32_t cnt = leaves ? 0u : (uint32_t)__popc(m);
+    return Expansion{pair, fa, fb, leaves ? 0u : m};
+}
+
+// Exclusive prefix over the warp of each lane's child count; `total` = the
+// warp's sum.
+__device__ __forceinline__ uint32_t child_prefix(uint32_t cnt, uint32_t lane, uint32_t& total)
+{
     uint32_t incl = cnt;
 #pragma unroll
     for (int s = 1; s < 32; s <<= 1) {
         const uint32_t y = __shfl_up_sync(0xffffffffu, incl, s);
         if ((int)lane >= s) incl += y;
     }
-    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    if (total == 0) return lane == 0 ? tested : 0u;
+    total = __shfl_sync(0xffffffffu, incl, 31);
+    return incl - cnt;
+}
+
+// Children of position `pos` onward go to `slot(pos)` while pos < fit, the
+// rest to the spill list from sbase.
+template <typename Slot>
+__device__ __forceinline__ void write_children(const DetectArgs& a, const Expansion& e, uint32_t pos, uint32_t fit,
+                                               uint64_t* __restrict__ spill, uint32_t sbase, Slot slot)
+{
+    bool overflow = false;
+    uint32_t mm = e.m;
+    while (mm) {
+        const uint32_t k = __ffs(mm) - 1;
+        mm &= mm - 1;
+        const uint64_t child = bvtt_pack(e.pair, e.fa + (k >> 1), e.fb + (k & 1));
+        if (pos < fit) *slot(pos) = child;
+        else {
+            const uint32_t sp = sbase + (pos - fit);
+            if (sp < a.work_cap) spill[sp] = child;
+            else overflow = true;
+        }
+        ++pos;
+    }
+    if (overflow) atomicOr(a.counts + kCountFlags, (uint32_t)kFlagFrontOverflow);
+}
+
+// expand_test, then the overlapping internal pairs go to the CTA's next
+// front in shared memory (one shared atomic per warp); what does not fit
+// goes to the spill list of the next round. Returns the number of child
+// pairs tested (lane 0 only, else 0).
+template <bool kFused>
+__device__ __forceinline__ uint32_t expand_pair(const DetectArgs& a, WarpCands& wc, bool valid, uint64_t node,
+                                                uint64_t* next, uint32_t* next_cnt, uint32_t next_cap,
+                                                uint64_t* __restrict__ spill, uint32_t* spill_cnt, uint32_t lane)
+{
+    uint32_t tested;
+    const Expansion e = expand_test<kFused>(a, wc, valid, node, lane, tested);
+    uint32_t total;
+    const uint32_t ex = child_prefix((uint32_t)__popc(e.m), lane, total);
+    if (total == 0) return tested;
     uint32_t wbase = 0, sbase = 0;
     if (lane == 31) {
         wbase = atomicAdd(next_cnt, total);
@@ -530,24 +582,10 @@ __device__ __forceinline__ uint32_t expand_pair(const DetectArgs& a, WarpCands& 
     }
     wbase = __shfl_sync(0xffffffffu, wbase, 31);
     sbase = __shfl_sync(0xffffffffu, sbase, 31);
-    const uint32_t spill_from = max(wbase, next_cap);  // first front position that spills
-    uint32_t pos = wbase + incl - cnt;
-    bool overflow = false;
-    uint32_t mm = leaves ? 0u : m;
-    while (mm) {
-        const uint32_t k = __ffs(mm) - 1;
-        mm &= mm - 1;
-        const uint64_t child = bvtt_pack(pair, fa + (k >> 1), fb + (k & 1));
-        if (pos < next_cap) next[pos] = child;
-        else {
-            const uint32_t sp = sbase + (pos - spill_from);
-            if (sp < a.work_cap) spill[sp] = child;
-            else overflow = true;
-        }
-        ++pos;
-    }
-    if (overflow) atomicOr(a.counts + kCountFlags, (uint32_t)kFlagFrontOverflow);
-    return lane == 0 ? tested : 0u;
+    // warp-relative positions: [0, fit) in the front from wbase, the rest spill
+    const uint32_t fit = wbase >= next_cap ? 0u : min(total, next_cap - wbase);
+    write_children(a, e, ex, fit, spill, sbase, [&](uint32_t p) { return next + wbase + p; });
+    return tested;
 }
 
 // Initial work list: every start-level node pair of every mesh pair (the
@@ -656,15 +694,19 @@ __global__ void __launch_bounds__(kTopThreads) k_top(DetectArgs a)
 // The wide bottom of the traversal, round `round` (>= 1): every warp takes
 // the work-list items w, w+W, w+2W, ... (W = warps in the grid; the
 // interleave spreads each region of the intersection over many warps) and
-// walks them to the leaves level by level with a private front in shared
-// memory: warps never wait for each other. A warp whose front outgrows its
-// buffer spills the excess to the next round's list.
+// walks them to the leaves through a private FIFO ring of node pairs in
+// shared memory: each step pops up to 32 pairs (one per lane), expands them
+// and appends the overlapping children at the tail, with no barrier between
+// tree levels, so lanes stay busy as long as a warp's worth of pairs is
+// queued (a level-by-level front leaves the last chunk of every level part
+// empty). The ring is topped up from the warp's share of the list whenever
+// it holds fewer than 32 pairs. Warps never wait for each other; children
+// that do not fit in the ring spill to the next round's list.
 template <bool kFused>
 __global__ void __launch_bounds__(kDetectThreads) k_walk(DetectArgs a, uint32_t round)
 {
-    extern __shared__ uint64_t s_front[];  // [warp][2][cap]
+    extern __shared__ uint64_t s_front[];  // [warp][walk_ring(cap)]: one ring per warp
     __shared__ uint64_t s_cand[kDetectThreads / 32][kCandBuf];
-    __shared__ uint32_t s_cnt[kDetectThreads / 32][2];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     WarpCands wc{s_cand[wib], 0};
     const uint64_t* __restrict__ src = (round & 1) ? a.work[1] : a.work[0];
@@ -673,34 +715,47 @@ __global__ void __launch_bounds__(kDetectThreads) k_walk(DetectArgs a, uint32_t 
     const uint32_t n_src = min(*(volatile uint32_t*)(a.counts + kCountWork0 + round), a.work_cap);
     const uint32_t W = (gridDim.x * blockDim.x) >> 5;
     const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t cap = a.walk_cap ? a.walk_cap : kWalkCap;
-    uint64_t* f0 = s_front + (size_t)wib * 2 * cap;
-    uint64_t* f1 = f0 + cap;
-    uint32_t* cnt = s_cnt[wib];
+    const uint32_t R = walk_ring(a.walk_cap);  // ring entries (>= 64)
+    uint64_t* ring = s_front + (size_t)wib * R;
+    // items of this warp's share: w + j * W for j < n_mine
+    const uint32_t n_mine = n_src > w ? (n_src - w + W - 1) / W : 0u;
+    uint32_t next_item = 0;
+    uint32_t head = 0, live = 0;  // warp-uniform: ring[head .. head + live) mod R is queued
     uint32_t tested = 0;
-
-    for (uint32_t k0 = 0;; k0 += 32) {
-        const uint32_t first = w + k0 * W;
-        if (first >= n_src) break;
-        const uint32_t c0 = min(32u, (n_src - first + W - 1) / W);
-        if (lane < c0) f0[lane] = __ldcg(src + first + lane * W);
-        uint32_t cur = 0, c = c0;
-        __syncwarp();
-        while (c > 0) {
-            uint64_t* fc = cur ? f1 : f0;
-            uint64_t* fn = cur ? f0 : f1;
-            if (lane == 0) cnt[cur ^ 1] = 0;
+    auto slot = [&](uint32_t off) {  // ring index of the entry `off` after head (off < R)
+        const uint32_t i = head + off;
+        return i >= R ? i - R : i;
+    };
+    for (;;) {
+        if (live < 32 && next_item < n_mine) {
+            const uint32_t take = min(32u, n_mine - next_item);  // live + take <= 63 < R
+            if (lane < take) ring[slot(live + lane)] = __ldcg(src + w + (size_t)(next_item + lane) * W);
+            next_item += take;
+            live += take;
             __syncwarp();
-            for (uint32_t base = 0; base < c; base += 32) {
-                const uint32_t i = base + lane;
-                const bool valid = i < c;
-                const uint64_t node = valid ? fc[i] : 0ull;
-                tested += expand_pair<kFused>(a, wc, valid, node, fn, &cnt[cur ^ 1], cap, spill, spill_cnt, lane);
-            }
-            __syncwarp();
-            c = min(cnt[cur ^ 1], cap);
-            cur ^= 1;
         }
+        if (live == 0) break;
+        const uint32_t n = min(32u, live);
+        const bool valid = lane < n;
+        const uint64_t node = valid ? ring[slot(lane)] : 0ull;
+        __syncwarp();  // every lane has read its entry before the slots are reused
+        head = slot(n);
+        live -= n;
+        uint32_t t;
+        const Expansion e = expand_test<kFused>(a, wc, valid, node, lane, t);
+        tested += t;
+        uint32_t total;
+        const uint32_t ex = child_prefix((uint32_t)__popc(e.m), lane, total);
+        if (total == 0) continue;
+        const uint32_t fit = min(total, R - live);
+        uint32_t sbase = 0;
+        if (total > fit) {
+            if (lane == 31) sbase = atomicAdd(spill_cnt, total - fit);
+            sbase = __shfl_sync(0xffffffffu, sbase, 31);
+        }
+        write_children(a, e, ex, fit, spill, sbase, [&](uint32_t p) { return ring + slot(live + p); });
+        live += fit;
+        __syncwarp();  // appended entries are visible to the lanes that pop them
     }
     if (lane == 0 && tested) atomicAdd(a.counts + kCountTested, tested);
     flush_found(a, wc, lane);
@@ -965,7 +1020,7 @@ cudaError_t launch_top(const DetectArgs& a, cudaStream_t s)
     return cudaGetLastError();
 }
 
-static size_t walk_smem(uint32_t cap) { return (size_t)(kDetectThreads / 32) * 2 * (cap ? cap : kWalkCap) * 8; }
+static size_t walk_smem(uint32_t cap) { return (size_t)(kDetectThreads / 32) * walk_ring(cap) * 8; }  // one ring per warp
 
 static cudaError_t walk_configure()
 {

@@ -1186,7 +1186,7 @@ API int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t rep
         }
     s->tune_start_log2 = b_start;
     s->tune_handoff = b_handoff;
-    for (uint32_t cap : {64u, 256u}) {
+    for (uint32_t cap : {64u, 256u, 512u}) {
         if (st != OIBVH_OK) break;
         s->tune_walk_cap = cap;
         float ms;

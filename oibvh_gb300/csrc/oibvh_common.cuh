@@ -192,7 +192,8 @@ __device__ __forceinline__ Box leaf_box(const float4* __restrict__ pos, uint4 f)
 // Read-only path: for nodes written by an earlier kernel.
 __device__ __forceinline__ Box load_node_nc(const float4* p)
 {
-    float a, b, c, d, e, f, g, h;
+    float a, b, c, e, f, g;
+    [[maybe_unused]] float d, h;  // the two padding words
     asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
         : "=f"(a), "=f"(b), "=f"(c), "=f"(d), "=f"(e), "=f"(f), "=f"(g), "=f"(h)
         : "l"(p));
@@ -201,7 +202,8 @@ __device__ __forceinline__ Box load_node_nc(const float4* p)
 // L2 path (no L1): for nodes written by other CTAs of the same kernel.
 __device__ __forceinline__ Box load_node_cg(const float4* p)
 {
-    float a, b, c, d, e, f, g, h;
+    float a, b, c, e, f, g;
+    [[maybe_unused]] float d, h;
     asm volatile("ld.global.cg.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
                  : "=f"(a), "=f"(b), "=f"(c), "=f"(d), "=f"(e), "=f"(f), "=f"(g), "=f"(h)
                  : "l"(p)
