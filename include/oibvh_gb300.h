@@ -76,7 +76,10 @@ int oibvh_tree_create(const float* xyz, uint32_t n_vertices, const uint32_t* tri
 int oibvh_tree_create_copy(oibvh_tree_t other, const float* xyz, uint32_t n_vertices, oibvh_tree_t* out);
 
 /* OibvhTree::build() (src/cuda/oibvhTree.cu:237-388): mesh bounds, Morton
- * codes, stable radix sort, then every tree level. Blocking. */
+ * codes, stable radix sort, then every tree level. The tree then keeps its
+ * vertices numbered in the order the sorted faces first use them (so that
+ * consecutive leaves gather nearby positions); this is internal: every call
+ * takes and returns vertices in the caller's numbering. Blocking. */
 int oibvh_tree_build(oibvh_tree_t t, void* stream);
 
 /* OibvhTree::refit() (src/cuda/oibvhTree.cu:193-235): new leaf boxes from the
@@ -97,9 +100,13 @@ int oibvh_tree_refit_device(oibvh_tree_t t, const float* d_xyz, void* stream);
  *   _set_positions:          host xyz, copied (stream-ordered);
  *   _set_positions_device:   device xyz, converted (stream-ordered);
  *   _set_positions4_device:  device xyzw, 16 bytes per vertex,
- *                            16-byte aligned: used in place, no copy; the
- *                            caller keeps it alive and unchanged until every
- *                            refit and detect that reads it has finished.
+ *                            16-byte aligned, kept by reference: every
+ *                            following refit (of this tree or of its scene)
+ *                            first reads it into the tree's own buffer (one
+ *                            gather pass, in the tree's vertex order), until
+ *                            other positions are set; the caller keeps it
+ *                            alive and unchanged while those refits run. A
+ *                            detect reads the positions of the last refit.
  * Inside the library every vertex is a 16-byte (x, y, z, unused) record, so
  * each vertex gather is one vector load. */
 int oibvh_tree_set_positions(oibvh_tree_t t, const float* xyz, void* stream);
@@ -124,8 +131,8 @@ uint32_t oibvh_tree_get_size(oibvh_tree_t t);
 int oibvh_tree_get_aabbs(oibvh_tree_t t, float* out6, uint64_t cap_nodes);
 
 /* m_faces after build (src/cuda/oibvhTree.cu:377): the faces in Morton
- * order, and perm[i] = original index of sorted face i (either output may be
- * NULL). Blocking. */
+ * order (vertex indices in the caller's numbering), and perm[i] = original
+ * index of sorted face i (either output may be NULL). Blocking. */
 int oibvh_tree_get_sorted_faces(oibvh_tree_t t, uint32_t* out3, uint32_t* perm, uint64_t cap);
 
 int oibvh_tree_destroy(oibvh_tree_t t);
@@ -233,7 +240,9 @@ int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t reps, o
  * graph (re-capturing first if the scene or tuning changed); finish_frame
  * waits for it and validates: if a queue overflowed, it reruns the detect the
  * synchronous way and marks the graph for re-capture, so results are always
- * complete. Matrix contents at d_mats may change between launches. */
+ * complete. Matrix contents at d_mats may change between launches; the rest
+ * positions are copied at capture (in each tree's vertex order), so capture
+ * again after changing them. */
 int oibvh_scene_capture_frame(oibvh_scene_t s, uint32_t entry_level, uint32_t expand_levels, int refit,
                               const float* d_rest_xyzw, const float* d_mats, void* stream);
 int oibvh_scene_launch_frame(oibvh_scene_t s, void* stream);

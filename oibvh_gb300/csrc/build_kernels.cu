@@ -40,13 +40,79 @@ __global__ void k_bounds_init(uint32_t* keys)
 
 // Positions as given (x, y, z) to the device layout (x, y, z, 0): one
 // 16-byte vector load per vertex everywhere else.
-__global__ void __launch_bounds__(256) k_xyz_to_pos4(const float* __restrict__ xyz, uint32_t nV,
-                                                     float4* __restrict__ pos)
+// Positions in the tree's vertex order: tree vertex v is the caller's vertex
+// vperm[v] (vperm == nullptr: the caller's order).
+__global__ void __launch_bounds__(256) k_xyz_to_pos4(const float* __restrict__ xyz, const uint32_t* __restrict__ vperm,
+                                                     uint32_t nV, float4* __restrict__ pos)
 {
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nV) return;
-    pos[v] = make_float4(__ldg(xyz + 3 * (size_t)v), __ldg(xyz + 3 * (size_t)v + 1), __ldg(xyz + 3 * (size_t)v + 2),
-                         0.0f);
+    const size_t u = vperm ? __ldg(vperm + v) : v;
+    pos[v] = make_float4(__ldg(xyz + 3 * u), __ldg(xyz + 3 * u + 1), __ldg(xyz + 3 * u + 2), 0.0f);
+}
+__global__ void __launch_bounds__(256) k_gather_pos4(const float4* __restrict__ src, const uint32_t* __restrict__ vperm,
+                                                     uint32_t nV, float4* __restrict__ pos)
+{
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    pos[v] = __ldg(src + (vperm ? __ldg(vperm + v) : v));
+}
+
+// ---------------------------------------------------------------------------
+// Vertex order: after the faces are sorted, a tree renumbers its vertices in
+// the order the sorted faces first use them, so that the refit's and the
+// traversal's vertex gathers for consecutive leaves fall on nearby positions
+// (the caller's order is arbitrary). Unreferenced vertices go last, in their
+// previous order. Results do not depend on it: faces keep their order and
+// original indices, and a face's three corners keep theirs.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kUnused = (1u << 25) - 1u;  // above every 3 f + slot (f < 2^23): 25-bit sort keys
+
+__global__ void __launch_bounds__(256) k_first_use_init(uint32_t* __restrict__ first, uint32_t* __restrict__ idx,
+                                                        uint32_t nV)
+{
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    first[v] = kUnused;
+    idx[v] = v;
+}
+__global__ void __launch_bounds__(256) k_first_use(const uint4* __restrict__ face, uint32_t nT,
+                                                   uint32_t* __restrict__ first)
+{
+    const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nT) return;
+    const uint4 r = __ldg(face + f);
+    atomicMin(first + r.x, 3u * f);
+    atomicMin(first + r.y, 3u * f + 1u);
+    atomicMin(first + r.z, 3u * f + 2u);
+}
+// order[j] = the current index of new vertex j: inv[order[j]] = j, the new
+// positions and the new caller-order map.
+__global__ void __launch_bounds__(256) k_apply_order(const uint32_t* __restrict__ order, uint32_t nV,
+                                                     uint32_t* __restrict__ inv, const float4* __restrict__ pos,
+                                                     float4* __restrict__ pos_new, const uint32_t* __restrict__ vperm,
+                                                     uint32_t* __restrict__ vperm_new)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nV) return;
+    const uint32_t o = __ldg(order + j);
+    inv[o] = j;
+    pos_new[j] = __ldg(pos + o);
+    vperm_new[j] = vperm ? __ldg(vperm + o) : o;
+}
+__global__ void __launch_bounds__(256) k_renumber_faces(uint4* __restrict__ face, uint32_t* __restrict__ tri,
+                                                        uint32_t nT, const uint32_t* __restrict__ inv)
+{
+    const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nT) return;
+    uint4 r = face[f];
+    r.x = __ldg(inv + r.x);
+    r.y = __ldg(inv + r.y);
+    r.z = __ldg(inv + r.z);
+    face[f] = r;
+    tri[3 * (size_t)f] = __ldg(inv + tri[3 * (size_t)f]);
+    tri[3 * (size_t)f + 1] = __ldg(inv + tri[3 * (size_t)f + 1]);
+    tri[3 * (size_t)f + 2] = __ldg(inv + tri[3 * (size_t)f + 2]);
 }
 
 __global__ void __launch_bounds__(256) k_mesh_bounds(const float4* __restrict__ pos, uint32_t nV, uint32_t* keys)
@@ -334,11 +400,52 @@ size_t radix_sort_scratch_bytes(uint32_t n)
     return (size_t)256 * n_tiles * sizeof(uint32_t) + 256 * sizeof(uint32_t) + 2 * (size_t)n * sizeof(uint32_t);
 }
 
-cudaError_t launch_xyz_to_pos4(const float* xyz, uint32_t nV, float4* pos, cudaStream_t s)
+cudaError_t launch_xyz_to_pos4(const float* xyz, const uint32_t* vperm, uint32_t nV, float4* pos, cudaStream_t s)
 {
     note_launches(1);
-    k_xyz_to_pos4<<<(nV + 255) / 256, 256, 0, s>>>(xyz, nV, pos);
+    k_xyz_to_pos4<<<(nV + 255) / 256, 256, 0, s>>>(xyz, vperm, nV, pos);
     return cudaGetLastError();
+}
+
+cudaError_t launch_gather_pos4(const float4* src, const uint32_t* vperm, uint32_t nV, float4* pos, cudaStream_t s)
+{
+    note_launches(1);
+    k_gather_pos4<<<(nV + 255) / 256, 256, 0, s>>>(src, vperm, nV, pos);
+    return cudaGetLastError();
+}
+
+size_t reorder_scratch_bytes(uint32_t nV)
+{
+    const size_t arr = ((size_t)nV * 4 + 255) / 256 * 256;
+    return 4 * arr + ((size_t)nV * 16 + 255) / 256 * 256 + radix_sort_scratch_bytes(nV);
+}
+
+cudaError_t launch_reorder_vertices(uint4* face, uint32_t* tri, uint32_t nT, uint32_t nV, float4* pos,
+                                    uint32_t* vperm, bool has_vperm, void* scratch, cudaStream_t s)
+{
+    const size_t arr = ((size_t)nV * 4 + 255) / 256 * 256;
+    uint8_t* base = (uint8_t*)scratch;
+    uint32_t* first = (uint32_t*)base;
+    uint32_t* order = (uint32_t*)(base + arr);
+    uint32_t* inv = (uint32_t*)(base + 2 * arr);
+    uint32_t* vperm_new = (uint32_t*)(base + 3 * arr);
+    float4* pos_new = (float4*)(base + 4 * arr);
+    void* sort_scratch = base + 4 * arr + ((size_t)nV * 16 + 255) / 256 * 256;
+    const uint32_t vb = (nV + 255) / 256, fb = (nT + 255) / 256;
+    note_launches(3);
+    k_first_use_init<<<vb, 256, 0, s>>>(first, order, nV);
+    k_first_use<<<fb, 256, 0, s>>>(face, nT, first);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = launch_radix_sort(first, order, nV, 25, sort_scratch, s);  // stable: unused vertices keep their order
+    if (e != cudaSuccess) return e;
+    k_apply_order<<<vb, 256, 0, s>>>(order, nV, inv, pos, pos_new, has_vperm ? vperm : nullptr, vperm_new);
+    k_renumber_faces<<<fb, 256, 0, s>>>(face, tri, nT, inv);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(pos, pos_new, (size_t)nV * sizeof(float4), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyAsync(vperm, vperm_new, (size_t)nV * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
 }
 
 cudaError_t launch_mesh_bounds(const float4* xyz, uint32_t nV, uint32_t* bound_keys, int num_sms, cudaStream_t s)
@@ -525,7 +632,8 @@ constexpr uint32_t kTransformUnroll = 4;
 __global__ void __launch_bounds__(256, 8) k_transform_multi(const BuildJob* __restrict__ jobs, uint32_t n_jobs,
                                                          const uint32_t* __restrict__ vjob,
                                                          const float4* __restrict__ rest,
-                                                         const float* __restrict__ mats, uint32_t v_blocks)
+                                                         const float* __restrict__ mats, uint32_t v_blocks,
+                                                         bool rest_tree_order)
 {
     float4 p[kTransformUnroll];
     uint32_t jj[kTransformUnroll], vv[kTransformUnroll];
@@ -539,8 +647,10 @@ __global__ void __launch_bounds__(256, 8) k_transform_multi(const BuildJob* __re
         if (v >= jobs[j].nV) continue;
         jj[k] = j;
         vv[k] = v;
-        // packed rest positions of all jobs, or (rest == nullptr) each job's own source
-        p[k] = __ldg(rest ? rest + jobs[j].vert_off + v : jobs[j].pos + v);
+        // packed rest positions of all jobs (the caller's vertex order: through vperm), or
+        // (rest == nullptr) each job's own source (the tree's order)
+        const uint32_t* vp = rest_tree_order ? nullptr : jobs[j].vperm;
+        p[k] = rest ? __ldg(rest + jobs[j].vert_off + (vp ? __ldg(vp + v) : v)) : __ldg(jobs[j].pos + v);
     }
 #pragma unroll
     for (uint32_t k = 0; k < kTransformUnroll; ++k) {
@@ -596,11 +706,34 @@ size_t build_multi_scratch_bytes(uint32_t n_faces)
 }
 
 cudaError_t launch_transform_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, const uint32_t* vjob,
-                                   const float4* rest, const float* mats, cudaStream_t s)
+                                   const float4* rest, const float* mats, bool rest_tree_order, cudaStream_t s)
 {
     note_launches(1);
     k_transform_multi<<<(v_blocks + kTransformUnroll - 1) / kTransformUnroll, 256, 0, s>>>(d_jobs, n_jobs, vjob, rest,
-                                                                                            mats, v_blocks);
+                                                                                            mats, v_blocks,
+                                                                                            rest_tree_order);
+    return cudaGetLastError();
+}
+
+// Packed rest positions (caller's vertex order per tree) into each tree's
+// vertex order: out[vert_off + v] = rest[vert_off + vperm[v]].
+__global__ void __launch_bounds__(256) k_gather_rest_multi(const BuildJob* __restrict__ jobs, uint32_t n_jobs,
+                                                           const uint32_t* __restrict__ vjob,
+                                                           const float4* __restrict__ rest, float4* __restrict__ out)
+{
+    const uint32_t j = find_job(jobs, n_jobs, blockIdx.x, false, vjob);
+    const uint32_t v = (blockIdx.x - jobs[j].vblock_begin) * 256u + threadIdx.x;
+    if (v >= jobs[j].nV) return;
+    const uint32_t* vp = jobs[j].vperm;
+    out[jobs[j].vert_off + v] = __ldg(rest + jobs[j].vert_off + (vp ? __ldg(vp + v) : v));
+}
+
+cudaError_t launch_gather_rest_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, const uint32_t* vjob,
+                                     const float4* rest, float4* out, cudaStream_t s)
+{
+    if (v_blocks == 0) return cudaSuccess;
+    note_launches(1);
+    k_gather_rest_multi<<<v_blocks, 256, 0, s>>>(d_jobs, n_jobs, vjob, rest, out);
     return cudaGetLastError();
 }
 

@@ -77,7 +77,7 @@ static int tree_create_impl(const float* xyz, uint32_t nV, const uint32_t* tri, 
     if (st == OIBVH_OK) {
         cudaError_t e = cudaMemcpy(t->xyz.p, xyz, 3 * (size_t)nV * sizeof(float), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemcpy(t->tri.p, tri, 3 * (size_t)nT * sizeof(uint32_t), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = launch_xyz_to_pos4(t->xyz.p, nV, t->pos4.p, 0);
+        if (e == cudaSuccess) e = launch_xyz_to_pos4(t->xyz.p, nullptr, nV, t->pos4.p, 0);
         if (e == cudaSuccess) e = cudaStreamSynchronize(0);
         if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpy(mesh)");
     }
@@ -87,6 +87,29 @@ static int tree_create_impl(const float* xyz, uint32_t nV, const uint32_t* tri, 
     }
     t->cur_pos = t->pos4.p;
     *out = t;
+    return OIBVH_OK;
+}
+
+// Borrowed positions (caller's order) into the tree's own buffer, in the
+// tree's vertex order.
+static int sync_positions(oibvh_tree_t t, cudaStream_t s)
+{
+    if (t->borrowed) CUDA_TRY(launch_gather_pos4(t->borrowed, t->vmap(), t->nV, t->pos4.p, s));
+    t->cur_pos = t->pos4.p;
+    return OIBVH_OK;
+}
+
+// After the faces are sorted: vertices renumbered in the order the sorted
+// faces first use them (faces, `tri`, positions and the caller-order map).
+static int reorder_vertices(oibvh_tree_t t, cudaStream_t s)
+{
+    DevBuf<uint8_t> scratch;
+    OK_TRY(scratch.ensure(reorder_scratch_bytes(t->nV), "cudaMalloc(reorder scratch)"));
+    OK_TRY(t->vperm.ensure(t->nV, "cudaMalloc(vertex order)"));
+    CUDA_TRY(launch_reorder_vertices(t->face.p, t->tri.p, t->nT, t->nV, t->pos4.p, t->vperm.p, t->reordered,
+                                     scratch.p, s));
+    CUDA_TRY(cudaStreamSynchronize(s));  // the scratch is freed on return
+    t->reordered = true;
     return OIBVH_OK;
 }
 
@@ -108,6 +131,7 @@ static int tree_build_impl(oibvh_tree_t t, cudaStream_t s)
     uint32_t* idx = (uint32_t*)(scratch.p + idx_off);
     uint32_t* hi = (uint32_t*)(scratch.p + hi_off);
     uint32_t* hi_sorted = (uint32_t*)(scratch.p + gath_off);
+    OK_TRY(sync_positions(t, s));
     CUDA_TRY(launch_mesh_bounds(t->cur_pos, t->nV, keys6, sm_count(t->device), s));
     CUDA_TRY(launch_leaf_morton(t->tri.p, t->cur_pos, nT, keys6, codes, idx, wide ? hi : nullptr, s));
     // stable LSD order by (key, original index): low key bits first, then the high ones
@@ -117,6 +141,7 @@ static int tree_build_impl(oibvh_tree_t t, cudaStream_t s)
         CUDA_TRY(launch_radix_sort(hi_sorted, idx, nT, 31, scratch.p + sort_off, s));
     }
     CUDA_TRY(launch_gather_faces(t->tri.p, idx, nT, t->face.p, s));
+    OK_TRY(reorder_vertices(t, s));
     CUDA_TRY(launch_refit_one(t->job(), s));
     CUDA_TRY(cudaStreamSynchronize(s));
     t->built = true;
@@ -174,6 +199,7 @@ struct oibvh_scene_s {
     uint32_t frame_entry = 0, frame_expand = 1, frame_rounds = 3, frame_kernels = 0, frame_redos = 0;
     bool frame_refit = true;
     const float4* frame_rest = nullptr;
+    DevBuf<float4> frame_rest_tree;  // frame_rest in each tree's vertex order (gathered at capture)
     const float* frame_mats = nullptr;
     PinnedBuf<uint32_t> h_frame_counts;
     cudaStream_t capture_stream = nullptr;  // private stream the frame is captured on
@@ -553,8 +579,15 @@ API int oibvh_tree_create_copy(oibvh_tree_t other, const float* xyz, uint32_t n_
     t->shape = other->shape;
     int st = tree_alloc(t);
     if (st == OIBVH_OK) {
-        cudaError_t e = cudaMemcpy(t->xyz.p, xyz, 3 * (size_t)t->nV * sizeof(float), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = launch_xyz_to_pos4(t->xyz.p, t->nV, t->pos4.p, 0);
+        cudaError_t e = cudaSuccess;
+        if (other->reordered) {
+            e = t->vperm.ensure(t->nV, "cudaMalloc(vertex order)") == OIBVH_OK ? cudaSuccess : cudaErrorMemoryAllocation;
+            if (e == cudaSuccess)
+                e = cudaMemcpy(t->vperm.p, other->vperm.p, (size_t)t->nV * sizeof(uint32_t), cudaMemcpyDeviceToDevice);
+            t->reordered = true;
+        }
+        if (e == cudaSuccess) e = cudaMemcpy(t->xyz.p, xyz, 3 * (size_t)t->nV * sizeof(float), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = launch_xyz_to_pos4(t->xyz.p, t->vmap(), t->nV, t->pos4.p, 0);
         if (e == cudaSuccess) e = cudaStreamSynchronize(0);
         if (e == cudaSuccess)
             e = cudaMemcpy(t->tri.p, other->tri.p, 3 * (size_t)t->nT * sizeof(uint32_t), cudaMemcpyDeviceToDevice);
@@ -591,8 +624,9 @@ static int stage_xyz(oibvh_tree_t t, const float* xyz, bool on_device, cudaStrea
         CUDA_TRY(cudaMemcpyAsync(t->xyz.p, xyz, 3 * (size_t)t->nV * sizeof(float), cudaMemcpyHostToDevice, s));
         src = t->xyz.p;
     }
-    CUDA_TRY(launch_xyz_to_pos4(src, t->nV, t->pos4.p, s));
+    CUDA_TRY(launch_xyz_to_pos4(src, t->vmap(), t->nV, t->pos4.p, s));
     t->cur_pos = t->pos4.p;
+    t->borrowed = nullptr;
     return OIBVH_OK;
 }
 
@@ -614,6 +648,7 @@ API int oibvh_tree_refit(oibvh_tree_t t, const float* xyz, void* stream)
     DeviceGuard g(t->device);
     cudaStream_t s = (cudaStream_t)stream;
     if (xyz) OK_TRY(stage_xyz(t, xyz, false, s));
+    else OK_TRY(sync_positions(t, s));
     CUDA_TRY(launch_refit_one(t->job(), s));
     return OIBVH_OK;
     GUARD_END
@@ -657,7 +692,7 @@ API int oibvh_tree_set_positions4_device(oibvh_tree_t t, const float* d_xyzw)
     if (!t || !d_xyzw) return fail(OIBVH_ERR_ARG, "tree or d_xyzw is NULL");
     DeviceGuard g(t->device);
     OK_TRY(check_device_ptr(d_xyzw, 16));
-    t->cur_pos = (const float4*)d_xyzw;
+    t->borrowed = (const float4*)d_xyzw;  // read (in the tree's vertex order) by every following refit
     return OIBVH_OK;
     GUARD_END
 }
@@ -718,11 +753,17 @@ API int oibvh_tree_get_sorted_faces(oibvh_tree_t t, uint32_t* out3, uint32_t* pe
     std::vector<uint4> tmp(n);
     CUDA_TRY(cudaDeviceSynchronize());
     CUDA_TRY(cudaMemcpy(tmp.data(), t->face.p, n * sizeof(uint4), cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> vp;  // the tree's vertex numbering back to the caller's
+    if (out3 && t->reordered) {
+        vp.resize(t->nV);
+        CUDA_TRY(cudaMemcpy(vp.data(), t->vperm.p, (size_t)t->nV * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    }
+    auto caller = [&](uint32_t v) { return vp.empty() ? v : vp[v]; };
     for (size_t i = 0; i < n; ++i) {
         if (out3) {
-            out3[3 * i] = tmp[i].x;
-            out3[3 * i + 1] = tmp[i].y;
-            out3[3 * i + 2] = tmp[i].z;
+            out3[3 * i] = caller(tmp[i].x);
+            out3[3 * i + 1] = caller(tmp[i].y);
+            out3[3 * i + 2] = caller(tmp[i].z);
         }
         if (perm) perm[i] = tmp[i].w;
     }
@@ -827,6 +868,7 @@ API int oibvh_scene_refit(oibvh_scene_t s, void* stream)
     for (size_t i = 0; i < n; ++i) {
         const oibvh_tree_t t = s->trees[i];
         if (!t->built) return fail(OIBVH_ERR_STATE, "every tree must be built before refit");
+        OK_TRY(sync_positions(t, st));
         RefitJob j = t->job();
         j.n_blocks = refit_blocks_for(t->nT, s->tune_refit_log);
         j.block_begin = blocks;
@@ -1006,6 +1048,7 @@ int ensure_build_jobs(oibvh_scene_s* s, cudaStream_t st)
         j.fblock_begin = fb;
         j.face_off = fo;
         j.vert_off = vo;
+        j.vperm = t->vmap();
         vb += (t->nV + 255) / 256;
         fb += (t->nT + 255) / 256;
         if ((uint64_t)fo + t->nT > 0xffffffffull || (uint64_t)vo + t->nV > 0xffffffffull)
@@ -1050,6 +1093,7 @@ API int oibvh_scene_build(oibvh_scene_t s, void* stream)
     if (s->trees.empty()) return OIBVH_OK;
     DeviceGuard g(s->device);
     cudaStream_t st = (cudaStream_t)stream;
+    for (auto t : s->trees) OK_TRY(sync_positions(t, st));
     OK_TRY(ensure_build_jobs(s, st));
     DevBuf<uint8_t> scratch;
     OK_TRY(scratch.ensure(build_multi_scratch_bytes(s->n_faces), "cudaMalloc(build scratch)"));
@@ -1061,6 +1105,7 @@ API int oibvh_scene_build(oibvh_scene_t s, void* stream)
             return fail(OIBVH_ERR_UNSUPPORTED, "a scene build needs the same Morton key width for every tree");
     CUDA_TRY(launch_build_multi(s->build_jobs.p, n, s->v_blocks, s->f_blocks, s->vblock_job.p, s->fblock_job.p,
                                 s->n_faces, tree_bits, wide, scratch.p, st));
+    for (auto t : s->trees) OK_TRY(reorder_vertices(t, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     for (auto t : s->trees) t->built = true;
     const int r = oibvh_scene_refit(s, stream);
@@ -1078,10 +1123,13 @@ API int oibvh_scene_transform(oibvh_scene_t s, const float* d_rest_xyzw, const f
     if (((uintptr_t)d_rest_xyzw) % 16) return fail(OIBVH_ERR_ARG, "rest positions must be 16-byte aligned");
     DeviceGuard g(s->device);
     cudaStream_t st = (cudaStream_t)stream;
-    for (auto t : s->trees) t->cur_pos = t->pos4.p;  // the transform writes each tree's own positions
+    for (auto t : s->trees) {  // the transform writes each tree's own positions
+        t->cur_pos = t->pos4.p;
+        t->borrowed = nullptr;
+    }
     OK_TRY(ensure_build_jobs(s, st));
     CUDA_TRY(launch_transform_multi(s->build_jobs.p, (uint32_t)s->trees.size(), s->v_blocks, s->vblock_job.p,
-                                    (const float4*)d_rest_xyzw, d_mats, st));
+                                    (const float4*)d_rest_xyzw, d_mats, false, st));
     return OIBVH_OK;
     GUARD_END
 }
@@ -1292,7 +1340,14 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
     std::memcpy(s->h_pairs.p, plan.pv.data(), np * sizeof(PairView));
     CUDA_TRY(cudaMemcpyAsync(s->pairv.p, s->h_pairs.p, np * sizeof(PairView), cudaMemcpyHostToDevice, st));
     OK_TRY(upload_views(s, st));
-    if (s->frame_rest) OK_TRY(ensure_build_jobs(s, st));
+    if (s->frame_rest) {
+        OK_TRY(ensure_build_jobs(s, st));
+        // the graph reads the rest positions in each tree's vertex order: one
+        // gathered copy now, so that every frame's transform reads them in order
+        OK_TRY(s->frame_rest_tree.ensure(std::max<size_t>(s->n_verts, 1), "cudaMalloc(rest positions)"));
+        CUDA_TRY(launch_gather_rest_multi(s->build_jobs.p, (uint32_t)s->trees.size(), s->v_blocks, s->vblock_job.p,
+                                          s->frame_rest, s->frame_rest_tree.p, st));
+    }
     if (s->frame_refit) OK_TRY(oibvh_scene_refit(s, st));  // refreshes the refit job table
     CUDA_TRY(cudaStreamSynchronize(st));
 
@@ -1325,7 +1380,7 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
     cudaError_t e = cudaSuccess;
     if (s->frame_rest && e == cudaSuccess) {
         e = launch_transform_multi(s->build_jobs.p, (uint32_t)s->trees.size(), s->v_blocks, s->vblock_job.p,
-                                   s->frame_rest, s->frame_mats, st);
+                                   s->frame_rest_tree.p, s->frame_mats, true, st);
         ++kernels;
     }
     if (s->frame_refit && e == cudaSuccess) {

@@ -167,14 +167,19 @@ struct oibvh_tree_s {
     uint32_t nV = 0, nT = 0;
     TreeShape shape{};
     DevBuf<float> xyz;          // staging for positions given as xyz (3 * nV)
-    DevBuf<float4> pos4;        // owned positions in the device layout (x, y, z, 0)
-    const float4* cur_pos = nullptr;  // positions the next refit / detect use (owned or borrowed)
-    DevBuf<uint32_t> tri;       // faces as given (3 * nT)
+    DevBuf<float4> pos4;        // positions in the device layout (x, y, z, 0), in the tree's vertex order
+    const float4* cur_pos = nullptr;  // positions the refit and detect read (pos4)
+    const float4* borrowed = nullptr; // caller's (x, y, z, w) positions, caller's order: copied into pos4 before each refit
+    DevBuf<uint32_t> vperm;     // tree vertex v is the caller's vertex vperm[v] (set by the first build)
+    bool reordered = false;     // vperm holds the map (before the first build: the caller's order)
+    DevBuf<uint32_t> tri;       // faces (3 * nT) in the tree's vertex numbering
     DevBuf<uint4> face;         // Morton-ordered faces (v0, v1, v2, original index)
     DevBuf<float4> box;         // 2 * (size - nT): internal nodes only
     DevBuf<uint32_t> counters;  // refit climbing counters
     bool built = false;
     uint32_t morton_bits = 30;  // 30 (the reference's key) or 63 (21 bits per axis)
+
+    const uint32_t* vmap() const { return reordered ? vperm.p : nullptr; }
 
     RefitJob job() const
     {

@@ -36,6 +36,7 @@ struct BuildJob {
     uint32_t fblock_begin;  // first CTA of this tree in face-chunk launches (256 faces per CTA)
     uint32_t face_off;      // first face of this tree in the global face numbering
     uint32_t vert_off;      // first vertex of this tree in packed rest positions
+    const uint32_t* vperm;  // tree vertex v is the caller's vertex vperm[v] (nullptr: the same order)
 };
 
 // build_kernels.cu
@@ -47,9 +48,23 @@ size_t build_multi_scratch_bytes(uint32_t n_faces);
 cudaError_t launch_build_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, uint32_t f_blocks,
                                const uint32_t* vjob, const uint32_t* fjob, uint32_t n_faces, uint32_t tree_bits,
                                bool wide, void* scratch, cudaStream_t s);
+// rest: packed positions of all jobs in each caller's vertex order (read
+// through the jobs' vperm), or in each tree's order (rest_tree_order), or
+// nullptr (each job's own pos). Writes each job's pos_out.
 cudaError_t launch_transform_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, const uint32_t* vjob,
-                                   const float4* rest, const float* mats, cudaStream_t s);
-cudaError_t launch_xyz_to_pos4(const float* xyz, uint32_t nV, float4* pos, cudaStream_t s);
+                                   const float4* rest, const float* mats, bool rest_tree_order, cudaStream_t s);
+cudaError_t launch_gather_rest_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks, const uint32_t* vjob,
+                                     const float4* rest, float4* out, cudaStream_t s);
+// pos[v] = (xyz of the caller's vertex vperm[v], 0); vperm == nullptr: the same order
+cudaError_t launch_xyz_to_pos4(const float* xyz, const uint32_t* vperm, uint32_t nV, float4* pos, cudaStream_t s);
+// pos[v] = src[vperm[v]] (vperm == nullptr: a copy)
+cudaError_t launch_gather_pos4(const float4* src, const uint32_t* vperm, uint32_t nV, float4* pos, cudaStream_t s);
+// Renumber a built tree's vertices in the order its sorted faces first use
+// them: face records and `tri` get the new indices, `pos` the new order and
+// vperm (nV entries; read first when has_vperm) the new caller-order map.
+size_t reorder_scratch_bytes(uint32_t nV);
+cudaError_t launch_reorder_vertices(uint4* face, uint32_t* tri, uint32_t nT, uint32_t nV, float4* pos,
+                                    uint32_t* vperm, bool has_vperm, void* scratch, cudaStream_t s);
 cudaError_t launch_mesh_bounds(const float4* pos, uint32_t nV, uint32_t* bound_keys, int num_sms, cudaStream_t s);
 // codes_hi != nullptr: 63-bit keys, low 32 bits in codes and high 31 in codes_hi
 cudaError_t launch_leaf_morton(const uint32_t* tri, const float4* pos, uint32_t nT, const uint32_t* bound_keys,

@@ -311,7 +311,7 @@ int oibvh_server_s::launch(Lane& L, std::vector<Query*>& batch)
     CUDA_TRY(cudaMemcpyAsync(L.rjobs.p, L.h_rjobs.p, n * sizeof(RefitJob), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(L.mats.p, L.h_mats.p, 12 * n * sizeof(float), cudaMemcpyHostToDevice, st));
     // a batch has few jobs: the kernels binary-search them (no block maps)
-    CUDA_TRY(launch_transform_multi(L.jobs.p, n, vblocks, nullptr, nullptr, L.mats.p, st));
+    CUDA_TRY(launch_transform_multi(L.jobs.p, n, vblocks, nullptr, nullptr, L.mats.p, false, st));
     CUDA_TRY(launch_refit(L.rjobs.p, n, rblocks, nullptr, L.rcount.p, (size_t)per * n, 0, st));
     L.batch = batch;
     const auto now = Clock::now();

@@ -149,8 +149,10 @@ def test_stream_argument(gpu):
     assert np.array_equal(sc.int_tri_pairs(), g["hits"][0])
 
 
-def test_positions_xyzw_in_place(gpu):
-    """oibvh_tree_set_positions4_device: 16-byte (x, y, z, w) records used in place."""
+def test_positions_xyzw_by_reference(gpu):
+    """oibvh_tree_set_positions4_device: 16-byte (x, y, z, w) records in the
+    caller's vertex order, kept by reference and read again by every refit
+    (the tree's own vertex numbering differs after the build)."""
     import torch
 
     from oibvh_gb300 import DeviceType
@@ -164,6 +166,13 @@ def test_positions_xyzw_in_place(gpu):
     sc.refit()
     sc.detectCollision(DeviceType.GPU0, 4, 3)
     assert np.array_equal(sc.int_tri_pairs(), g["hits"][1])
+    # the same buffers, new contents: the next refit reads them
+    for d, x in zip(dev, g["frames"][1]):
+        d[:, :3].copy_(torch.from_numpy(np.ascontiguousarray(x)).cuda())
+    torch.cuda.synchronize()
+    sc.refit()
+    sc.detectCollision(DeviceType.GPU0, 4, 3)
+    assert np.array_equal(sc.int_tri_pairs(), g["hits"][2])
     # misaligned pointer is refused
     from oibvh_gb300 import OibvhError
 
