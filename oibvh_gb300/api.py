@@ -148,7 +148,8 @@ class OibvhTree:
                                                          _stream_handle(stream)), "oibvh_tree_set_positions_device")
 
     def set_positions4_device(self, d_xyzw_ptr: int) -> None:
-        """Device xyzw positions (16 B per vertex, 16-B aligned), used in place."""
+        """Device xyzw positions (16 B per vertex, 16-B aligned, the caller's vertex
+        order), kept by reference: every following refit reads them."""
         N.check(N.lib().oibvh_tree_set_positions4_device(self._h, ctypes.c_void_p(int(d_xyzw_ptr))),
                 "oibvh_tree_set_positions4_device")
 
