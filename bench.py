@@ -45,8 +45,8 @@ METRIC = "collision queries/s"
 UNIT = "queries/s"
 ENTRY_LEVEL, EXPAND_LEVELS = 4, 3  # src/main.cpp:284
 # DRAM bytes (read + written) per triangle of one k_refit launch, measured with
-# ncu on 64 batched pairs (15,520,000 triangles: 372.7 MB read, 453.8 MB written)
-REFIT_DRAM_BYTES_PER_TRIANGLE = (372.653824e6 + 453.766656e6) / 15520000
+# ncu on 64 batched pairs (15,520,000 triangles: 372.6 MB read, 453.5 MB written)
+REFIT_DRAM_BYTES_PER_TRIANGLE = (372.647936e6 + 453.495552e6) / 15520000
 
 
 def parse():
