@@ -370,9 +370,11 @@ def run_ours(args, rank, world, local):
     ms_e2e, wall_e2e, _ = timed(step_e2e)
     clocks = sampler.stop() if sampler else None
 
-    # dominant HBM kernel (the one-launch refit of both trees) timed alone on the same stream
-    for t, x in zip(trees, dev_frames[0]):
-        t.set_positions4_device(x.data_ptr())
+    # dominant HBM kernel (the one-launch refit of both trees) timed alone on the same stream:
+    # positions converted into the trees' own buffers first, so each refit is the one kernel
+    xyz0 = [x[:, :3].contiguous() for x in dev_frames[0]]
+    for t, x in zip(trees, xyz0):
+        t.set_positions_device(x.data_ptr(), stream=sh)
     rf_s = [torch.cuda.Event(enable_timing=True) for _ in range(20)]
     rf_e = [torch.cuda.Event(enable_timing=True) for _ in range(20)]
     for k in range(20):
