@@ -703,7 +703,7 @@ __global__ void __launch_bounds__(kTopThreads) k_top(DetectArgs a)
 // it holds fewer than 32 pairs. Warps never wait for each other; children
 // that do not fit in the ring spill to the next round's list.
 template <bool kFused>
-__global__ void __launch_bounds__(kDetectThreads) k_walk(DetectArgs a, uint32_t round)
+__global__ void __launch_bounds__(kDetectThreads, 4) k_walk(DetectArgs a, uint32_t round)  // 4 CTAs per SM: 64 registers
 {
     extern __shared__ uint64_t s_front[];  // [warp][walk_ring(cap)]: one ring per warp
     __shared__ uint64_t s_cand[kDetectThreads / 32][kCandBuf];
