@@ -702,8 +702,11 @@ __global__ void __launch_bounds__(kTopThreads) k_top(DetectArgs a)
 // empty). The ring is topped up from the warp's share of the list whenever
 // it holds fewer than 32 pairs. Warps never wait for each other; children
 // that do not fit in the ring spill to the next round's list.
-template <bool kFused>
-__global__ void __launch_bounds__(kDetectThreads, 4) k_walk(DetectArgs a, uint32_t round)  // 4 CTAs per SM: 64 registers
+// kDense: compiled for 4 CTAs per SM (64 registers; the fused form spills a
+// few bytes), used when the grid asks for 4; otherwise the register budget of
+// 3 CTAs per SM (no spills).
+template <bool kFused, bool kDense>
+__global__ void __launch_bounds__(kDetectThreads, kDense ? 4 : 3) k_walk(DetectArgs a, uint32_t round)
 {
     extern __shared__ uint64_t s_front[];  // [warp][walk_ring(cap)]: one ring per warp
     __shared__ uint64_t s_cand[kDetectThreads / 32][kCandBuf];
@@ -1022,16 +1025,27 @@ cudaError_t launch_top(const DetectArgs& a, cudaStream_t s)
 
 static size_t walk_smem(uint32_t cap) { return (size_t)(kDetectThreads / 32) * walk_ring(cap) * 8; }  // one ring per warp
 
+static int walk_sm_count()
+{
+    static int sms[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 1;
+    if (!sms[dev]) cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+    return sms[dev] > 0 ? sms[dev] : 1;
+}
+
 static cudaError_t walk_configure()
 {
     static bool configured[64] = {};
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev >= 0 && dev < 64 && configured[dev]) return cudaSuccess;
-    cudaError_t e =
-        cudaFuncSetAttribute(k_walk<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)walk_smem(kWalkCapMax));
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_walk<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)walk_smem(kWalkCapMax));
+    const int smem = (int)walk_smem(kWalkCapMax);
+    cudaError_t e = cudaFuncSetAttribute(k_walk<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_walk<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_walk<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_walk<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess && dev >= 0 && dev < 64) configured[dev] = true;
     return e;
 }
@@ -1043,8 +1057,15 @@ cudaError_t launch_walk(const DetectArgs& a, uint32_t round, cudaStream_t s)
     cudaError_t e = walk_configure();
     if (e != cudaSuccess) return e;
     note_launches(1);
-    if (a.fuse_narrow) k_walk<true><<<a.grid, kDetectThreads, walk_smem(a.walk_cap), s>>>(a, round);
-    else k_walk<false><<<a.grid, kDetectThreads, walk_smem(a.walk_cap), s>>>(a, round);
+    const size_t smem = walk_smem(a.walk_cap);
+    const bool dense = a.grid > 3u * (uint32_t)walk_sm_count();  // 4 walker CTAs per SM asked for
+    if (a.fuse_narrow) {
+        if (dense) k_walk<true, true><<<a.grid, kDetectThreads, smem, s>>>(a, round);
+        else k_walk<true, false><<<a.grid, kDetectThreads, smem, s>>>(a, round);
+    } else {
+        if (dense) k_walk<false, true><<<a.grid, kDetectThreads, smem, s>>>(a, round);
+        else k_walk<false, false><<<a.grid, kDetectThreads, smem, s>>>(a, round);
+    }
     return cudaGetLastError();
 }
 
@@ -1053,8 +1074,8 @@ int walk_blocks_per_sm(uint32_t walk_cap, bool fused)
     if (walk_configure() != cudaSuccess) return 1;
     int n = 0;
     const cudaError_t e =
-        fused ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_walk<true>, kDetectThreads, walk_smem(walk_cap))
-              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_walk<false>, kDetectThreads, walk_smem(walk_cap));
+        fused ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_walk<true, true>, kDetectThreads, walk_smem(walk_cap))
+              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_walk<false, true>, kDetectThreads, walk_smem(walk_cap));
     if (e != cudaSuccess) return 1;
     return n > 0 ? n : 1;
 }
