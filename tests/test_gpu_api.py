@@ -262,3 +262,35 @@ def test_maximum_tree_size(gpu):
     big = M.Mesh(np.zeros((3, 3), np.float32), np.zeros(((1 << 23) + 1, 3), np.uint32))
     with pytest.raises(OibvhError):
         OibvhTree(big)
+
+
+def test_rebuild_and_scene_build_keep_caller_numbering(gpu):
+    """A tree built twice, then built again by its scene (each build renumbers
+    the vertices on top of the last): sorted faces still come back in the
+    caller's vertex numbering, and positions set afterwards in the caller's
+    order give the oracle's pair sets."""
+    from oibvh_gb300 import DeviceType, OibvhTree, Scene
+
+    g = load_golden("deforming")
+    trees = [OibvhTree(m) for m in g["meshes"]]
+    for t in trees:
+        t.build()
+        t.build()
+    for t, m in zip(trees, g["meshes"]):
+        _, st, perm = Port.oibvh_build(m.xyz, m.tri)
+        f, p = t.sorted_faces()
+        assert np.array_equal(f, st) and np.array_equal(p, perm)
+    sc = Scene()
+    for t in trees:
+        sc.addOibvhTree(t)
+    sc.build()
+    for t, m in zip(trees, g["meshes"]):
+        _, st, _ = Port.oibvh_build(m.xyz, m.tri)
+        assert np.array_equal(t.sorted_faces()[0], st)
+    sc.detectCollision(DeviceType.GPU0, 4, 3)
+    assert np.array_equal(sc.int_tri_pairs(), g["hits"][0])
+    for f, fr in enumerate(g["frames"]):
+        for t, x in zip(trees, fr):
+            t.refit(x)
+        sc.detectCollision(DeviceType.GPU0, 4, 3)
+        assert np.array_equal(sc.int_tri_pairs(), g["hits"][f + 1]), f
