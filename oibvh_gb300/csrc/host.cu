@@ -45,6 +45,7 @@ static int tree_alloc(oibvh_tree_t t)
     // one record more than the faces: traversal reads two sibling leaves' faces as one
     // 32-byte load, and the last leaf's sibling may be virtual (past the end)
     OK_TRY(t->face.ensure((size_t)t->nT + 1, "cudaMalloc(sorted faces)"));
+    OK_TRY(t->vperm.ensure(t->nV, "cudaMalloc(vertex order)"));
     OK_TRY(t->box.ensure(2 * (size_t)std::max(1u, t->shape.size - t->nT), "cudaMalloc(tree)"));
     OK_TRY(t->counters.ensure(refit_counters_per_tree(), "cudaMalloc(counters)"));
     return OIBVH_OK;
@@ -101,14 +102,19 @@ static int sync_positions(oibvh_tree_t t, cudaStream_t s)
 
 // After the faces are sorted: vertices renumbered in the order the sorted
 // faces first use them (faces, `tri`, positions and the caller-order map).
-static int reorder_vertices(oibvh_tree_t t, cudaStream_t s)
+// `scratch` (reorder_scratch_bytes(nV) or more) may be shared by trees
+// renumbered one after another on the same stream; nullptr: a private one.
+static int reorder_vertices(oibvh_tree_t t, cudaStream_t s, void* scratch = nullptr)
 {
-    DevBuf<uint8_t> scratch;
-    OK_TRY(scratch.ensure(reorder_scratch_bytes(t->nV), "cudaMalloc(reorder scratch)"));
+    DevBuf<uint8_t> own;
+    if (!scratch) {
+        OK_TRY(own.ensure(reorder_scratch_bytes(t->nV), "cudaMalloc(reorder scratch)"));
+        scratch = own.p;
+    }
     OK_TRY(t->vperm.ensure(t->nV, "cudaMalloc(vertex order)"));
     CUDA_TRY(launch_reorder_vertices(t->face.p, t->tri.p, t->nT, t->nV, t->pos4.p, t->vperm.p, t->reordered,
-                                     scratch.p, s));
-    CUDA_TRY(cudaStreamSynchronize(s));  // the scratch is freed on return
+                                     scratch, s));
+    if (own.p) CUDA_TRY(cudaStreamSynchronize(s));  // the private scratch is freed on return
     t->reordered = true;
     return OIBVH_OK;
 }
@@ -1105,8 +1111,14 @@ API int oibvh_scene_build(oibvh_scene_t s, void* stream)
             return fail(OIBVH_ERR_UNSUPPORTED, "a scene build needs the same Morton key width for every tree");
     CUDA_TRY(launch_build_multi(s->build_jobs.p, n, s->v_blocks, s->f_blocks, s->vblock_job.p, s->fblock_job.p,
                                 s->n_faces, tree_bits, wide, scratch.p, st));
-    for (auto t : s->trees) OK_TRY(reorder_vertices(t, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
+    {
+        size_t most = 0;
+        for (auto t : s->trees) most = std::max(most, reorder_scratch_bytes(t->nV));
+        DevBuf<uint8_t> rscratch;  // one scratch for every tree: the renumberings run in stream order
+        OK_TRY(rscratch.ensure(most, "cudaMalloc(reorder scratch)"));
+        for (auto t : s->trees) OK_TRY(reorder_vertices(t, st, rscratch.p));
+        CUDA_TRY(cudaStreamSynchronize(st));
+    }
     for (auto t : s->trees) t->built = true;
     const int r = oibvh_scene_refit(s, stream);
     if (r != OIBVH_OK) return r;
