@@ -668,9 +668,18 @@ __global__ void __launch_bounds__(kTopThreads) k_top(DetectArgs a)
         uint64_t* fc = cur ? s_dyn + kTopCap : s_dyn;
         uint64_t* fn = cur ? s_dyn : s_dyn + kTopCap;
         if (c > handoff) {
-            // wide enough: hand the front to the walkers
-            for (uint32_t i = threadIdx.x; i < c; i += kTopThreads) out[i] = fc[i];
-            if (threadIdx.x == 0) *out_cnt = c;
+            // wide enough: hand the front to the walkers, after the children the
+            // last level spilled to the list (a handoff above kTopCap / 4 lets a
+            // level outgrow the buffer); the count is stable: every spill
+            // happened before the last __syncthreads
+            const uint32_t base = *(volatile uint32_t*)out_cnt;
+            const uint32_t room = base < a.work_cap ? min(c, a.work_cap - base) : 0u;
+            for (uint32_t i = threadIdx.x; i < room; i += kTopThreads) out[base + i] = fc[i];
+            __syncthreads();  // every thread has read the count before it moves
+            if (threadIdx.x == 0) {
+                *out_cnt = base + c;
+                if (room < c) atomicOr(a.counts + kCountFlags, (uint32_t)kFlagFrontOverflow);
+            }
             break;
         }
         if (threadIdx.x == 0) s_cnt[cur ^ 1] = 0;

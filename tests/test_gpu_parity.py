@@ -187,3 +187,36 @@ def test_wide_morton_keys_order_and_pair_set(gpu):
     for t, t2 in zip(trees, trees2):
         assert np.array_equal(t.sorted_faces()[1], t2.sorted_faces()[1])
         assert np.array_equal(t.aabb_tree().view(np.uint32), t2.aabb_tree().view(np.uint32))
+
+
+def test_top_walk_handoff_widths_keep_every_pair(gpu):
+    """The single-CTA top walk hands its front to the walkers once it is wider
+    than the handoff width; its front buffer holds 8,192 pairs and a wider
+    level spills to the walkers' list. With a handoff above 2,048 a level of
+    at most `handoff` pairs can have more than 8,192 children, so the front
+    handed over must be appended after the spilled pairs, not written over
+    them. Two nearly coincident spheres give fronts of 5,098 and then 10,253
+    pairs from start level 4: handoffs of 6,000 and 8,000 take that path."""
+    from oibvh_gb300 import DeviceType, OibvhTree, Scene
+    from oibvh_gb300 import meshes as M
+    from tests_support import bvtt_front_widths
+
+    a = M.icosphere(5, 1.0, (0.0, 0.0, 0.0))
+    b = M.icosphere(5, 1.0, (0.01, 0.0, 0.0))
+    widths = bvtt_front_widths(a, b, 4)
+    spills = [h for h in (6000, 8000) if any(w0 <= h and w1 > 8192 for w0, w1 in zip(widths, widths[1:]))]
+    assert spills == [6000, 8000], widths  # the case reaches the spill for both widths
+    want, wc = _oracle_pairs([a, b])
+    trees = [OibvhTree(m) for m in (a, b)]
+    for t in trees:
+        t.build()
+    sc = Scene()
+    for t in trees:
+        sc.addOibvhTree(t)
+    for handoff in (32, 2048, 4096, 6000, 8000, 8192):
+        sc.set_tuning(start_pairs_log2=8, handoff=handoff)  # one pair: start level 4
+        sc.detectCollision(DeviceType.GPU0, 0, 1)
+        got = sc.int_tri_pairs()
+        assert got.shape == want.shape, f"handoff {handoff}: {got.shape[0]} pairs, expected {want.shape[0]}"
+        assert np.array_equal(got, want), f"handoff {handoff}"
+        assert sc.candidate_count() == wc, f"handoff {handoff}"

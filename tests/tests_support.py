@@ -96,3 +96,75 @@ def morton63_order(xyz, tri):
 
     key = (stretch(q[:, 0]) << np.uint64(2)) | (stretch(q[:, 1]) << np.uint64(1)) | stretch(q[:, 2])
     return np.argsort(key, kind="stable").astype(np.uint32)
+
+
+def bvtt_front_widths(ma, mb, start, steps=40):
+    """Widths of the BVTT front, level by level, of the one-level-per-step
+    traversal from the cross product of both trees' nodes at `start`: the
+    number of overlapping node pairs that are not leaf x leaf after each
+    expansion (a leaf stays put while the other side descends). Computed on
+    the oracle's restatement of the GPU tree, so a test can show that a
+    tuning reaches a given front shape."""
+    from oracle.oracle import Port
+
+    def shape(nT):
+        p = 1 << max(0, (nT - 1).bit_length())
+        return p.bit_length() - 1, p - nT
+
+    def virtual_above(L, vl, l):
+        if l == 0:
+            return 0
+        vc = vl >> (L - (l - 1))
+        return (vc << 1) - bin(vc).count("1")
+
+    trees = []
+    for m in (ma, mb):
+        boxes, _, _ = Port.oibvh_build(m.xyz, m.tri)
+        L, vl = shape(m.tri.shape[0])
+        va = np.array([virtual_above(L, vl, l) for l in range(L + 1)], dtype=np.int64)
+        trees.append((boxes, L, vl, va))
+
+    def level(i):
+        return np.floor(np.log2(i + 1)).astype(np.int64)
+
+    def box(t, i):
+        boxes, L, vl, va = t
+        return boxes[i - va[level(i)]]
+
+    def keep(ia, ib):
+        a, b = box(trees[0], ia), box(trees[1], ib)
+        ov = np.all(a[:, :3] <= b[:, 3:], 1) & np.all(a[:, 3:] >= b[:, :3], 1)
+        leaves = (level(ia) == trees[0][1]) & (level(ib) == trees[1][1])
+        m = ov & ~leaves
+        return ia[m], ib[m]
+
+    def children(t, i):
+        _, L, vl, _ = t
+        li = level(i)
+        leaf = li == L
+        first = np.where(leaf, i, 2 * i + 1)
+        nl = np.minimum(li + 1, L)
+        right = (np.int64(2) << nl) - 2 - (vl >> (L - nl))
+        return first, np.where(leaf, 1, np.minimum(2, right - first + 1))
+
+    ea, eb = min(start, trees[0][1]), min(start, trees[1][1])
+    na = (1 << ea) - (trees[0][2] >> (trees[0][1] - ea))
+    nb = (1 << eb) - (trees[1][2] >> (trees[1][1] - eb))
+    ia = np.repeat((1 << ea) - 1 + np.arange(na, dtype=np.int64), nb)
+    ib = np.tile((1 << eb) - 1 + np.arange(nb, dtype=np.int64), na)
+    ia, ib = keep(ia, ib)
+    out = [int(ia.shape[0])]
+    for _ in range(steps):
+        if ia.shape[0] == 0:
+            break
+        fa, ca = children(trees[0], ia)
+        fb, cb = children(trees[1], ib)
+        xa, xb = [], []
+        for x in (0, 1):
+            for y in (0, 1):
+                m = (x < ca) & (y < cb)
+                xa.append((fa + x)[m])
+                xb.append((fb + y)[m])
+        ia, ib = keep(np.concatenate(xa), np.concatenate(xb))
+        out.append(int(ia.shape[0]))
+    return out
