@@ -156,11 +156,15 @@ int oibvh_scene_set_pairs(oibvh_scene_t s, const uint32_t* pairs, uint32_t n_pai
  * product of the nodes at entry_level (clamped to each tree's leaf level),
  * with the triangle test fused into the traversal. The pair set does not
  * depend on entry_level or expand_levels (they only shape the reference's
- * work): entry_level sets the initial front as in the reference;
- * expand_levels is validated (1..16) but this traversal always descends one
- * level per step and tests each child pair before queueing it, which visits
- * a subset of the pairs the reference visits. Blocking: returns once the
- * pair count is known. */
+ * work): entry_level sets the initial front as in the reference.
+ * expand_levels is validated (1..16) and otherwise has NO effect here: not on
+ * the result, not on the work done. The reference expands 2^e x 2^e children
+ * of every front pair unconditionally (src/cuda/collide.cu:165-176); this
+ * traversal always descends one level per step and tests each child pair
+ * before queueing it, which visits a subset of the pairs the reference
+ * visits, so a caller porting detectCollision(GPU0, 4, 3) gets no tuning
+ * from it (oibvh_scene_set_tuning / oibvh_scene_autotune shape the work
+ * instead). Blocking: returns once the pair count is known. */
 int oibvh_scene_detect(oibvh_scene_t s, int device_type, uint32_t entry_level, uint32_t expand_levels, void* stream);
 
 /* The two halves of detect (src/cuda/scene.cu:270-311 and :382-423):
@@ -354,10 +358,10 @@ int oibvh_server_destroy(oibvh_server_t s);
 /* Collision detection for ONE mesh pair (tree a against tree b) that
  * allocates nothing: no device memory, no pinned host memory. This entry
  * point has no counterpart in the reference; it exists for callers that must
- * not allocate while they run: a frame loop with a hard budget (cudaMalloc
- * synchronises the whole device), an application whose device memory belongs
- * to an outside pool allocator, or work issued while a CUDA graph capture in
- * global mode is under way on another stream (cudaMalloc is illegal then).
+ * not allocate while they run: a frame loop with a hard time budget (cudaMalloc
+ * may synchronise the whole device and take an unbounded time), or an
+ * application whose device memory is all reserved up front by an outside pool
+ * allocator, so that a library may not make allocations of its own.
  *
  * The traversal runs the same kernels as oibvh_scene_detect over a fixed
  * scratch area compiled into the library: about 4 MB of device memory held on
@@ -369,15 +373,18 @@ int oibvh_server_destroy(oibvh_server_t s);
  *
  * Inputs: two built trees on the same device (created beforehand). Output:
  * up to out_cap records {0, 1, triA, triB} (original face indices; 0 and 1
- * name a and b) written to the DEVICE buffer d_out4; *n_hits receives the
- * number of colliding pairs, also when it exceeds out_cap (then the call
- * returns OIBVH_ERR_OVERFLOW). Blocking.
+ * name a and b) written to the DEVICE buffer d_out4, which must be 16-byte
+ * aligned (else OIBVH_ERR_ARG); *n_hits receives the number of colliding
+ * pairs, also when it exceeds out_cap (then the call returns
+ * OIBVH_ERR_OVERFLOW). Blocking.
  *
  * The first call on a device resolves the scratch address (cudaGetSymbolAddress
- * with that device current) and caches it: make that first call before any
- * stream capture. All calls share the one scratch area and overwrite it;
- * calls whose GPU work overlaps (different host threads or streams) race and
- * must be serialised by the caller. */
+ * with that device current) and caches it with the id of the device's
+ * context: make that first call before any stream capture. A call in a new
+ * context (after cudaDeviceReset) resolves it again. All calls share the one
+ * scratch area and overwrite it (the counters are cleared at the start of
+ * each call); calls whose GPU work overlaps (different host threads or
+ * streams) race and must be serialised by the caller. */
 int oibvh_pair_detect_noalloc(oibvh_tree_t a, oibvh_tree_t b, uint32_t entry_level, uint32_t* d_out4,
                               uint32_t out_cap, uint32_t* n_hits, void* stream);
 

@@ -2,22 +2,24 @@
 // allocates no memory at all, neither on the device nor pinned on the host.
 //
 // Who needs it: callers that must not allocate while they run. A physics or
-// robotics step with a hard frame budget cannot afford cudaMalloc's implicit
-// device-wide synchronisation; an application whose device memory is owned
-// by an outside pool allocator may not create allocations of its own; code
-// issued while another stream is being captured into a CUDA graph in global
-// capture mode may not call cudaMalloc at all. oibvh_scene_detect grows its
-// queues on demand; this entry point instead runs the same traversal kernels
-// over a fixed scratch area that lives in this file.
+// robotics step with a hard frame budget cannot afford cudaMalloc, which may
+// synchronise the whole device and take an unbounded time; an application
+// whose device memory is owned by an outside pool allocator (all of it
+// reserved up front) may not create allocations of its own.
+// oibvh_scene_detect grows its queues on demand; this entry point instead
+// runs the same traversal kernels over a fixed scratch area that lives in
+// this file.
 //
 // The scratch is a file-scope __device__ array: every GPU that loads the
 // library holds it (kNoAllocBytes, about 4 MB) until the process exits. Host
 // code cannot use the array's name as a device address, so the first call on
-// a device (with that device current) resolves the address once with
-// cudaGetSymbolAddress and caches it; make that first call before any stream
-// capture. Every call shares the one array: the counters are cleared at the
-// start of each call, and calls whose GPU work overlaps (several host threads,
-// or several streams) race on it and must be serialised by the caller.
+// a device (with that device current) resolves the address with
+// cudaGetSymbolAddress and caches it together with the id of the device's
+// context; make that first call before any stream capture. A later call in a
+// new context (after cudaDeviceReset) resolves it again. Every call shares
+// the one array: the counters are cleared at the start of each call, and
+// calls whose GPU work overlaps (several host threads, or several streams)
+// race on it and must be serialised by the caller.
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -51,18 +53,41 @@ namespace {
 
 std::mutex g_scratch_mu;
 unsigned char* g_scratch_addr[64] = {};
+unsigned long long g_scratch_ctx[64] = {};  // id of the context the address belongs to
 
-// Device address of g_noalloc_scratch on `dev` (the current device).
+// cuCtxGetId through the runtime's driver entry point (no link to libcuda).
+typedef int (*CtxGetIdFn)(void* ctx, unsigned long long* id);
+
+// Id of the current context (0 when it cannot be read).
+unsigned long long current_context_id()
+{
+    static CtxGetIdFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return (CtxGetIdFn) nullptr;
+        return (CtxGetIdFn)f;
+    }();
+    unsigned long long id = 0;
+    if (!fn || fn(nullptr, &id) != 0) return 0;
+    return id;
+}
+
+// Device address of g_noalloc_scratch on `dev` (the current device, its
+// context already initialised by the caller).
 int scratch_address(int dev, unsigned char** out)
 {
     if (dev < 0 || dev >= 64) return noalloc_fail(OIBVH_ERR_UNSUPPORTED, "device index above 63");
+    const unsigned long long ctx = current_context_id();
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
+    if (!g_scratch_addr[dev] || ctx != g_scratch_ctx[dev]) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess)
             return noalloc_fail(OIBVH_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
         g_scratch_addr[dev] = (unsigned char*)p;
+        g_scratch_ctx[dev] = current_context_id();
     }
     *out = g_scratch_addr[dev];
     return OIBVH_OK;
@@ -87,6 +112,8 @@ extern "C" __attribute__((visibility("default"))) int oibvh_pair_detect_noalloc(
     try {
         if (!a || !b || !n_hits) return noalloc_fail(OIBVH_ERR_ARG, "a, b or n_hits is NULL");
         if (out_cap && !d_out4) return noalloc_fail(OIBVH_ERR_ARG, "d_out4 is NULL");
+        if (((uintptr_t)d_out4) % 16)
+            return noalloc_fail(OIBVH_ERR_ARG, "d_out4 must be 16-byte aligned (the kernels store 16-byte records)");
         *n_hits = 0;
         NoAllocHeader h;
         std::memset(&h, 0, sizeof(h));

@@ -90,3 +90,8 @@ def test_extension_argument_errors_need_no_gpu():
     # the allocation-free detect
     n = ctypes.c_uint32()
     assert L.oibvh_pair_detect_noalloc(None, None, 0, None, 0, ctypes.byref(n), None) == N.ERR_ARG
+    # a misaligned output buffer is refused before either handle is read (the
+    # handles here are never dereferenced)
+    fake = ctypes.c_void_p(64)
+    assert L.oibvh_pair_detect_noalloc(fake, fake, 0, ctypes.c_void_p(0x1008), 16, ctypes.byref(n), None) == N.ERR_ARG
+    assert b"16-byte aligned" in L.oibvh_last_error()

@@ -1,12 +1,11 @@
 """oibvh_pair_detect_noalloc, the allocation-free detect, against oibvh_scene_detect.
 
 The allocation-free entry point is for callers that may not allocate while they
-run: a frame loop with a hard time budget (cudaMalloc synchronises the whole
-device), an application whose device memory belongs to an outside pool
-allocator, or work issued while a CUDA graph capture in global mode is under
-way on another stream. It walks the same kernels over a fixed scratch area
-compiled into the library, so its pair set must equal the growing-queue
-detect's bit for bit. Two calls in a row (with a refit in between) also show
+run: a frame loop with a hard time budget (cudaMalloc may synchronise the whole
+device and take an unbounded time), or an application whose device memory is
+all reserved by an outside pool allocator. It walks the same kernels over a
+fixed scratch area compiled into the library, so its pair set must equal the
+growing-queue detect's bit for bit. Two calls in a row (with a refit in between) also show
 that the shared scratch left by one call does not leak into the next.
 
 This file is named so that pytest collects it last.
