@@ -1,15 +1,16 @@
 #!/usr/bin/env bash
 # ORACLE — test infrastructure only.
-# Compiles the reference's own CPU collision path, from the reference sources
-# where they lie, into oracle/_ref/libref_cpu.so. Needs the reference checkout
-# (default /root/reference, override with OIBVH_REFERENCE) and g++; it does not
-# use the reference's CMake build. Flags: -O2 -DNDEBUG (the reference asserts
+# Compiles the reference's own CPU collision path, unmodified, into
+# oracle/_ref/libref_cpu.so. Sources: the reference checkout named by
+# OIBVH_REFERENCE, else the copy stage_ref.sh made under baseline/_ref/oibvh
+# (for hosts without the checkout). Needs g++; it does not use the
+# reference's CMake build. Flags: -O2 -DNDEBUG (the reference asserts
 # on triangle 0, src/cpu/simpleCollide.cpp:91-92, and is built release) and
 # -ffp-contract=off (no fused multiply-add, as MSVC's default /fp:precise and
 # x86-64 without FMA give the reference's own build).
 set -euo pipefail
-REF="${OIBVH_REFERENCE:-/root/reference}"
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+REF="${OIBVH_REFERENCE:-$(dirname "$HERE")/baseline/_ref/oibvh}"
 OUT="$HERE/_ref"
 CUDA_INC="${CUDA_HOME:-/usr/local/cuda}/include"
 if [ ! -f "$REF/src/cpu/simpleBVH.cpp" ]; then

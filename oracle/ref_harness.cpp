@@ -18,6 +18,7 @@
  * own aabb_box_t::overlap and triangleIntersect.
  */
 #include <iostream>
+#include <mutex>
 #include <sstream>
 #include <stack>
 #include <vector>
@@ -136,11 +137,16 @@ public:
 
 namespace
 {
+/* std::cout is process-wide: the redirect is held under a lock, so that
+ * scenes built on several threads at once (untimed set-up of the benches)
+ * never restore each other's buffers. */
+std::mutex g_cout_mu;
 struct QuietCout
 {
+    std::lock_guard<std::mutex> lock;
     std::streambuf* saved;
     std::ostringstream sink;
-    QuietCout() : saved(std::cout.rdbuf(sink.rdbuf())) {}
+    QuietCout() : lock(g_cout_mu), saved(std::cout.rdbuf(sink.rdbuf())) {}
     ~QuietCout() { std::cout.rdbuf(saved); }
 };
 } // namespace
