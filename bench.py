@@ -47,6 +47,11 @@ ENTRY_LEVEL, EXPAND_LEVELS = 4, 3  # src/main.cpp:284
 # DRAM bytes (read + written) per triangle of one k_refit launch, measured with
 # ncu on 64 batched pairs (15,520,000 triangles: 372.6 MB read, 453.5 MB written)
 REFIT_DRAM_BYTES_PER_TRIANGLE = (372.647936e6 + 453.495552e6) / 15520000
+# DRAM bytes per vertex of one k_transform_multi launch (ncu, 64 batched pairs)
+TRANSFORM_DRAM_BYTES_PER_VERTEX = (124.3e6 + 77.5e6) / 7766272
+# DRAM bytes of the traversal kernels (k_init_front, k_top, k_walk) of one frame
+# per BVTT pair tested (ncu, 64 batched pairs); None until measured
+TRAVERSAL_DRAM_BYTES_PER_TESTED = None
 
 
 def parse():
@@ -63,10 +68,30 @@ def parse():
     ap.add_argument("--pairs", type=int, default=512, help="mesh pairs of the batched workload")
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-subconfigs", action="store_true",
+                    help="batched: leave out the served and precision sub-objects")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = {"batched": 60, "deforming": 100}.get(args.workload, 30)
     return args
+
+
+REF_NOTE = {
+    "reference": "the reference's own CPU path (src/cpu/simpleBVH.cpp, src/utils/utils.cpp), compiled unmodified on "
+                 "this host from the sources staged under baseline/_ref",
+    "port": "the reference's sources are not staged on this host; the oracle's C restatement of its CPU path runs",
+}
+
+
+def reference_cpu():
+    """The reference's own CPU path where it is built on this host
+    (oracle/_ref, compiled unmodified from its sources), else the oracle's C
+    restatement of it: (class with add_mesh / set_positions / detect, kind)."""
+    from oracle.oracle import Port, Reference
+
+    if Reference.available():
+        return Reference, "reference"
+    return Port, "port"
 
 
 def max_over_ranks(values, dist, device):
@@ -471,12 +496,12 @@ def load_peaks():
 def cpu_baseline_sample(w, seconds, threads=1):
     """The oracle port (C restatement of the reference CPU path) on this host:
     one frame = refit both SimpleBVHs to the frame's positions + detect."""
-    from oracle.oracle import Port
+    Ref, ref_kind = reference_cpu()
 
     frames = jitter_frames(w, 64, seed=99)
 
     def worker(out, idx0, stride, deadline):
-        p = Port()
+        p = Ref()
         for m in w.meshes:
             p.add_mesh(m.xyz, m.tri)
         n = 0
@@ -501,7 +526,7 @@ def cpu_baseline_sample(w, seconds, threads=1):
         t.join()
     el = time.perf_counter() - t0
     n = sum(out)
-    return {"value": round(n / el, 3), "unit": UNIT, "cores": threads, "kind": "port",
+    return {"value": round(n / el, 3), "unit": UNIT, "cores": threads, "kind": ref_kind,
             "sample": f"{n} frames of the workload (refit both + detect) in {el:.1f} s, build included"}
 
 
@@ -511,13 +536,13 @@ def run_reference(args, rank, world):
         return None
     w = make_workload(args.workload)
     threads = os.cpu_count() or 1
-    from oracle.oracle import Port
+    Ref, ref_kind = reference_cpu()
 
     frames = jitter_frames(w, max(8, threads), seed=5)
     scenes = [None] * threads
 
     def setup(k):
-        p = Port()
+        p = Ref()
         for m in w.meshes:
             p.add_mesh(m.xyz, m.tri)
         scenes[k] = p
@@ -556,10 +581,10 @@ def run_reference(args, rank, world):
         "data": "synthetic (seeded noise icospheres, per-frame Gaussian jitter)",
         "config": workload_config(w, args, {"parallelism": f"{threads} host threads, one frame each per step"}),
         "impl": "reference",
-        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": ref_kind,
                          "sample": f"{q} frames (refit both + detect), {threads} per step"},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the reference's C++ sources are not on the GPU host; the C restatement of its CPU path runs instead",
+        "note": REF_NOTE[ref_kind],
     }
 
 
@@ -695,7 +720,19 @@ def run_ours_batched(args, rank, world, local):
     plain_ms = ev0.elapsed_time(ev1) / plain_frames
     plain_hits = sum(ps.getIntTriPairCount() for ps in plain)
 
-    # dominant HBM kernel: the one-launch refit of all 1024 trees, timed alone
+    # every stage of the frame timed on its own: the same kernels, enqueued
+    # stage by stage with CUDA events between the stages (L2 flushed before each)
+    profs = []
+    for k in range(10):
+        flush.fill_(k & 255)
+        mats.copy_(mats_all[k % n_frames])
+        profs.append(sc.profile_frame(stream=sh))
+    prof = {key: statistics.median(p_[key] for p_ in profs)
+            for key in ("transform_ms", "refit_ms", "start_ms", "walk_ms", "narrow_ms")}
+    prof_hits, prof_cands = sc.getIntTriPairCount(), sc.candidate_count()
+    prof_tested = sc.stats()["nodes_tested"]
+
+    # the one-launch refit of all 1024 trees, also timed alone
     rf = []
     for k in range(10):
         flush.fill_(k & 255)
@@ -725,6 +762,7 @@ def run_ours_batched(args, rank, world, local):
     refit_bytes = sum(12 * m.n_vertices + 12 * m.n_triangles + 24 * tree_size(m.n_triangles) for m in w.rest)
     peaks = load_peaks()
     achieved = refit_bytes / (refit_ms / 1e3) / 1e9
+    rooflines = frame_rooflines(w, prof, prof_cands, prof_hits, prof_tested, peaks, refit_ms, refit_bytes, ms_dev / K)
     line = {
         "metric": "collision queries/s (mesh pairs through refit + broad + narrow)",
         "value": round(value, 1),
@@ -756,13 +794,7 @@ def run_ours_batched(args, rank, world, local):
         "e2e": {"value": round(queries / (ms_e2e / 1e3), 1), "unit": "queries/s",
                 "h2d_bytes_per_step": 48 * len(w.rest), "d2h_bytes_per_step": int(d2h[0] / max(1, K)),
                 "ms_per_step": round(ms_e2e / K, 4)},
-        "roofline": {"kernel": "k_refit (one launch: all 1024 trees, leaf boxes + every level)", "bound": "hbm",
-                     "achieved": round(achieved, 1), "peak": peaks[0], "unit": "GB/s",
-                     "frac": round(achieved / peaks[0], 4), "peak_source": peaks[1],
-                     "algorithmic_bytes_per_launch": refit_bytes, "launch_ms": round(refit_ms, 4),
-                     "traffic": int(REFIT_DRAM_BYTES_PER_TRIANGLE * w.info["triangles_total"]),
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_refit on 64 batched "
-                                       "pairs (15.52 M triangles), scaled by the triangle count"},
+        "roofline": rooflines,
         "gpu_launches": int(launches),
         "clocks": clocks,
         "setup_s": round(setup_s, 2),
@@ -771,6 +803,62 @@ def run_ours_batched(args, rank, world, local):
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_batched(w, args.cpu_seconds)
     return line
+
+
+def _tree_size(T):
+    """Real nodes of an oibvh tree of T leaves (include/cuda/oibvh.cuh:56-59)."""
+    p2 = 1 << (T - 1).bit_length()
+    return 2 * T + bin(p2 - T).count("1") - 1
+
+
+def frame_rooflines(w, prof, cands, hits, tested, peaks, refit_alone_ms, refit_bytes, ms_step):
+    """HBM roofline of every stage of one batched frame, each timed inside
+    the frame (CUDA events between the stages). Algorithmic bytes follow the
+    compulsory-traffic rule of the reference layout: refit 12 B per vertex +
+    12 B per face read and 24 B per tree node written; traversal 24 B per
+    node of both trees of every pair (broad phase in), 8 B per candidate out,
+    104 B per candidate in (narrow phase: the candidate, two faces, six
+    vertices) and 8 B per hit out; transform 16 B in + 16 B out per vertex.
+    `traffic` is the DRAM bytes ncu measured for the stage on a smaller case,
+    scaled by the units it processes; `frac_dram` = traffic / time / peak."""
+    peak, src = peaks
+    tri_total = w.info["triangles_total"]
+    broad = sum(24 * (_tree_size(w.rest[a].n_triangles) + _tree_size(w.rest[b].n_triangles)) for a, b in w.pairs)
+    stages = {
+        "transform": ("k_transform_multi (one launch: every vertex of every mesh)",
+                      sum(32 * m.n_vertices + 48 for m in w.rest), prof["transform_ms"],
+                      TRANSFORM_DRAM_BYTES_PER_VERTEX * w.info["vertices_total"],
+                      "16 B in + 16 B out per vertex, 48 B of matrix per mesh"),
+        "refit": ("k_refit (one launch: all trees, leaf boxes + every level)", refit_bytes, prof["refit_ms"],
+                  REFIT_DRAM_BYTES_PER_TRIANGLE * tri_total,
+                  "12 B per vertex + 12 B per face read, 24 B per tree node written (the reference layout; this "
+                  "layout stores internal nodes only, 32 B each, and reads 16 B per face and per vertex)"),
+        "traversal": ("k_init_front + k_top + k_walk rounds (broad phase, fused 17-axis narrow phase)",
+                      broad + 112 * cands + 8 * hits, prof["start_ms"] + prof["walk_ms"],
+                      TRAVERSAL_DRAM_BYTES_PER_TESTED * tested if TRAVERSAL_DRAM_BYTES_PER_TESTED else None,
+                      "24 B per node of both trees of every pair + 112 B per candidate + 8 B per hit"),
+    }
+    out = {}
+    for name, (kern, b, ms, traffic, rule) in stages.items():
+        ach = b / (ms / 1e3) / 1e9
+        e = {"kernel": kern, "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+             "frac": round(ach / peak, 4), "traffic": int(traffic) if traffic else None,
+             "algorithmic_bytes_per_launch": int(b), "launch_ms": round(ms, 4),
+             "share_of_step": round(ms / ms_step, 4), "bytes_rule": rule}
+        if traffic:
+            e["frac_dram"] = round(traffic / (ms / 1e3) / 1e9 / peak, 4)
+        out[name] = e
+    out["refit"]["frac_effective"] = out["refit"]["frac"]
+    out["refit"]["alone_ms"] = round(refit_alone_ms, 4)
+    dominant = max(("transform", "refit", "traversal"), key=lambda k: out[k]["launch_ms"])
+    top = dict(out[dominant])
+    top.update({"stage": dominant, "peak_source": src, "stages": out,
+                "stages_ms_sum": round(sum(prof[k] for k in ("transform_ms", "refit_ms", "start_ms", "walk_ms")), 4),
+                "stages_cover_of_step": round(sum(out[k]["launch_ms"] for k in out) / ms_step, 4),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per stage on 64 batched pairs "
+                                  "(profiles/), scaled by the units the stage processes",
+                "bvtt_pairs_tested": tested, "candidates": cands, "hits": hits})
+    return top
 
 
 def _sample_pairs(w, n):
@@ -787,14 +875,14 @@ def _sample_positions(w, sample, frames):
 def cpu_baseline_batched(w, seconds, threads=1, frames=(1, 2, 3, 4)):
     """The oracle port on this host: for a fixed sample of the pairs, refit both
     SimpleBVHs to the frame's transformed positions and detect, pair by pair."""
-    from oracle.oracle import Port
+    Ref, ref_kind = reference_cpu()
 
     sample = _sample_pairs(w, 32)
     pos = _sample_positions(w, sample, frames)
     scenes = []
     for p in sample:
         a, b = w.pairs[p]
-        ps = Port()
+        ps = Ref()
         ps.add_mesh(pos[frames[0]][a], w.rest[a].tri)
         ps.add_mesh(pos[frames[0]][b], w.rest[b].tri)
         scenes.append((ps, a, b))
@@ -811,7 +899,7 @@ def cpu_baseline_batched(w, seconds, threads=1, frames=(1, 2, 3, 4)):
         if n % len(scenes) == 0:
             k += 1
     el = time.perf_counter() - t0
-    return {"value": round(n / el, 3), "unit": "queries/s", "cores": threads, "kind": "port",
+    return {"value": round(n / el, 3), "unit": "queries/s", "cores": threads, "kind": ref_kind,
             "sample": f"{n} pair queries (refit both + detect) over a fixed sample of {len(sample)} pairs, {el:.1f} s"}
 
 
@@ -820,7 +908,7 @@ def run_reference_batched(args, rank, world):
     bounded sample of the workload, 8 pair queries per thread."""
     if rank != 0:
         return None
-    from oracle.oracle import Port
+    Ref, ref_kind = reference_cpu()
 
     w = batched_workload(args)
     threads = os.cpu_count() or 1
@@ -836,7 +924,7 @@ def run_reference_batched(args, rank, world):
         lst = []
         for p in per[k]:
             a, b = w.pairs[p]
-            ps = Port()
+            ps = Ref()
             ps.add_mesh(pos[1][a], w.rest[a].tri)
             ps.add_mesh(pos[1][b], w.rest[b].tri)
             lst.append((ps, a, b))
@@ -879,10 +967,10 @@ def run_reference_batched(args, rank, world):
         "config": {"workload": w.name, **w.info,
                    "parallelism": f"{threads} host threads; each step: {len(sample)} sampled pairs, 8 per thread"},
         "impl": "reference",
-        "cpu_baseline": {"value": round(value, 3), "unit": "queries/s", "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": round(value, 3), "unit": "queries/s", "cores": threads, "kind": ref_kind,
                          "sample": f"{q} pair queries over a fixed sample of {len(sample)} of the {len(w.pairs)} pairs"},
         "e2e": {"value": round(value, 3), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the reference's C++ sources are not on the GPU host; the C restatement of its CPU path runs instead",
+        "note": REF_NOTE[ref_kind],
     }
 
 
@@ -1064,7 +1152,37 @@ def run_ours_precision(args, rank, world, local):
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_precision(w, got_f, args.cpu_seconds)
+        line["fp64_oracle"] = fp64_oracle_all_pairs(w, got_f, min(16, os.cpu_count() or 1))
     return line
+
+
+def fp64_oracle_all_pairs(w, got, threads):
+    """The all-FP64 oracle over EVERY pair of the workload on `threads` host
+    threads (outside any timed region): pair-set mismatches against the
+    GPU's FP64-filtered result, summed over the pairs."""
+    from oracle.oracle import Port
+
+    mism = [0] * len(w.pairs)
+
+    def work(k):
+        for p in range(k, len(w.pairs), threads):
+            a, b = w.pairs[p]
+            port = Port()
+            port.add_mesh(w.meshes[a].xyz, w.meshes[a].tri)
+            port.add_mesh(w.meshes[b].xyz, w.meshes[b].tri)
+            h64, _ = port.detect(fp64=True)
+            mine = got[(got[:, 0] == a) & (got[:, 1] == b)][:, 2:]
+            mism[p] = len({tuple(r) for r in h64[:, 2:].tolist()} ^ {tuple(r) for r in mine.tolist()})
+
+    t0 = time.perf_counter()
+    ts = [threading.Thread(target=work, args=(k,)) for k in range(threads)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    return {"fp64_oracle_mismatches": int(sum(mism)), "pairs_checked": len(w.pairs),
+            "pairs_with_mismatches": sum(1 for x in mism if x), "threads": threads,
+            "seconds": round(time.perf_counter() - t0, 1)}
 
 
 def cpu_baseline_precision(w, got, seconds):
@@ -1101,7 +1219,7 @@ def run_reference_precision(args, rank, world):
     reference's arithmetic) on every host core, 1 pair per thread per step."""
     if rank != 0:
         return None
-    from oracle.oracle import Port
+    Ref, ref_kind = reference_cpu()
     from oibvh_gb300 import workloads as W
 
     w = W.sheets(64, 256)
@@ -1110,7 +1228,7 @@ def run_reference_precision(args, rank, world):
     ports = []
     for p in sample:
         a, b = w.pairs[p]
-        port = Port()
+        port = Ref()
         port.add_mesh(w.meshes[a].xyz, w.meshes[a].tri)
         port.add_mesh(w.meshes[b].xyz, w.meshes[b].tri)
         ports.append((port, a, b))
@@ -1142,7 +1260,7 @@ def run_reference_precision(args, rank, world):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded sine sheets)",
             "config": {"workload": w.name, **w.info, "parallelism": f"{len(ports)} host threads, 1 pair each"},
             "impl": "reference",
-            "cpu_baseline": {"value": round(value, 3), "unit": "queries/s", "cores": len(ports), "kind": "port",
+            "cpu_baseline": {"value": round(value, 3), "unit": "queries/s", "cores": len(ports), "kind": ref_kind,
                              "sample": f"{q} pair queries (refit both + detect, float test) over {len(ports)} pairs"},
             "e2e": {"value": round(value, 3), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -1283,7 +1401,7 @@ def run_ours_serving(args, rank, world, local):
 def cpu_baseline_serving(w, seconds):
     """The reference CPU path per query on 1 core: B's SimpleBVH refit to the
     transformed positions, then detect against A (both meshes resident)."""
-    from oracle.oracle import Port
+    Ref, ref_kind = reference_cpu()
     from oibvh_gb300 import workloads as W
 
     ab, mats = w.queries(64, seed=777)
@@ -1294,7 +1412,7 @@ def cpu_baseline_serving(w, seconds):
     for k in range(64):
         a, b = int(ab[k, 0]), int(ab[k, 1])
         if (a, b) not in ports:
-            p = Port()
+            p = Ref()
             p.add_mesh(w.meshes[a].xyz, w.meshes[a].tri)
             p.add_mesh(w.meshes[b].xyz, w.meshes[b].tri)
             ports[(a, b)] = p
@@ -1308,7 +1426,7 @@ def cpu_baseline_serving(w, seconds):
         del ports[(a, b)]
         if time.perf_counter() - t0 > seconds:
             break
-    return {"value": round(n / t_run, 3), "unit": "queries/s", "cores": 1, "kind": "port",
+    return {"value": round(n / t_run, 3), "unit": "queries/s", "cores": 1, "kind": ref_kind,
             "sample": f"{n} queries of the stream (refit B + detect; BVH build and the transform untimed), "
                       f"{t_run:.1f} s"}
 
@@ -1318,7 +1436,7 @@ def run_reference_serving(args, rank, world):
     independently, one per thread, refit + detect each."""
     if rank != 0:
         return None
-    from oracle.oracle import Port
+    Ref, ref_kind = reference_cpu()
     from oibvh_gb300 import workloads as W
 
     w = W.serving(args.pool)
@@ -1327,7 +1445,7 @@ def run_reference_serving(args, rank, world):
     ports = []
     for k in range(threads):
         a, b = int(ab[k, 0]), int(ab[k, 1])
-        p = Port()
+        p = Ref()
         p.add_mesh(w.meshes[a].xyz, w.meshes[a].tri)
         p.add_mesh(w.meshes[b].xyz, w.meshes[b].tri)
         ports.append((p, W.rigid_apply(w.meshes[b].xyz, mats[k])))
@@ -1358,9 +1476,98 @@ def run_reference_serving(args, rank, world):
             "data": "synthetic (seeded noise icospheres, seeded query stream)",
             "config": {"workload": w.name, **w.info, "parallelism": f"{threads} host threads, 1 query each"},
             "impl": "reference",
-            "cpu_baseline": {"value": round(value, 3), "unit": "queries/s", "cores": threads, "kind": "port",
+            "cpu_baseline": {"value": round(value, 3), "unit": "queries/s", "cores": threads, "kind": ref_kind,
                              "sample": f"{args.steps * threads} queries (refit B + detect), {threads} per step"},
             "e2e": {"value": round(value, 3), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# --------------------------------------------------------------------------- sub-configs of the default line
+def _sub_args(args, **kw):
+    sub = argparse.Namespace(**vars(args))
+    for k, v in kw.items():
+        setattr(sub, k, v)
+    return sub
+
+
+def _free_device_memory():
+    import gc
+
+    gc.collect()
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
+    except Exception:
+        pass
+
+
+SERVED_RATES = "10000,30000,60000,100000"
+
+
+def subconfigs_ours(args, local):
+    """The serving config (2,000-mesh pool, Poisson sweep) and the precision
+    config (64 sheet pairs, FP64-filtered test) as compact sub-objects of the
+    default line: served queries/s with p50/p99 and served vs plain; frame and
+    per-query p50/p99, the FP64 oracle's mismatch count over all 64 pairs
+    and the float/FP64 disagreements. Run on this rank's GPU alone."""
+    out = {}
+    _free_device_memory()
+    sv = run_ours_serving(_sub_args(args, rates=SERVED_RATES, pool=2000, budget_gb=16.0,
+                                    cpu_seconds=min(args.cpu_seconds, 4.0)), 0, 1, local)
+    out["served"] = {
+        "workload": sv["config"]["workload"], "pool_triangles": sv["config"]["triangles_total"],
+        "memory_budget_gb": sv["config"]["memory_budget_gb"],
+        "queries_per_s": sv["value"],
+        "sweep": [{"offered_per_s": r["offered_per_s"], "queries": r["queries"],
+                   "throughput_per_s": r["throughput_per_s"], "p50_ms": r["latency_ms"]["p50"],
+                   "p99_ms": r["latency_ms"]["p99"], "max_ms": r["latency_ms"]["max"],
+                   "mean_batch": r["mean_batch"]} for r in sv["sweep"]],
+        "plain_one_at_a_time": sv["plain_one_at_a_time"], "served_over_plain": sv["served_over_plain"],
+        "latency_how": "per query: (submit - scheduled Poisson arrival) + queue + service, host clock",
+        "gpu_launches": sv["gpu_launches"], "clocks": sv["clocks"],
+    }
+    if "cpu_baseline" in sv:
+        out["served"]["cpu_baseline"] = sv["cpu_baseline"]
+    _free_device_memory()
+    pr = run_ours_precision(_sub_args(args, pairs=64, steps=100, warmup=5,
+                                      cpu_seconds=min(args.cpu_seconds, 4.0)), 0, 1, local)
+    f = pr["fp64_filter"]
+    out["precision"] = {
+        "workload": pr["config"]["workload"], "queries_per_s": pr["value"], "frame_ms": pr["ms_per_step"],
+        "frames": pr["steps"], "frame_latency_ms": pr["frame_latency_ms"],
+        "plain_single_pair": pr["plain_single_pair"], "batched_over_plain": pr["batched_over_plain"],
+        "fp64_oracle_mismatches": pr.get("fp64_oracle", {}).get("fp64_oracle_mismatches"),
+        "fp64_oracle": pr.get("fp64_oracle"),
+        "fp32_vs_fp64_disagreements": int(sum(f["fp32_vs_fp64_disagreements_per_pair"])),
+        "pairs_with_disagreements": f["pairs_with_disagreements"],
+        "candidates": f["candidates"], "fp64_candidates": f["fp64_candidates"], "fp64_axes": f["fp64_axes"],
+        "fp32_frame": pr["fp32_frame"], "e2e": pr["e2e"], "gpu_launches": pr["gpu_launches"],
+        "clocks": pr["clocks"], "tuning": pr["config"]["tuning"],
+    }
+    if "cpu_baseline" in pr:
+        out["precision"]["cpu_baseline"] = pr["cpu_baseline"]
+    out["targets"] = {
+        "batched_and_served_over_plain_min": 5.0,
+        "p99_ms_max": 2.0,
+        "p99_ms_precision_frame": pr["frame_latency_ms"]["p99"],
+        "p99_ms_precision_per_query": pr["plain_single_pair"]["latency_ms"]["p99"],
+        "p99_ms_served": {str(int(r["offered_per_s"])): r["latency_ms"]["p99"] for r in sv["sweep"]},
+        "fp64_oracle_mismatches": out["precision"]["fp64_oracle_mismatches"],
+        "reading": "config numbering is ambiguous (1-based: batching + precision; 0-based: precision + serving); "
+                   "both are reported",
+    }
+    return out
+
+
+def subconfigs_reference(args):
+    """The reference CPU path on the same sub-configs, on every host core."""
+    sub = _sub_args(args, steps=3, warmup=1)
+    sv = run_reference_serving(sub, 0, 1)
+    pr = run_reference_precision(sub, 0, 1)
+    pick = ("value", "unit", "cpu_baseline", "config", "ms_per_step")
+    return {"served": {k: sv[k] for k in pick}, "precision": {k: pr[k] for k in pick}}
 
 
 def main():
@@ -1374,6 +1581,8 @@ def main():
         line = {"batched": run_ours_batched, "precision": run_ours_precision,
                 "serving": run_ours_serving}.get(
             args.workload, run_ours)(args, rank, world, local)
+    if line is not None and args.workload == "batched" and not args.no_subconfigs:
+        line.update(subconfigs_reference(args) if args.impl == "reference" else subconfigs_ours(args, local))
     if line is not None:
         print(json.dumps(line), flush=True)
 

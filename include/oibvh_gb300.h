@@ -60,6 +60,17 @@ int oibvh_version(void);
 /* Kernels this library has launched so far in this process (all devices). */
 uint64_t oibvh_get_launch_count(void);
 
+/* Test hook for the out-of-memory paths (no counterpart in the reference,
+ * which ignores every CUDA error, include/cuda/utils.cuh:6-34): the n-th
+ * device or pinned-host allocation this library attempts from now on (n = 0:
+ * the next one) fails as cudaMalloc would with cudaErrorMemoryAllocation, but
+ * without calling CUDA, so OIBVH_ERR_OOM can be driven on a healthy device;
+ * the hook is then off again. n < 0 switches it off. Process-wide; inert
+ * unless called. */
+int oibvh_debug_fail_alloc_after(int64_t n);
+/* Device and pinned-host allocations attempted so far (process-wide). */
+uint64_t oibvh_debug_alloc_attempts(void);
+
 /* ------------------------------------------------------------------ tree */
 
 /* OibvhTree::OibvhTree(std::shared_ptr<Mesh>) + setup()
@@ -251,6 +262,25 @@ int oibvh_scene_capture_frame(oibvh_scene_t s, uint32_t entry_level, uint32_t ex
                               const float* d_rest_xyzw, const float* d_mats, void* stream);
 int oibvh_scene_launch_frame(oibvh_scene_t s, void* stream);
 int oibvh_scene_finish_frame(oibvh_scene_t s, void* stream);
+
+/* Per-stage device times of one frame (milliseconds, CUDA events on the
+ * caller's stream between the stages). */
+typedef struct oibvh_frame_profile {
+    float transform_ms;    /* rigid transforms of every tree (0 without) */
+    float refit_ms;        /* the one refit launch (0 without) */
+    float start_ms;        /* start front + top walk */
+    float walk_ms;         /* every captured walk round */
+    float narrow_ms;       /* precision mode's narrow phase (0 in float mode) */
+    uint32_t walk_rounds;  /* walk rounds launched */
+    uint32_t kernels;      /* kernels launched */
+} oibvh_frame_profile;
+/* One frame of the captured work (oibvh_scene_capture_frame) enqueued stage
+ * by stage instead of as the graph, with CUDA events between the stages, so
+ * that each stage's device time can be read; the same kernels with the same
+ * arguments. Blocking; afterwards the results are those of the frame, as
+ * after oibvh_scene_finish_frame. No counterpart in the reference, whose
+ * stages print their own timers (src/cuda/scene.cu:299,320,419). */
+int oibvh_scene_profile_frame(oibvh_scene_t s, void* stream, oibvh_frame_profile* out);
 
 /* Arithmetic of the triangle test. OIBVH_PRECISION_FP32 (the default) is
  * the reference's float test, operation for operation (src/utils/utils.cpp:71-169):

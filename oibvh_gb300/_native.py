@@ -67,6 +67,18 @@ class ServerStats(ctypes.Structure):
         "arena_bytes", "arena_used_bytes", "arena_peak_bytes", "queued")]
 
 
+class FrameProfile(ctypes.Structure):
+    _fields_ = [
+        ("transform_ms", ctypes.c_float),
+        ("refit_ms", ctypes.c_float),
+        ("start_ms", ctypes.c_float),
+        ("walk_ms", ctypes.c_float),
+        ("narrow_ms", ctypes.c_float),
+        ("walk_rounds", ctypes.c_uint32),
+        ("kernels", ctypes.c_uint32),
+    ]
+
+
 class Tuning(ctypes.Structure):
     _fields_ = [
         ("start_pairs_log2", ctypes.c_uint32),
@@ -85,6 +97,8 @@ SIGNATURES = [
     ("oibvh_last_error", ctypes.c_char_p, []),
     ("oibvh_version", ctypes.c_int, []),
     ("oibvh_get_launch_count", _u64, []),
+    ("oibvh_debug_fail_alloc_after", ctypes.c_int, [ctypes.c_int64]),
+    ("oibvh_debug_alloc_attempts", _u64, []),
     ("oibvh_tree_create", ctypes.c_int, [_f32p, _u32, _u32p, _u32, ctypes.c_int, ctypes.POINTER(_vp)]),
     ("oibvh_tree_create_copy", ctypes.c_int, [_vp, _f32p, _u32, ctypes.POINTER(_vp)]),
     ("oibvh_tree_build", ctypes.c_int, [_vp, _vp]),
@@ -124,6 +138,7 @@ SIGNATURES = [
     ("oibvh_scene_set_precision", ctypes.c_int, [_vp, ctypes.c_int]),
     ("oibvh_scene_get_precision", ctypes.c_int, [_vp]),
     ("oibvh_scene_get_stats", ctypes.c_int, [_vp, ctypes.POINTER(DetectStats)]),
+    ("oibvh_scene_profile_frame", ctypes.c_int, [_vp, _vp, ctypes.POINTER(FrameProfile)]),
     ("oibvh_scene_destroy", ctypes.c_int, [_vp]),
     ("oibvh_pair_detect_noalloc", ctypes.c_int, [_vp, _vp, _u32, _vp, _u32, _u32p, _vp]),
     ("oibvh_server_create", ctypes.c_int, [ctypes.c_int, _u64, _u32, _u32, ctypes.POINTER(_vp)]),

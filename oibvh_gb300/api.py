@@ -280,6 +280,15 @@ class Scene:
     def finish_frame(self, stream=None) -> None:
         N.check(N.lib().oibvh_scene_finish_frame(self._h, _stream_handle(stream)), "oibvh_scene_finish_frame")
 
+    def profile_frame(self, stream=None) -> dict:
+        """One frame stage by stage with CUDA events between the stages:
+        device milliseconds of transform, refit, start (start front + top
+        walk), walk (every walk round) and narrow; the results are the frame's."""
+        p = N.FrameProfile()
+        N.check(N.lib().oibvh_scene_profile_frame(self._h, _stream_handle(stream), ctypes.byref(p)),
+                "oibvh_scene_profile_frame")
+        return {k: (float(getattr(p, k)) if k.endswith("_ms") else int(getattr(p, k))) for k, _ in p._fields_}
+
     def getIntTriPairCount(self) -> int:
         return int(N.lib().oibvh_scene_get_int_tri_pair_count(self._h))
 

@@ -623,6 +623,226 @@ __global__ void __launch_bounds__(256) k_gather_faces_multi(const BuildJob* __re
         make_uint4(__ldg(job.tri + 3 * (size_t)o), __ldg(job.tri + 3 * (size_t)o + 1), __ldg(job.tri + 3 * (size_t)o + 2), o);
 }
 
+// ---------------------------------------------------------------------------
+// Multi-tree vertex renumbering: the order of launch_reorder_vertices (used
+// vertices in the order of their first use by the sorted faces, then unused
+// ones in their previous order) for every tree at once, without a sort. A
+// vertex's new index is the number of first uses before its own: each
+// 256-face block counts the corners that are a first use, one scan over the
+// block counts gives every block its offset, and the tree's own offset is
+// that of its first block (blocks never straddle trees). Unused vertices are
+// ranked the same way over 256-vertex blocks, after the tree's used ones.
+// Global vertex index g = vert_off + v; six launches for any number of trees.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kNoUse = 0xffffffffu;
+
+struct RenumberScratch {
+    uint32_t* first;     // n_verts: first-use slot (3 f + corner) of each vertex
+    uint32_t* inv;       // n_verts: new index of each vertex
+    float4* pos_new;     // n_verts
+    uint32_t* vperm_new; // n_verts
+    uint32_t* fscan;     // f_blocks + 1: first uses per face block, then their exclusive scan
+    uint32_t* vscan;     // v_blocks + 1: unused vertices per vertex block, then the scan
+};
+
+__host__ __device__ inline size_t rn_align(size_t b) { return (b + 255) / 256 * 256; }
+
+__host__ __device__ inline RenumberScratch rn_scratch(void* base, uint32_t n_verts, uint32_t v_blocks,
+                                                      uint32_t f_blocks)
+{
+    uint8_t* p = (uint8_t*)base;
+    RenumberScratch r;
+    const size_t a4 = rn_align((size_t)n_verts * 4);
+    r.first = (uint32_t*)p;
+    r.inv = (uint32_t*)(p + a4);
+    r.vperm_new = (uint32_t*)(p + 2 * a4);
+    r.pos_new = (float4*)(p + 3 * a4);
+    r.fscan = (uint32_t*)(p + 3 * a4 + rn_align((size_t)n_verts * 16));
+    r.vscan = r.fscan + rn_align((size_t)(f_blocks + 1) * 4) / 4;
+    return r;
+}
+
+__global__ void __launch_bounds__(256) k_rn_init(const BuildJob* __restrict__ jobs, const uint32_t* __restrict__ vjob,
+                                                 uint32_t* __restrict__ first)
+{
+    const BuildJob& job = jobs[__ldg(vjob + blockIdx.x)];
+    const uint32_t v = (blockIdx.x - job.vblock_begin) * 256u + threadIdx.x;
+    if (v < job.nV) first[job.vert_off + v] = kNoUse;
+}
+
+__global__ void __launch_bounds__(256) k_rn_first_use(const BuildJob* __restrict__ jobs,
+                                                      const uint32_t* __restrict__ fjob, uint32_t* __restrict__ first)
+{
+    const BuildJob& job = jobs[__ldg(fjob + blockIdx.x)];
+    const uint32_t f = (blockIdx.x - job.fblock_begin) * 256u + threadIdx.x;
+    if (f >= job.nT) return;
+    const uint4 r = job.face_out[f];
+    uint32_t* fj = first + job.vert_off;
+    atomicMin(fj + r.x, 3u * f);
+    atomicMin(fj + r.y, 3u * f + 1u);
+    atomicMin(fj + r.z, 3u * f + 2u);
+}
+
+// This thread's count (first-use corners of its face, or 1 for an unused
+// vertex) for the block kinds below: CTAs [0, f_blocks) are face blocks,
+// the rest vertex blocks.
+struct RnItem {
+    const BuildJob* job;
+    bool face_block;
+    uint32_t i;      // face or vertex of the job
+    uint32_t cnt;
+    uint32_t mask;   // face blocks: which corners are first uses
+    uint4 r;         // face blocks: the face record
+};
+__device__ __forceinline__ RnItem rn_item(const BuildJob* jobs, const uint32_t* vjob, const uint32_t* fjob,
+                                          uint32_t f_blocks, const uint32_t* first)
+{
+    RnItem it{};
+    it.face_block = blockIdx.x < f_blocks;
+    if (it.face_block) {
+        it.job = jobs + __ldg(fjob + blockIdx.x);
+        it.i = (blockIdx.x - it.job->fblock_begin) * 256u + threadIdx.x;
+        if (it.i < it.job->nT) {
+            it.r = it.job->face_out[it.i];
+            const uint32_t* fj = first + it.job->vert_off;
+            it.mask = (__ldg(fj + it.r.x) == 3u * it.i ? 1u : 0u) | (__ldg(fj + it.r.y) == 3u * it.i + 1u ? 2u : 0u) |
+                      (__ldg(fj + it.r.z) == 3u * it.i + 2u ? 4u : 0u);
+            it.cnt = __popc(it.mask);
+        }
+    } else {
+        const uint32_t b = blockIdx.x - f_blocks;
+        it.job = jobs + __ldg(vjob + b);
+        it.i = (b - it.job->vblock_begin) * 256u + threadIdx.x;
+        if (it.i < it.job->nV) it.cnt = __ldg(first + it.job->vert_off + it.i) == kNoUse ? 1u : 0u;
+    }
+    return it;
+}
+
+__global__ void __launch_bounds__(256) k_rn_count(const BuildJob* __restrict__ jobs, const uint32_t* __restrict__ vjob,
+                                                  const uint32_t* __restrict__ fjob, uint32_t f_blocks,
+                                                  RenumberScratch sc)
+{
+    __shared__ uint32_t sh[8];
+    const RnItem it = rn_item(jobs, vjob, fjob, f_blocks, sc.first);
+    uint32_t tot;
+    block_exclusive_scan(it.cnt, &tot, sh);
+    if (threadIdx.x == 0) {
+        if (it.face_block) sc.fscan[blockIdx.x] = tot;
+        else sc.vscan[blockIdx.x - f_blocks] = tot;
+    }
+}
+
+// CTA 0 scans fscan[0..f_blocks), CTA 1 vscan[0..v_blocks), in place
+// (exclusive; the total goes to entry n), 4 entries per thread per step.
+__global__ void __launch_bounds__(256) k_rn_scan(RenumberScratch sc, uint32_t f_blocks, uint32_t v_blocks)
+{
+    __shared__ uint32_t sh[8];
+    uint32_t* a = blockIdx.x == 0 ? sc.fscan : sc.vscan;
+    const uint32_t n = blockIdx.x == 0 ? f_blocks : v_blocks;
+    uint32_t carry = 0;
+    for (uint32_t s = 0; s < n; s += 4 * 256) {
+        const uint32_t i0 = s + 4 * threadIdx.x;
+        uint32_t v[4], sum = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            v[k] = i0 + k < n ? a[i0 + k] : 0u;
+            sum += v[k];
+        }
+        uint32_t tot;
+        uint32_t ex = carry + block_exclusive_scan(sum, &tot, sh);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (i0 + k < n) a[i0 + k] = ex;
+            ex += v[k];
+        }
+        carry += tot;
+    }
+    if (threadIdx.x == 0) a[n] = carry;
+}
+
+// New index of every vertex; positions and the caller-order map in the new
+// order into the scratch.
+__global__ void __launch_bounds__(256) k_rn_assign(const BuildJob* __restrict__ jobs, const uint32_t* __restrict__ vjob,
+                                                   const uint32_t* __restrict__ fjob, uint32_t f_blocks,
+                                                   RenumberScratch sc)
+{
+    __shared__ uint32_t sh[8];
+    const RnItem it = rn_item(jobs, vjob, fjob, f_blocks, sc.first);
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan(it.cnt, &tot, sh);
+    if (it.cnt == 0) return;
+    const BuildJob& job = *it.job;
+    const uint32_t vo = job.vert_off;
+    const uint32_t f_first = job.fblock_begin, f_end = job.fblock_begin + (job.nT + 255u) / 256u;
+    auto place = [&](uint32_t v, uint32_t nv) {
+        sc.inv[vo + v] = nv;
+        sc.pos_new[vo + nv] = __ldg(job.pos_out + v);
+        sc.vperm_new[vo + nv] = job.vperm ? __ldg(job.vperm + v) : v;
+    };
+    if (it.face_block) {
+        uint32_t rank = sc.fscan[blockIdx.x] - sc.fscan[f_first] + ex;
+        if (it.mask & 1u) place(it.r.x, rank++);
+        if (it.mask & 2u) place(it.r.y, rank++);
+        if (it.mask & 4u) place(it.r.z, rank);
+    } else {
+        const uint32_t used = sc.fscan[f_end] - sc.fscan[f_first];
+        const uint32_t b = blockIdx.x - f_blocks;
+        place(it.i, used + sc.vscan[b] - sc.vscan[job.vblock_begin] + ex);
+    }
+}
+
+// Faces and `tri` to the new numbering; positions and the map copied back
+// into each tree's own buffers.
+__global__ void __launch_bounds__(256) k_rn_apply(const BuildJob* __restrict__ jobs, const uint32_t* __restrict__ vjob,
+                                                  const uint32_t* __restrict__ fjob, uint32_t f_blocks,
+                                                  RenumberScratch sc)
+{
+    if (blockIdx.x < f_blocks) {
+        const BuildJob& job = jobs[__ldg(fjob + blockIdx.x)];
+        const uint32_t f = (blockIdx.x - job.fblock_begin) * 256u + threadIdx.x;
+        if (f >= job.nT) return;
+        const uint32_t* inv = sc.inv + job.vert_off;
+        uint4 r = job.face_out[f];
+        r.x = __ldg(inv + r.x);
+        r.y = __ldg(inv + r.y);
+        r.z = __ldg(inv + r.z);
+        job.face_out[f] = r;
+        uint32_t* t = job.tri_rw + 3 * (size_t)f;
+        t[0] = __ldg(inv + t[0]);
+        t[1] = __ldg(inv + t[1]);
+        t[2] = __ldg(inv + t[2]);
+    } else {
+        const uint32_t b = blockIdx.x - f_blocks;
+        const BuildJob& job = jobs[__ldg(vjob + b)];
+        const uint32_t v = (b - job.vblock_begin) * 256u + threadIdx.x;
+        if (v >= job.nV) return;
+        job.pos_out[v] = sc.pos_new[job.vert_off + v];
+        job.vperm_out[v] = sc.vperm_new[job.vert_off + v];
+    }
+}
+
+size_t reorder_multi_scratch_bytes(uint32_t n_verts, uint32_t v_blocks, uint32_t f_blocks)
+{
+    return 3 * rn_align((size_t)n_verts * 4) + rn_align((size_t)n_verts * 16) + rn_align((size_t)(f_blocks + 1) * 4) +
+           rn_align((size_t)(v_blocks + 1) * 4);
+}
+
+cudaError_t launch_reorder_vertices_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks,
+                                          uint32_t f_blocks, const uint32_t* vjob, const uint32_t* fjob,
+                                          uint32_t n_verts, void* scratch, cudaStream_t s)
+{
+    if (n_jobs == 0 || v_blocks == 0 || f_blocks == 0) return cudaSuccess;
+    const RenumberScratch sc = rn_scratch(scratch, n_verts, v_blocks, f_blocks);
+    note_launches(6);
+    k_rn_init<<<v_blocks, 256, 0, s>>>(d_jobs, vjob, sc.first);
+    k_rn_first_use<<<f_blocks, 256, 0, s>>>(d_jobs, fjob, sc.first);
+    k_rn_count<<<f_blocks + v_blocks, 256, 0, s>>>(d_jobs, vjob, fjob, f_blocks, sc);
+    k_rn_scan<<<2, 256, 0, s>>>(sc, f_blocks, v_blocks);
+    k_rn_assign<<<f_blocks + v_blocks, 256, 0, s>>>(d_jobs, vjob, fjob, f_blocks, sc);
+    k_rn_apply<<<f_blocks + v_blocks, 256, 0, s>>>(d_jobs, vjob, fjob, f_blocks, sc);
+    return cudaGetLastError();
+}
+
 // Rigid transforms of every tree: pos = M * rest, M a row-major 3x4 matrix per
 // tree, each product and sum rounded on its own: x' = ((m0 x + m1 y) + m2 z) + m3.
 // Four 256-vertex blocks per CTA (vertex v of block k at thread v): the four

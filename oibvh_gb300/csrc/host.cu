@@ -35,6 +35,8 @@ void note_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relax
 
 namespace oibvh_host {
 thread_local std::string g_last_error;
+std::atomic<int64_t> g_fail_alloc{-1};
+std::atomic<uint64_t> g_alloc_attempts{0};
 }  // namespace oibvh_host
 
 static int tree_alloc(oibvh_tree_t t)
@@ -209,6 +211,8 @@ struct oibvh_scene_s {
     const float* frame_mats = nullptr;
     PinnedBuf<uint32_t> h_frame_counts;
     cudaStream_t capture_stream = nullptr;  // private stream the frame is captured on
+    DetectArgs frame_args{};                // the captured detect's arguments
+    uint32_t frame_front0 = 0;              // its start cross product
 
     uint64_t hit_count = 0;
     uint64_t cand_count = 0;
@@ -560,6 +564,14 @@ API const char* oibvh_last_error(void) { return g_last_error.c_str(); }
 API int oibvh_version(void) { return 100; }
 
 API uint64_t oibvh_get_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+API int oibvh_debug_fail_alloc_after(int64_t n)
+{
+    g_fail_alloc.store(n < 0 ? -1 : n, std::memory_order_relaxed);
+    return OIBVH_OK;
+}
+
+API uint64_t oibvh_debug_alloc_attempts(void) { return g_alloc_attempts.load(std::memory_order_relaxed); }
 
 API int oibvh_tree_create(const float* xyz, uint32_t n_vertices, const uint32_t* tri, uint32_t n_triangles, int device,
                           oibvh_tree_t* out)
@@ -1055,6 +1067,8 @@ int ensure_build_jobs(oibvh_scene_s* s, cudaStream_t st)
         j.face_off = fo;
         j.vert_off = vo;
         j.vperm = t->vmap();
+        j.vperm_out = t->vperm.p;
+        j.tri_rw = t->tri.p;
         vb += (t->nV + 255) / 256;
         fb += (t->nT + 255) / 256;
         if ((uint64_t)fo + t->nT > 0xffffffffull || (uint64_t)vo + t->nV > 0xffffffffull)
@@ -1101,8 +1115,10 @@ API int oibvh_scene_build(oibvh_scene_t s, void* stream)
     cudaStream_t st = (cudaStream_t)stream;
     for (auto t : s->trees) OK_TRY(sync_positions(t, st));
     OK_TRY(ensure_build_jobs(s, st));
-    DevBuf<uint8_t> scratch;
-    OK_TRY(scratch.ensure(build_multi_scratch_bytes(s->n_faces), "cudaMalloc(build scratch)"));
+    DevBuf<uint8_t> scratch;  // the build stages, then (in stream order) the renumbering
+    OK_TRY(scratch.ensure(std::max(build_multi_scratch_bytes(s->n_faces),
+                                   reorder_multi_scratch_bytes(s->n_verts, s->v_blocks, s->f_blocks)),
+                          "cudaMalloc(build scratch)"));
     const uint32_t n = (uint32_t)s->trees.size();
     const uint32_t tree_bits = n <= 1 ? 0u : ilog2(next_pow2(n));
     const bool wide = s->trees[0]->morton_bits == 63;
@@ -1111,15 +1127,15 @@ API int oibvh_scene_build(oibvh_scene_t s, void* stream)
             return fail(OIBVH_ERR_UNSUPPORTED, "a scene build needs the same Morton key width for every tree");
     CUDA_TRY(launch_build_multi(s->build_jobs.p, n, s->v_blocks, s->f_blocks, s->vblock_job.p, s->fblock_job.p,
                                 s->n_faces, tree_bits, wide, scratch.p, st));
-    {
-        size_t most = 0;
-        for (auto t : s->trees) most = std::max(most, reorder_scratch_bytes(t->nV));
-        DevBuf<uint8_t> rscratch;  // one scratch for every tree: the renumberings run in stream order
-        OK_TRY(rscratch.ensure(most, "cudaMalloc(reorder scratch)"));
-        for (auto t : s->trees) OK_TRY(reorder_vertices(t, st, rscratch.p));
-        CUDA_TRY(cudaStreamSynchronize(st));
+    // every tree's vertices renumbered in the order its sorted faces first use
+    // them: six launches for all trees
+    CUDA_TRY(launch_reorder_vertices_multi(s->build_jobs.p, n, s->v_blocks, s->f_blocks, s->vblock_job.p,
+                                           s->fblock_job.p, s->n_verts, scratch.p, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    for (auto t : s->trees) {
+        t->reordered = true;
+        t->built = true;
     }
-    for (auto t : s->trees) t->built = true;
     const int r = oibvh_scene_refit(s, stream);
     if (r != OIBVH_OK) return r;
     CUDA_TRY(cudaStreamSynchronize(st));
@@ -1312,6 +1328,58 @@ API int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t rep
 
 namespace {
 
+// The frame's work on `st`, as captured: [transform of every tree], [refit
+// of every tree], the detect of every pair (start front, top walk, the
+// captured walk rounds), [the precision narrow phase], the counters to the
+// host. `ev` (optional, 6 events) brackets the stages for per-stage times:
+// ev[0] | transform | ev[1] | refit | ev[2] | start + top | ev[3] | walk
+// rounds | ev[4] | narrow | ev[5].
+cudaError_t enqueue_frame(oibvh_scene_s* s, cudaStream_t st, cudaEvent_t* ev, uint32_t* kernels)
+{
+    const DetectArgs& a = s->frame_args;
+    uint32_t k = 0;
+    cudaError_t e = cudaSuccess;
+    auto mark = [&](int i) {
+        if (ev && e == cudaSuccess) e = cudaEventRecord(ev[i], st);
+    };
+    mark(0);
+    if (s->frame_rest && e == cudaSuccess) {
+        e = launch_transform_multi(s->build_jobs.p, (uint32_t)s->trees.size(), s->v_blocks, s->vblock_job.p,
+                                   s->frame_rest_tree.p, s->frame_mats, true, st);
+        ++k;
+    }
+    mark(1);
+    if (s->frame_refit && e == cudaSuccess) {
+        e = launch_refit(s->refit_jobs.p, (uint32_t)s->trees.size(), s->refit_blocks, s->refit_block_job.p,
+                         s->refit_counters.p, refit_counters_per_tree() * s->trees.size(), s->tune_refit_log, st);
+        ++k;
+    }
+    mark(2);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->counts.p, 0, kCountTotal * sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = launch_init_front(a, s->frame_front0, st);
+    if (e == cudaSuccess) e = launch_top(a, st);
+    k += 2;
+    mark(3);
+    for (uint32_t r = 1; r <= s->frame_rounds && e == cudaSuccess; ++r) {
+        e = launch_walk(a, r, st);
+        ++k;
+    }
+    mark(4);
+    if (s->precision && e == cudaSuccess) {
+        DetectArgs n = a;
+        n.fuse_narrow = 1;
+        n.grid = sm_count(s->device) * 8;
+        e = launch_narrow(n, st);
+        ++k;
+    }
+    mark(5);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s->h_frame_counts.p, s->counts.p, kCountTotal * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                            st);
+    if (kernels) *kernels = k;
+    return e;
+}
+
 // Capture [transform] + refit + detect of every pair (one pass) into a graph.
 int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
 {
@@ -1382,6 +1450,9 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
     a.walk_cap = s->tune_walk_cap;
     a.precision = s->precision;
 
+    s->frame_args = a;
+    s->frame_front0 = (uint32_t)plan.front0;
+
     // capture on a private non-blocking stream (the legacy default stream
     // cannot be captured); the graph is launched on the caller's stream
     if (!s->capture_stream) CUDA_TRY(cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking));
@@ -1389,35 +1460,7 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
     cudaGraph_t graph = nullptr;
     CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     uint32_t kernels = 0;
-    cudaError_t e = cudaSuccess;
-    if (s->frame_rest && e == cudaSuccess) {
-        e = launch_transform_multi(s->build_jobs.p, (uint32_t)s->trees.size(), s->v_blocks, s->vblock_job.p,
-                                   s->frame_rest_tree.p, s->frame_mats, true, st);
-        ++kernels;
-    }
-    if (s->frame_refit && e == cudaSuccess) {
-        e = launch_refit(s->refit_jobs.p, (uint32_t)s->trees.size(), s->refit_blocks, s->refit_block_job.p,
-                         s->refit_counters.p, refit_counters_per_tree() * s->trees.size(), s->tune_refit_log, st);
-        ++kernels;
-    }
-    if (e == cudaSuccess) e = cudaMemsetAsync(s->counts.p, 0, kCountTotal * sizeof(uint32_t), st);
-    if (e == cudaSuccess) e = launch_init_front(a, (uint32_t)plan.front0, st);
-    if (e == cudaSuccess) e = launch_top(a, st);
-    kernels += 2;
-    for (uint32_t r = 1; r <= s->frame_rounds && e == cudaSuccess; ++r) {
-        e = launch_walk(a, r, st);
-        ++kernels;
-    }
-    if (s->precision && e == cudaSuccess) {
-        DetectArgs n = a;
-        n.fuse_narrow = 1;
-        n.grid = sm_count(s->device) * 8;
-        e = launch_narrow(n, st);
-        ++kernels;
-    }
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(s->h_frame_counts.p, s->counts.p, kCountTotal * sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                            st);
+    cudaError_t e = enqueue_frame(s, st, nullptr, &kernels);
     const cudaError_t e2 = cudaStreamEndCapture(st, &graph);
     if (e != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
@@ -1503,5 +1546,38 @@ API int oibvh_scene_finish_frame(oibvh_scene_t s, void* stream)
     s->stats.hits = s->hit_count;
     s->cands_valid = false;
     return OIBVH_OK;
+    GUARD_END
+}
+
+API int oibvh_scene_profile_frame(oibvh_scene_t s, void* stream, oibvh_frame_profile* out)
+{
+    GUARD_BEGIN
+    if (!s || !out) return fail(OIBVH_ERR_ARG, "scene or out is NULL");
+    DeviceGuard g(s->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (s->frame_stale || !s->frame_exec) OK_TRY(capture_frame_impl(s, st));
+    struct Events {
+        cudaEvent_t e[6] = {};
+        ~Events()
+        {
+            for (auto& x : e)
+                if (x) cudaEventDestroy(x);
+        }
+    } ev;
+    for (auto& x : ev.e) CUDA_TRY(cudaEventCreate(&x));
+    uint32_t kernels = 0;
+    CUDA_TRY(enqueue_frame(s, st, ev.e, &kernels));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    float ms[5] = {};
+    for (int i = 0; i < 5; ++i) CUDA_TRY(cudaEventElapsedTime(&ms[i], ev.e[i], ev.e[i + 1]));
+    *out = oibvh_frame_profile{};
+    out->transform_ms = ms[0];
+    out->refit_ms = ms[1];
+    out->start_ms = ms[2];
+    out->walk_ms = ms[3];
+    out->narrow_ms = ms[4];
+    out->walk_rounds = s->frame_rounds;
+    out->kernels = kernels;
+    return oibvh_scene_finish_frame(s, stream);
     GUARD_END
 }

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <string>
 
@@ -16,6 +17,20 @@ namespace oibvh_host {
 
 // Last error message of the calling thread (oibvh_last_error).
 extern thread_local std::string g_last_error;
+
+// Allocation-failure injection (oibvh_debug_fail_alloc_after): -1 = off;
+// n >= 0: the allocation attempt n places ahead (0 = the next one) reports
+// cudaErrorMemoryAllocation without calling CUDA, then the hook is off again.
+extern std::atomic<int64_t> g_fail_alloc;
+extern std::atomic<uint64_t> g_alloc_attempts;  // device + pinned allocation attempts
+inline bool injected_alloc_failure()
+{
+    g_alloc_attempts.fetch_add(1, std::memory_order_relaxed);
+    int64_t c = g_fail_alloc.load(std::memory_order_relaxed);
+    while (c >= 0)
+        if (g_fail_alloc.compare_exchange_weak(c, c - 1, std::memory_order_relaxed)) return c == 0;
+    return false;
+}
 
 inline int fail(int code, const std::string& msg)
 {
@@ -87,7 +102,7 @@ struct DevBuf {
         if (want <= n && p) return OIBVH_OK;
         release();
         if (want == 0) want = 1;
-        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+        cudaError_t e = injected_alloc_failure() ? cudaErrorMemoryAllocation : cudaMalloc(&p, want * sizeof(T));
         if (e != cudaSuccess) {
             p = nullptr;
             cudaGetLastError();
@@ -101,7 +116,7 @@ struct DevBuf {
     {
         if (want <= n && p) return OIBVH_OK;
         T* q = nullptr;
-        cudaError_t e = cudaMalloc(&q, want * sizeof(T));
+        cudaError_t e = injected_alloc_failure() ? cudaErrorMemoryAllocation : cudaMalloc(&q, want * sizeof(T));
         if (e != cudaSuccess) {
             cudaGetLastError();
             return cuda_fail(e, what);
@@ -143,7 +158,7 @@ struct PinnedBuf {
         p = nullptr;
         n = 0;
         if (want == 0) want = 1;
-        cudaError_t e = cudaMallocHost(&p, want * sizeof(T));
+        cudaError_t e = injected_alloc_failure() ? cudaErrorMemoryAllocation : cudaMallocHost(&p, want * sizeof(T));
         if (e != cudaSuccess) {
             p = nullptr;
             cudaGetLastError();

@@ -37,6 +37,8 @@ struct BuildJob {
     uint32_t face_off;      // first face of this tree in the global face numbering
     uint32_t vert_off;      // first vertex of this tree in packed rest positions
     const uint32_t* vperm;  // tree vertex v is the caller's vertex vperm[v] (nullptr: the same order)
+    uint32_t* vperm_out;    // the tree's map buffer (nV entries), rewritten by the renumbering
+    uint32_t* tri_rw;       // the tree's faces (3 * nT), rewritten by the renumbering (tri, writable)
 };
 
 // build_kernels.cu
@@ -65,6 +67,13 @@ cudaError_t launch_gather_pos4(const float4* src, const uint32_t* vperm, uint32_
 size_t reorder_scratch_bytes(uint32_t nV);
 cudaError_t launch_reorder_vertices(uint4* face, uint32_t* tri, uint32_t nT, uint32_t nV, float4* pos,
                                     uint32_t* vperm, bool has_vperm, void* scratch, cudaStream_t s);
+// The same renumbering for every tree of a multi-tree build, in a fixed
+// number of launches: each job's face_out, tri_rw, pos_out (the positions,
+// read and rewritten) and vperm_out (from vperm, or the identity when nullptr).
+size_t reorder_multi_scratch_bytes(uint32_t n_verts, uint32_t v_blocks, uint32_t f_blocks);
+cudaError_t launch_reorder_vertices_multi(const BuildJob* d_jobs, uint32_t n_jobs, uint32_t v_blocks,
+                                          uint32_t f_blocks, const uint32_t* vjob, const uint32_t* fjob,
+                                          uint32_t n_verts, void* scratch, cudaStream_t s);
 cudaError_t launch_mesh_bounds(const float4* pos, uint32_t nV, uint32_t* bound_keys, int num_sms, cudaStream_t s);
 // codes_hi != nullptr: 63-bit keys, low 32 bits in codes and high 31 in codes_hi
 cudaError_t launch_leaf_morton(const uint32_t* tri, const float4* pos, uint32_t nT, const uint32_t* bound_keys,

@@ -89,6 +89,15 @@ def test_captured_frame_graph_vs_oracle(gpu):
         assert sc.candidate_count() == wc
     # the captured walk rounds cover these frames: none was redone synchronously
     assert sc.stats()["frame_redos"] == 0
+    # the same frame stage by stage (per-stage times): the same pair set
+    mats.copy_(torch.from_numpy(w.matrices(6)))
+    prof = sc.profile_frame()
+    want, wc = _oracle(w.positions(6), [m.tri for m in w.rest], w.pairs)
+    assert np.array_equal(sc.int_tri_pairs(), want) and sc.candidate_count() == wc
+    assert prof["walk_rounds"] >= 3 and prof["kernels"] == 4 + prof["walk_rounds"]
+    for k in ("transform_ms", "refit_ms", "start_ms", "walk_ms"):
+        assert prof[k] > 0.0, k
+    assert prof["narrow_ms"] >= 0.0
 
 
 def test_frame_graph_recovers_from_small_queues(gpu):
@@ -222,3 +231,81 @@ def test_full_batched_workload_parity(gpu):
         want, _ = port.detect()
         got = frame[(frame[:, 0] == a) & (frame[:, 1] == b)][:, 2:]
         assert np.array_equal(got, sort_pairs(want)[:, 2:]), p
+
+
+def _with_unused_vertices(m, rng):
+    """The same mesh with vertices no face uses scattered through its vertex
+    array (and the used ones in a shuffled order)."""
+    from oibvh_gb300 import meshes as M
+
+    nV = m.xyz.shape[0]
+    total = nV + int(rng.integers(1, nV + 2))
+    where = rng.choice(total, nV, replace=False)
+    xyz = rng.uniform(-2.0, 2.0, size=(total, 3)).astype(np.float32)
+    xyz[where] = m.xyz
+    return M.Mesh(xyz, where[m.tri.astype(np.int64)].astype(np.uint32))
+
+
+def test_scene_build_renumbers_meshes_with_unused_vertices(gpu):
+    """A scene build renumbers every tree's vertices in one set of launches
+    (used vertices in first-use order, unused ones after them). Meshes whose
+    vertex arrays hold unused vertices, built twice by their scene, keep the
+    caller's numbering: sorted faces, refits from caller-order positions and
+    pair sets equal the oracle's."""
+    from oibvh_gb300 import DeviceType, OibvhTree, Scene
+    from oibvh_gb300 import meshes as M
+    from tests_support import soup
+
+    rng = np.random.Generator(np.random.PCG64(31))
+    base = [M.noise_displace(M.icosphere(3), 0.05, seed=3), M.icosphere(2, 0.9, (0.4, 0.1, 0.0)),
+            soup(rng, 300, 0.1), M.grid_sheet(12, 1.5, 0.2, 0.5, origin=(-0.7, -0.7, 0.0)), soup(rng, 1, 0.3)]
+    meshes = [_with_unused_vertices(m, rng) for m in base]
+    trees = [OibvhTree(m) for m in meshes]
+    sc = Scene()
+    for t in trees:
+        sc.addOibvhTree(t)
+    sc.build()
+    sc.build()  # a second renumbering on top of the first
+    for t, m in zip(trees, meshes):
+        aabbs, st, perm = Port.oibvh_build(m.xyz, m.tri)
+        f, p = t.sorted_faces()
+        assert np.array_equal(p, perm) and np.array_equal(f, st)
+        assert np.array_equal(t.aabb_tree().view(np.uint32), aabbs.view(np.uint32))
+    sc.detectCollision(DeviceType.GPU0, 4, 1)
+    port = Port()
+    for m in meshes:
+        port.add_mesh(m.xyz, m.tri)
+    want, wc = port.detect()
+    assert np.array_equal(sc.int_tri_pairs(), sort_pairs(want)) and sc.candidate_count() == wc
+    moved = [(m.xyz + rng.normal(scale=2e-3, size=m.xyz.shape)).astype(np.float32) for m in meshes]
+    for t, x in zip(trees, moved):
+        t.set_positions(x)
+    sc.refit()
+    for k, (t, x) in enumerate(zip(trees, moved)):
+        st, _ = t.sorted_faces()
+        assert np.array_equal(t.aabb_tree().view(np.uint32), Port.oibvh_refit(x, st).view(np.uint32)), k
+        port.set_positions(k, x)
+    sc.detectCollision(DeviceType.GPU0, 4, 1)
+    want, wc = port.detect()
+    assert np.array_equal(sc.int_tri_pairs(), sort_pairs(want)) and sc.candidate_count() == wc
+
+
+def test_scene_build_launches_do_not_grow_with_trees(gpu):
+    """Every stage of a scene build, the vertex renumbering included, is one
+    launch for all trees: 3 and 60 trees take the same number of launches
+    (both sort tree ids in one 8-bit radix pass)."""
+    from oibvh_gb300 import OibvhTree, Scene
+    from oibvh_gb300 import _native as N
+    from oibvh_gb300 import meshes as M
+
+    def launches(n):
+        trees = [OibvhTree(M.noise_displace(M.icosphere(2 + k % 3), 0.05, seed=k)) for k in range(n)]
+        sc = Scene()
+        for t in trees:
+            sc.addOibvhTree(t)
+        sc.build()  # first build: tables uploaded
+        before = N.lib().oibvh_get_launch_count()
+        sc.build()
+        return N.lib().oibvh_get_launch_count() - before
+
+    assert launches(3) == launches(60)
