@@ -373,7 +373,7 @@ __device__ __forceinline__ void expand_side(const TreeShape& S, uint32_t ia, uin
 // shared memory and tested 32 at a time, one per lane, so the 17-axis test
 // runs at full SIMT width however sparse the candidates are.
 // ---------------------------------------------------------------------------
-constexpr int kCandBuf = 64;  // <= 31 left over + 32 added per round
+constexpr int kCandBuf = 96;  // <= 31 left over + up to 2 per lane added by one expansion step
 constexpr uint32_t kTopThreads = 1024;  // the single CTA of the top levels
 constexpr uint32_t kTopCap = 8192;      // its front capacity (two buffers: 128 KB)
 constexpr uint32_t kHandoff = 2048;     // front width at which the walkers take over
@@ -448,8 +448,8 @@ __device__ __forceinline__ void flush_candidates(const DetectArgs& a, const uint
     else store_candidates(a, buf, count, lane);
 }
 
-// Queue one candidate per lane where `pred`; every 32 queued candidates are
-// tested (fused narrow phase) or stored (broad phase only) at once.
+// Queue one candidate per lane where `pred` in the warp's buffer (at most 2
+// per lane between two drains).
 template <bool kFused>
 __device__ __forceinline__ void push_candidate(const DetectArgs& a, WarpCands& wc, bool pred, uint64_t cval,
                                                uint32_t lane)
@@ -460,27 +460,36 @@ __device__ __forceinline__ void push_candidate(const DetectArgs& a, WarpCands& w
     if (pred) wc.buf[wc.n + __popc(mask & ((1u << lane) - 1u))] = cval;
     wc.n += __popc(mask);
     __syncwarp();
-    if (wc.n >= 32) {
+}
+
+// Every 32 queued candidates are tested (fused narrow phase) or stored (broad
+// phase only) at once; called once per step, where little else is live.
+template <bool kFused>
+__device__ __forceinline__ void drain_candidates(const DetectArgs& a, WarpCands& wc, uint32_t lane)
+{
+    while (wc.n >= 32) {
         flush_candidates<kFused>(a, wc.buf + wc.n - 32, 32, lane);
         wc.n -= 32;
         __syncwarp();
     }
 }
 
-// One BVTT pair per lane, one level down on both sides (a leaf stays put):
-// all child boxes are loaded first (independent loads), the up to 4 child
+// One BVTT pair per lane, one level down on the side its key names (the
+// larger box; a leaf never descends): the pair's own node on the other side
+// and the up to 2 children are loaded first (independent loads), the child
 // pairs are tested and overlapping leaf pairs become candidates. Returns the
-// overlapping internal child pairs (bit 2x + y: child pair (fa + x, fb + y));
-// `tested` gets the warp's number of child pairs tested (lane 0 only).
+// overlapping internal child pairs (bit 2x + y: child pair (fa + x, fb + y))
+// with the side each of them descends next (bit k of dm); `tested` gets the
+// warp's number of child pairs tested (lane 0 only).
 struct Expansion {
-    uint32_t pair, fa, fb, m;
+    uint32_t pair, fa, fb, m, dm;
 };
 template <bool kFused>
 __device__ __forceinline__ Expansion expand_test(const DetectArgs& a, WarpCands& wc, bool valid, uint64_t node,
                                                  uint32_t lane, uint32_t& tested)
 {
     uint32_t pair = 0, fa = 0, fb = 0, na = 0, nb = 0, leaf_a = 0, leaf_b = 0;
-    bool leaves = false;
+    bool leaves = false, a_leaf = false, b_leaf = false;
     Box A0{}, A1{}, B0{}, B1{};
     if (valid) {
         pair = bvtt_pair(node);
@@ -489,26 +498,44 @@ __device__ __forceinline__ Expansion expand_test(const DetectArgs& a, WarpCands&
         const TreeRef TA = load_tree_ref(pv.ta);
         const TreeRef TB = load_tree_ref(pv.tb);
         const uint32_t la = ilog2(ia + 1u), lb = ilog2(ib + 1u);
-        expand_side(TA.shape(), ia, la, 1, fa, na);
-        expand_side(TB.shape(), ib, lb, 1, fb, nb);
+        // the side to descend: the key's, unless that side is a leaf (then the
+        // other one), so every expansion goes one level down somewhere
+        uint32_t d = bvtt_desc(node);
+        if (d == 0 && la == TA.L) d = 1;
+        else if (d == 1 && lb == TB.L) d = 0;
+        if (d == 0) {
+            expand_side(TA.shape(), ia, la, 1, fa, na);
+            fb = ib;
+            nb = 1;
+        } else {
+            fa = ia;
+            na = 1;
+            expand_side(TB.shape(), ib, lb, 1, fb, nb);
+        }
         const uint32_t lca = ilog2(fa + 1u), lcb = ilog2(fb + 1u);
-        leaves = lca == TA.L && lcb == TB.L;
+        a_leaf = lca == TA.L;
+        b_leaf = lcb == TB.L;
+        leaves = a_leaf && b_leaf;
         leaf_a = fa - ((1u << lca) - 1u);  // Morton-order leaf index when lca is the leaf level
         leaf_b = fb - ((1u << lcb) - 1u);
         node_boxes(TA, fa, lca, na > 1, A0, A1);
         node_boxes(TB, fb, lcb, nb > 1, B0, B1);
     }
-    // bit (2x + y): child pair (fa + x, fb + y) overlaps
-    uint32_t m = 0;
+    // bit (2x + y): child pair (fa + x, fb + y) overlaps; one side has 1 entry
+    uint32_t m = 0, dm = 0;
     if (valid) {
         m |= overlap(A0, B0) ? 1u : 0u;
         if (nb > 1) m |= overlap(A0, B1) ? 2u : 0u;
         if (na > 1) m |= overlap(A1, B0) ? 4u : 0u;
-        if (na > 1 && nb > 1) m |= overlap(A1, B1) ? 8u : 0u;
+        if (!leaves) {
+            dm |= descend_side(A0, a_leaf, B0, b_leaf);
+            if (nb > 1) dm |= descend_side(A0, a_leaf, B1, b_leaf) << 1;
+            if (na > 1) dm |= descend_side(A1, a_leaf, B0, b_leaf) << 2;
+        }
     }
     const uint32_t t = __reduce_add_sync(0xffffffffu, na * nb);
     tested = lane == 0 ? t : 0u;
-    // candidates, one bit per round (at most 4 rounds); every lane joins each round
+    // candidates, one bit per round (at most 2 rounds); every lane joins each round
     uint32_t cm = leaves ? m : 0u;
     while (__any_sync(0xffffffffu, cm != 0)) {
         const bool pred = cm != 0;
@@ -520,7 +547,13 @@ __device__ __forceinline__ Expansion expand_test(const DetectArgs& a, WarpCands&
         }
         push_candidate<kFused>(a, wc, pred, c, lane);
     }
-    return Expansion{pair, fa, fb, leaves ? 0u : m};
+    return Expansion{pair, fa, fb, leaves ? 0u : m, dm};
+}
+
+// The key of child pair k (bit 2x + y) of an expansion.
+__device__ __forceinline__ uint64_t child_key(const Expansion& e, uint32_t k)
+{
+    return bvtt_pack(e.pair, e.fa + (k >> 1), e.fb + (k & 1), (e.dm >> k) & 1u);
 }
 
 // Exclusive prefix over the warp of each lane's child count; `total` = the
@@ -548,7 +581,7 @@ __device__ __forceinline__ void write_children(const DetectArgs& a, const Expans
     while (mm) {
         const uint32_t k = __ffs(mm) - 1;
         mm &= mm - 1;
-        const uint64_t child = bvtt_pack(e.pair, e.fa + (k >> 1), e.fb + (k & 1));
+        const uint64_t child = child_key(e, k);
         if (pos < fit) *slot(pos) = child;
         else {
             const uint32_t sp = sbase + (pos - fit);
@@ -617,12 +650,14 @@ __global__ void __launch_bounds__(kDetectThreads) k_init_front(DetectArgs a, uin
             const uint32_t ia = (1u << pv.entry_a) - 1u + x, ib = (1u << pv.entry_b) - 1u + y;
             const TreeRef TA = load_tree_ref(pv.ta);
             const TreeRef TB = load_tree_ref(pv.tb);
-            ov = overlap(node_box(TA, ia, pv.entry_a), node_box(TB, ib, pv.entry_b));
+            const Box ba = node_box(TA, ia, pv.entry_a), bb = node_box(TB, ib, pv.entry_b);
+            ov = overlap(ba, bb);
             leafpair = ov && pv.entry_a == TA.L && pv.entry_b == TB.L;
-            node = bvtt_pack(lo, ia, ib);
+            node = bvtt_pack(lo, ia, ib, descend_side(ba, pv.entry_a == TA.L, bb, pv.entry_b == TB.L));
             cval = bvtt_pack(lo, x, y);
         }
         push_candidate<kFused>(a, wc, leafpair, cval, lane);
+        drain_candidates<kFused>(a, wc, lane);
         const bool push = ov && !leafpair;
         const uint32_t pos = warp_append(a.counts + kCountWork0, push, lane);
         if (push) {
@@ -690,6 +725,7 @@ __global__ void __launch_bounds__(kTopThreads) k_top(DetectArgs a)
             const uint64_t node = valid ? fc[i] : 0ull;
             // what outgrows the buffer goes to the walkers' list directly
             tested += expand_pair<kFused>(a, wc, valid, node, fn, &s_cnt[cur ^ 1], kTopCap, out, out_cnt, lane);
+            drain_candidates<kFused>(a, wc, lane);
         }
         __syncthreads();
         c = min(s_cnt[cur ^ 1], kTopCap);
@@ -758,16 +794,20 @@ __global__ void __launch_bounds__(kDetectThreads, kDense ? 4 : 3) k_walk(DetectA
         tested += t;
         uint32_t total;
         const uint32_t ex = child_prefix((uint32_t)__popc(e.m), lane, total);
-        if (total == 0) continue;
-        const uint32_t fit = min(total, R - live);
-        uint32_t sbase = 0;
-        if (total > fit) {
-            if (lane == 31) sbase = atomicAdd(spill_cnt, total - fit);
-            sbase = __shfl_sync(0xffffffffu, sbase, 31);
+        if (total > 0) {
+            const uint32_t fit = min(total, R - live);
+            uint32_t sbase = 0;
+            if (total > fit) {
+                if (lane == 31) sbase = atomicAdd(spill_cnt, total - fit);
+                sbase = __shfl_sync(0xffffffffu, sbase, 31);
+            }
+            write_children(a, e, ex, fit, spill, sbase, [&](uint32_t p) { return ring + slot(live + p); });
+            live += fit;
+            __syncwarp();  // appended entries are visible to the lanes that pop them
         }
-        write_children(a, e, ex, fit, spill, sbase, [&](uint32_t p) { return ring + slot(live + p); });
-        live += fit;
-        __syncwarp();  // appended entries are visible to the lanes that pop them
+        // the step's candidates are tested (or stored) after its children are
+        // queued, where little else is live
+        drain_candidates<kFused>(a, wc, lane);
     }
     if (lane == 0 && tested) atomicAdd(a.counts + kCountTested, tested);
     flush_found(a, wc, lane);
