@@ -13,6 +13,7 @@
 //     unchecked, src/cuda/scene.cu:15-21, src/cuda/collide.cu:160-161);
 //   * every CUDA status is checked and returned.
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <cstdio>
 #include <cstdint>
@@ -261,17 +262,22 @@ TreeView view_of(const oibvh_tree_t t)
 }
 
 // Start level of each pair: the reference's entry level, deepened so that
-// the start cross product holds about 2^tune_start_log2 (default 2^16) node
-// pairs over the pass (the
-// pair set does not depend on it; a deeper start gives the traversal enough
-// independent work for every SM).
+// the start cross products hold about 2^tune_start_log2 (default 2^16) node
+// pairs over the pass, shared out in proportion to the pairs' triangle counts
+// (the pair set does not depend on it; a deeper start gives the traversal
+// enough independent work for every SM, and starting large pairs deeper
+// keeps the work items of similar size).
 int plan_pass(const oibvh_scene_s* s, const uint32_t* pr, uint32_t n, uint32_t entry, PassPlan& plan)
 {
     plan.pv.resize(n);
     plan.front0 = 0;
-    const uint32_t lg = ilog2(std::max(1u, n));
-    const uint32_t target = s->tune_start_log2;
-    const uint32_t auto_level = lg >= target ? 0u : (target - lg) / 2u;
+    // the pass's start budget of 2^tune_start_log2 node pairs, shared out in
+    // proportion to each pair's triangles: a large pair starts deeper, so the
+    // work items handed to the walkers cover subtrees of similar size
+    double total = 0.0;
+    for (uint32_t p = 0; p < n; ++p)
+        total += (double)s->trees[pr[2 * p]]->nT + (double)s->trees[pr[2 * p + 1]]->nT;
+    const double budget = std::ldexp(1.0, (int)s->tune_start_log2);
     for (uint32_t p = 0; p < n; ++p) {
         const TreeShape& A = s->trees[pr[2 * p]]->shape;
         const TreeShape& B = s->trees[pr[2 * p + 1]]->shape;
@@ -280,7 +286,9 @@ int plan_pass(const oibvh_scene_s* s, const uint32_t* pr, uint32_t n, uint32_t e
         v.b = pr[2 * p + 1];
         v.ta = view_of(s->trees[v.a]);
         v.tb = view_of(s->trees[v.b]);
-        const uint32_t start = std::max(entry, auto_level);
+        const double share = budget * ((double)A.nT + (double)B.nT) / total;  // start pairs for this pair
+        const uint32_t auto_level = share >= 4.0 ? (uint32_t)std::floor(std::log2(share) / 2.0) : 0u;
+        const uint32_t start = std::max(entry, std::min(auto_level, kMaxLeafLevel));
         v.entry_a = std::min(start, A.L);
         v.entry_b = std::min(start, B.L);
         v.front_cnt_a = A.level_count(v.entry_a);
