@@ -187,8 +187,8 @@ def test_refit_level_group_depths_agree(gpu):
 
 def test_full_batched_workload_parity(gpu):
     """The 512-pair workload at full size (103 M triangles): one captured frame
-    gives the pair set of the plain path run pair by pair, and a spread sample
-    of pairs matches the oracle."""
+    gives the pair set of the plain path run pair by pair, and every pair's
+    pair set and the frame's candidate count match the oracle's."""
     import torch
 
     from oibvh_gb300 import DeviceType, OibvhTree, Scene
@@ -221,16 +221,16 @@ def test_full_batched_workload_parity(gpu):
     plain = np.concatenate(parts, 0)
     plain = plain[np.lexsort((plain[:, 3], plain[:, 2], plain[:, 1], plain[:, 0]))]
     assert np.array_equal(frame, plain)
-    # a spread sample against the oracle
-    for p in range(0, 512, 64):
-        a, b = w.pairs[p]
-        xa, xb = w.positions(7, [a, b])
-        port = Port()
-        port.add_mesh(xa, w.rest[a].tri)
-        port.add_mesh(xb, w.rest[b].tri)
-        want, _ = port.detect()
+    # every one of the 512 pairs against the oracle (host threads), and the
+    # frame's candidate count against the oracle's total
+    from tests_support import oracle_pair_sets
+
+    pos = w.positions(7)
+    want = oracle_pair_sets([(pos[a], w.rest[a].tri, pos[b], w.rest[b].tri) for a, b in w.pairs])
+    for p, (a, b) in enumerate(w.pairs):
         got = frame[(frame[:, 0] == a) & (frame[:, 1] == b)][:, 2:]
-        assert np.array_equal(got, sort_pairs(want)[:, 2:]), p
+        assert np.array_equal(got, want[p][0]), p
+    assert sc.candidate_count() == sum(c for _, c in want)
 
 
 def _with_unused_vertices(m, rng):

@@ -108,16 +108,17 @@ def test_random_scenes_vs_oracle(gpu, seed):
 
 
 def test_deforming_s8_frames_vs_oracle(gpu):
-    """The deforming workload at full size (1,310,720 triangles per mesh), two frames."""
+    """The deforming workload at full size (1,310,720 triangles per mesh): the
+    rest pose and ten jittered frames, each refit and detected."""
     from oibvh_gb300 import workloads as W
 
     w = W.deforming()
-    frames = [w.frame_positions(f) for f in (1, 2)]
+    frames = [w.frame_positions(f) for f in range(1, 11)]
     res = run_gpu(w.meshes, None, frames, 4, 3)
     p = Port()
     for m in w.meshes:
         p.add_mesh(m.xyz, m.tri)
-    for f in range(3):
+    for f in range(len(frames) + 1):
         if f:
             for i, xyz in enumerate(frames[f - 1]):
                 p.set_positions(i, xyz)

@@ -168,3 +168,32 @@ def bvtt_front_widths(ma, mb, start, steps=40):
         ia, ib = keep(np.concatenate(xa), np.concatenate(xb))
         out.append(int(ia.shape[0]))
     return out
+
+
+def oracle_pair_sets(jobs, threads=None):
+    """The oracle's sorted (triA, triB) pair set and candidate count for each
+    job (xyz_a, tri_a, xyz_b, tri_b), on host threads (the oracle's calls
+    release the interpreter lock)."""
+    import os
+    import threading
+
+    from oracle.oracle import Port, sort_pairs
+
+    threads = threads or min(16, os.cpu_count() or 1)
+    out = [None] * len(jobs)
+
+    def work(k):
+        for i in range(k, len(jobs), threads):
+            xa, ta, xb, tb = jobs[i]
+            p = Port()
+            p.add_mesh(xa, ta)
+            p.add_mesh(xb, tb)
+            h, c = p.detect()
+            out[i] = (sort_pairs(h)[:, 2:].copy(), c)
+
+    ts = [threading.Thread(target=work, args=(k,)) for k in range(threads)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    return out
