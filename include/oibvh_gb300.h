@@ -21,7 +21,7 @@
  *     (the reference's detectCollisionOnCPU is an empty TODO,
  *     src/cuda/scene.cu:187-190).
  *
- * Limits: 1 <= triangles per mesh <= 2^23; at most 2^15 mesh pairs are
+ * Limits: 1 <= triangles per mesh <= 2^23; at most 2^14 mesh pairs are
  * traversed per pass (more are processed in several passes).
  */
 #ifndef OIBVH_GB300_H
@@ -249,7 +249,7 @@ int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t reps, o
 
 /* A whole frame as one CUDA graph: [oibvh_scene_transform(d_rest, d_mats)]
  * + [oibvh_scene_refit] (when refit != 0) + the detect of every pair (at most
- * 32768 pairs, fixed number of traversal rounds, results to pinned memory).
+ * 16384 pairs, fixed number of traversal rounds, results to pinned memory).
  * capture_frame runs one ordinary frame first (it sizes the queues with 2x
  * headroom and uploads the tables), then captures. launch_frame replays the
  * graph (re-capturing first if the scene or tuning changed); finish_frame
@@ -363,7 +363,7 @@ typedef struct oibvh_server_stats {
     uint64_t arena_bytes, arena_used_bytes, arena_peak_bytes;
     uint64_t queued;             /* waiting for admission */
 } oibvh_server_stats;
-/* max_batch: queries per batch, 1..32768 (one traversal pass); n_lanes:
+/* max_batch: queries per batch, 1..16384 (one traversal pass); n_lanes:
  * 1..16; the memory budget (>= 1 MiB) is allocated at once. */
 int oibvh_server_create(int device, uint64_t memory_budget_bytes, uint32_t max_batch, uint32_t n_lanes,
                         oibvh_server_t* out);

@@ -373,7 +373,7 @@ __device__ __forceinline__ void expand_side(const TreeShape& S, uint32_t ia, uin
 // shared memory and tested 32 at a time, one per lane, so the 17-axis test
 // runs at full SIMT width however sparse the candidates are.
 // ---------------------------------------------------------------------------
-constexpr int kCandBuf = 96;  // <= 31 left over + up to 2 per lane added by one expansion step
+constexpr int kCandBuf = 160;  // <= 31 left over + up to 4 per lane added by one expansion step
 constexpr uint32_t kTopThreads = 1024;  // the single CTA of the top levels
 constexpr uint32_t kTopCap = 8192;      // its front capacity (two buffers: 128 KB)
 constexpr uint32_t kHandoff = 2048;     // front width at which the walkers take over
@@ -448,7 +448,7 @@ __device__ __forceinline__ void flush_candidates(const DetectArgs& a, const uint
     else store_candidates(a, buf, count, lane);
 }
 
-// Queue one candidate per lane where `pred` in the warp's buffer (at most 2
+// Queue one candidate per lane where `pred` in the warp's buffer (at most 4
 // per lane between two drains).
 template <bool kFused>
 __device__ __forceinline__ void push_candidate(const DetectArgs& a, WarpCands& wc, bool pred, uint64_t cval,
@@ -474,13 +474,13 @@ __device__ __forceinline__ void drain_candidates(const DetectArgs& a, WarpCands&
     }
 }
 
-// One BVTT pair per lane, one level down on the side its key names (the
-// larger box; a leaf never descends): the pair's own node on the other side
-// and the up to 2 children are loaded first (independent loads), the child
-// pairs are tested and overlapping leaf pairs become candidates. Returns the
-// overlapping internal child pairs (bit 2x + y: child pair (fa + x, fb + y))
-// with the side each of them descends next (bit k of dm); `tested` gets the
-// warp's number of child pairs tested (lane 0 only).
+// One BVTT pair per lane, one level down on the sides its key names (both,
+// or the larger box's; a leaf never descends): the up to 2 + 2 boxes (a side
+// that stays contributes its own node) are loaded first (independent loads),
+// the up to 4 child pairs are tested and overlapping leaf pairs become
+// candidates. Returns the overlapping internal child pairs (bit 2x + y: child
+// pair (fa + x, fb + y)) with how each of them expands next (bits 2k, 2k + 1
+// of dm); `tested` gets the warp's number of child pairs tested (lane 0 only).
 struct Expansion {
     uint32_t pair, fa, fb, m, dm;
 };
@@ -498,20 +498,15 @@ __device__ __forceinline__ Expansion expand_test(const DetectArgs& a, WarpCands&
         const TreeRef TA = load_tree_ref(pv.ta);
         const TreeRef TB = load_tree_ref(pv.tb);
         const uint32_t la = ilog2(ia + 1u), lb = ilog2(ib + 1u);
-        // the side to descend: the key's, unless that side is a leaf (then the
-        // other one), so every expansion goes one level down somewhere
-        uint32_t d = bvtt_desc(node);
-        if (d == 0 && la == TA.L) d = 1;
-        else if (d == 1 && lb == TB.L) d = 0;
-        if (d == 0) {
-            expand_side(TA.shape(), ia, la, 1, fa, na);
-            fb = ib;
-            nb = 1;
-        } else {
-            fa = ia;
-            na = 1;
-            expand_side(TB.shape(), ib, lb, 1, fb, nb);
-        }
+        // the sides to descend: the key's, never a leaf (a leaf side stays and
+        // the other one descends), so every expansion goes one level down
+        const uint32_t d = bvtt_desc(node);
+        const bool down_a = la != TA.L && (d != kDescendB || lb == TB.L);
+        const bool down_b = lb != TB.L && (d != kDescendA || la == TA.L);
+        if (down_a) expand_side(TA.shape(), ia, la, 1, fa, na);
+        else fa = ia, na = 1;
+        if (down_b) expand_side(TB.shape(), ib, lb, 1, fb, nb);
+        else fb = ib, nb = 1;
         const uint32_t lca = ilog2(fa + 1u), lcb = ilog2(fb + 1u);
         a_leaf = lca == TA.L;
         b_leaf = lcb == TB.L;
@@ -521,21 +516,23 @@ __device__ __forceinline__ Expansion expand_test(const DetectArgs& a, WarpCands&
         node_boxes(TA, fa, lca, na > 1, A0, A1);
         node_boxes(TB, fb, lcb, nb > 1, B0, B1);
     }
-    // bit (2x + y): child pair (fa + x, fb + y) overlaps; one side has 1 entry
+    // bit (2x + y): child pair (fa + x, fb + y) overlaps
     uint32_t m = 0, dm = 0;
     if (valid) {
         m |= overlap(A0, B0) ? 1u : 0u;
         if (nb > 1) m |= overlap(A0, B1) ? 2u : 0u;
         if (na > 1) m |= overlap(A1, B0) ? 4u : 0u;
+        if (na > 1 && nb > 1) m |= overlap(A1, B1) ? 8u : 0u;
         if (!leaves) {
             dm |= descend_side(A0, a_leaf, B0, b_leaf);
-            if (nb > 1) dm |= descend_side(A0, a_leaf, B1, b_leaf) << 1;
-            if (na > 1) dm |= descend_side(A1, a_leaf, B0, b_leaf) << 2;
+            if (nb > 1) dm |= descend_side(A0, a_leaf, B1, b_leaf) << 2;
+            if (na > 1) dm |= descend_side(A1, a_leaf, B0, b_leaf) << 4;
+            if (na > 1 && nb > 1) dm |= descend_side(A1, a_leaf, B1, b_leaf) << 6;
         }
     }
     const uint32_t t = __reduce_add_sync(0xffffffffu, na * nb);
     tested = lane == 0 ? t : 0u;
-    // candidates, one bit per round (at most 2 rounds); every lane joins each round
+    // candidates, one bit per round (at most 4 rounds); every lane joins each round
     uint32_t cm = leaves ? m : 0u;
     while (__any_sync(0xffffffffu, cm != 0)) {
         const bool pred = cm != 0;
@@ -553,7 +550,7 @@ __device__ __forceinline__ Expansion expand_test(const DetectArgs& a, WarpCands&
 // The key of child pair k (bit 2x + y) of an expansion.
 __device__ __forceinline__ uint64_t child_key(const Expansion& e, uint32_t k)
 {
-    return bvtt_pack(e.pair, e.fa + (k >> 1), e.fb + (k & 1), (e.dm >> k) & 1u);
+    return bvtt_pack(e.pair, e.fa + (k >> 1), e.fb + (k & 1), (e.dm >> (2 * k)) & 3u);
 }
 
 // Exclusive prefix over the warp of each lane's child count; `total` = the

@@ -470,7 +470,7 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
             OK_TRY(narrow_pass(s, np, hits_before, st));
         } else if (!narrow) {
             if (n_pairs > kMaxPairsPerPass)
-                return fail(OIBVH_ERR_UNSUPPORTED, "the split broad phase handles at most 32768 pairs");
+                return fail(OIBVH_ERR_UNSUPPORTED, "the split broad phase handles at most 16384 pairs");
             s->last_pairs = plan.pv;
             s->cands_valid = true;
         }
@@ -1399,7 +1399,7 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
     list_pairs(s, pr);
     const uint32_t np = (uint32_t)(pr.size() / 2);
     if (np == 0) return fail(OIBVH_ERR_STATE, "no pairs to detect");
-    if (np > kMaxPairsPerPass) return fail(OIBVH_ERR_UNSUPPORTED, "a captured frame handles at most 32768 pairs");
+    if (np > kMaxPairsPerPass) return fail(OIBVH_ERR_UNSUPPORTED, "a captured frame handles at most 16384 pairs");
     // warm-up frame outside the capture: sizes every buffer and uploads the tables
     if (s->frame_rest) OK_TRY(oibvh_scene_transform(s, (const float*)s->frame_rest, s->frame_mats, st));
     if (s->frame_refit) OK_TRY(oibvh_scene_refit(s, st));

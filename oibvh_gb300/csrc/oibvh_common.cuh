@@ -22,18 +22,19 @@
 namespace oibvh {
 
 constexpr uint32_t kMaxLeafLevel = 23;   // T <= 2^23 triangles per mesh
-constexpr uint32_t kMaxPairsPerPass = 1u << 15;  // pair id field of a BVTT node
+constexpr uint32_t kMaxPairsPerPass = 1u << 14;  // pair id field of a BVTT node
 
-// BVTT node / candidate encoding: [pair:15][d:1][a:24][b:24], a and b are
-// implicit indices (candidates: leaf indices in Morton order, d = 0). d is the
-// side the traversal descends when it expands the node pair: 0 = a's
-// children against b, 1 = a against b's children.
+// BVTT node / candidate encoding: [pair:14][d:2][a:24][b:24], a and b are
+// implicit indices (candidates: leaf indices in Morton order, d = 0). d is how
+// the traversal expands the node pair: kDescendBoth = both sides' children,
+// kDescendA = a's children against b, kDescendB = a against b's children.
+enum : uint32_t { kDescendBoth = 0, kDescendA = 1, kDescendB = 2 };
 __host__ __device__ __forceinline__ uint64_t bvtt_pack(uint32_t pair, uint32_t a, uint32_t b, uint32_t d = 0)
 {
-    return ((uint64_t)pair << 49) | ((uint64_t)d << 48) | ((uint64_t)a << 24) | (uint64_t)b;
+    return ((uint64_t)pair << 50) | ((uint64_t)d << 48) | ((uint64_t)a << 24) | (uint64_t)b;
 }
-__host__ __device__ __forceinline__ uint32_t bvtt_pair(uint64_t v) { return (uint32_t)(v >> 49); }
-__host__ __device__ __forceinline__ uint32_t bvtt_desc(uint64_t v) { return (uint32_t)(v >> 48) & 1u; }
+__host__ __device__ __forceinline__ uint32_t bvtt_pair(uint64_t v) { return (uint32_t)(v >> 50); }
+__host__ __device__ __forceinline__ uint32_t bvtt_desc(uint64_t v) { return (uint32_t)(v >> 48) & 3u; }
 __host__ __device__ __forceinline__ uint32_t bvtt_a(uint64_t v) { return (uint32_t)(v >> 24) & 0xffffffu; }
 __host__ __device__ __forceinline__ uint32_t bvtt_b(uint64_t v) { return (uint32_t)v & 0xffffffu; }
 
@@ -285,11 +286,17 @@ __device__ __forceinline__ TreeRef load_tree_ref(const TreeView& T)
     return t;
 }
 
-// Which side of an overlapping node pair to descend next: the one with the
-// larger box (squared diagonal), never a leaf. The pair set does not depend
-// on it; descending one side tests 2 child pairs per step instead of 4 and
-// keeps the two boxes of a pair of similar size, which tests about 40 % fewer
-// pairs than descending both sides at once.
+// How to expand an overlapping node pair next: both sides while their boxes
+// are of similar size (squared diagonals within kDescendRatio), else only the
+// larger box's side; a leaf never descends. The pair set does not depend on
+// it. Descending only the larger of two very different boxes keeps the pairs'
+// boxes matched (trees of different depths, meshes of different scales) and
+// tests fewer pairs; descending both keeps the number of expansion steps of
+// equal trees at one per level.
+#ifndef OIBVH_DESCEND_RATIO
+#define OIBVH_DESCEND_RATIO 16.0f
+#endif
+constexpr float kDescendRatio = OIBVH_DESCEND_RATIO;
 __device__ __forceinline__ float box_size2(const Box& b)
 {
     const float x = b.xx - b.nx, y = b.xy - b.ny, z = b.xz - b.nz;
@@ -297,9 +304,12 @@ __device__ __forceinline__ float box_size2(const Box& b)
 }
 __device__ __forceinline__ uint32_t descend_side(const Box& a, bool a_leaf, const Box& b, bool b_leaf)
 {
-    if (a_leaf) return 1u;
-    if (b_leaf) return 0u;
-    return box_size2(a) >= box_size2(b) ? 0u : 1u;
+    if (a_leaf) return kDescendB;
+    if (b_leaf) return kDescendA;
+    const float sa = box_size2(a), sb = box_size2(b);
+    if (sa > kDescendRatio * sb) return kDescendA;
+    if (sb > kDescendRatio * sa) return kDescendB;
+    return kDescendBoth;
 }
 
 // aabb_box_t::overlap (include/utils/utils.h:39-44; src/cuda/collide.cu:12-17)

@@ -526,7 +526,7 @@ API int oibvh_server_create(int device, uint64_t memory_budget_bytes, uint32_t m
     if (!out) return fail(OIBVH_ERR_ARG, "out is NULL");
     *out = nullptr;
     if (memory_budget_bytes < (1u << 20)) return fail(OIBVH_ERR_ARG, "memory budget below 1 MiB");
-    if (max_batch == 0 || max_batch > kMaxPairsPerPass) return fail(OIBVH_ERR_ARG, "max_batch must be in 1..32768");
+    if (max_batch == 0 || max_batch > kMaxPairsPerPass) return fail(OIBVH_ERR_ARG, "max_batch must be in 1..16384");
     if (n_lanes == 0 || n_lanes > 16) return fail(OIBVH_ERR_ARG, "lanes must be in 1..16");
     int ndev = 0;
     CUDA_TRY(cudaGetDeviceCount(&ndev));

@@ -25,3 +25,25 @@ g++ -std=c++17 -O2 -DNDEBUG -ffp-contract=off -fPIC -shared -w \
   -o "$OUT/libref_cpu.so.tmp"
 mv "$OUT/libref_cpu.so.tmp" "$OUT/libref_cpu.so"
 echo "built $OUT/libref_cpu.so"
+
+# The reference's GPU kernels (src/cuda/oibvh.cu, src/cuda/collide.cu,
+# unmodified, nvcc's default flags as the reference's own build: FMA
+# contraction on) with the headless host sequence of ref_gpu_harness.cu, for
+# sm_103a, into oracle/_ref/libref_gpu.so. Skipped (with a note) without nvcc.
+NVCC="${NVCC:-${CUDA_HOME:-/usr/local/cuda}/bin/nvcc}"
+if [ "${OIBVH_REF_GPU:-1}" = "1" ] && [ -x "$NVCC" ]; then
+  OBJ="$OUT/gpu_obj"
+  mkdir -p "$OBJ"
+  NVF=(-gencode arch=compute_103a,code=sm_103a -O3 -std=c++17 -w -Xcompiler -fPIC
+       -include "$HERE/ref_compat.h" -I"$REF/include" -I"$REF/third" -I"$REF/third/glad/include")
+  "$NVCC" "${NVF[@]}" -c "$REF/src/cuda/oibvh.cu" -o "$OBJ/oibvh.o" &
+  "$NVCC" "${NVF[@]}" -c "$REF/src/cuda/collide.cu" -o "$OBJ/collide.o" &
+  "$NVCC" "${NVF[@]}" -c "$HERE/ref_gpu_harness.cu" -o "$OBJ/harness.o" &
+  wait
+  "$NVCC" -gencode arch=compute_103a,code=sm_103a -shared -o "$OUT/libref_gpu.so.tmp" \
+    "$OBJ/oibvh.o" "$OBJ/collide.o" "$OBJ/harness.o"
+  mv "$OUT/libref_gpu.so.tmp" "$OUT/libref_gpu.so"
+  echo "built $OUT/libref_gpu.so"
+else
+  echo "reference GPU kernels not built (no nvcc)"
+fi

@@ -26,6 +26,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SRC = os.path.join(HERE, "oibvh_oracle.c")
 PORT_LIB = os.path.join(HERE, "_build", "liboibvh_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_cpu.so")
+REF_GPU_LIB = os.path.join(HERE, "_ref", "libref_gpu.so")
 
 _u32p = ctypes.POINTER(ctypes.c_uint32)
 _f32p = ctypes.POINTER(ctypes.c_float)
@@ -264,6 +265,99 @@ class Reference:
     def tri_intersect(cls, P1, P2, P3, Q1, Q2, Q3) -> bool:
         args = [_f32(v) for v in (P1, P2, P3, Q1, Q2, Q3)]
         return bool(cls.lib().ref_tri_intersect(*[a[1] for a in args]))
+
+
+class RefGPU:
+    """The reference's own GPU kernels (src/cuda/oibvh.cu and src/cuda/collide.cu,
+    compiled unmodified by build_ref.sh into oracle/_ref/libref_gpu.so) driven
+    by the headless host sequence of oracle/ref_gpu_harness.cu. A build whose
+    construction schedule has a partial block, or a detect whose traversal
+    would overflow the reference's fixed buffers, is refused on the host
+    before any kernel runs (status UNSAFE_*)."""
+
+    OK, CUDA, UNSAFE_SCHEDULE, UNSAFE_CAPACITY, ARG = 0, -1, -2, -3, -4
+    _lib = None
+
+    @classmethod
+    def available(cls) -> bool:
+        try:
+            cls.lib()
+            return True
+        except OSError:
+            return False
+
+    @classmethod
+    def lib(cls):
+        if cls._lib is None:
+            lib = ctypes.CDLL(REF_GPU_LIB)
+            vp = ctypes.c_void_p
+            lib.refgpu_tree_create.restype = vp
+            lib.refgpu_tree_create.argtypes = [_f32p, ctypes.c_uint32, _u32p, ctypes.c_uint32]
+            lib.refgpu_tree_destroy.argtypes = [vp]
+            lib.refgpu_tree_build.argtypes = [vp, ctypes.c_int, _f32p]
+            lib.refgpu_tree_refit.argtypes = [vp, _f32p, _f32p]
+            lib.refgpu_tree_get.argtypes = [vp, _f32p, _u32p]
+            lib.refgpu_tree_size.argtypes = [vp]
+            lib.refgpu_tree_size.restype = ctypes.c_uint32
+            lib.refgpu_detect.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, _u32p,
+                                          ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong), _f32p]
+            lib.refgpu_detect.restype = ctypes.c_longlong
+            cls._lib = lib
+        return cls._lib
+
+    class Tree:
+        def __init__(self, xyz, tri):
+            x, xp = _f32(xyz)
+            t, tp = _u32(tri)
+            self.n_tri = t.shape[0]
+            self._h = ctypes.c_void_p(RefGPU.lib().refgpu_tree_create(xp, x.shape[0], tp, t.shape[0]))
+            if not self._h.value:
+                raise ValueError("reference GPU tree: needs at least 2 triangles")
+
+        def __del__(self):
+            h = getattr(self, "_h", None)
+            if h is not None and h.value:
+                RefGPU.lib().refgpu_tree_destroy(h)
+                self._h = None
+
+        def build(self, construct: bool = True):
+            """(status, [whole ms, kernels ms]); UNSAFE_SCHEDULE: sorted faces only."""
+            ms = np.zeros(2, dtype=np.float32)
+            st = RefGPU.lib().refgpu_tree_build(self._h, int(construct), ms.ctypes.data_as(_f32p))
+            return int(st), ms
+
+        def refit(self, xyz):
+            x, xp = _f32(xyz)
+            ms = np.zeros(2, dtype=np.float32)
+            st = RefGPU.lib().refgpu_tree_refit(self._h, xp, ms.ctypes.data_as(_f32p))
+            return int(st), ms
+
+        def boxes(self) -> np.ndarray:
+            n = RefGPU.lib().refgpu_tree_size(self._h)
+            out = np.empty((n, 6), dtype=np.float32)
+            RefGPU.lib().refgpu_tree_get(self._h, out.ctypes.data_as(_f32p), None)
+            return out
+
+        def sorted_faces(self) -> np.ndarray:
+            out = np.empty((self.n_tri, 3), dtype=np.uint32)
+            RefGPU.lib().refgpu_tree_get(self._h, None, out.ctypes.data_as(_u32p))
+            return out
+
+    @classmethod
+    def detect(cls, trees, entry: int = 4, expand: int = 3):
+        """(status or hit count, hits uint32[n, 4] {bvhA, bvhB, triA, triB} with
+        Morton-order triangle indices, candidate count, [whole, traversal,
+        narrow] ms). A negative first value is a refusal or a CUDA error."""
+        hs = (ctypes.c_void_p * len(trees))(*[t._h.value for t in trees])
+        cap = 1 << 22
+        out = np.empty((cap, 4), dtype=np.uint32)
+        nc = ctypes.c_longlong(0)
+        ms = np.zeros(3, dtype=np.float32)
+        n = cls.lib().refgpu_detect(hs, len(trees), entry, expand, out.ctypes.data_as(_u32p), cap, ctypes.byref(nc),
+                                    ms.ctypes.data_as(_f32p))
+        if n < 0:
+            return int(n), None, 0, ms
+        return int(n), out[: min(n, cap)].copy(), int(nc.value), ms
 
 
 def sort_pairs(hits: np.ndarray) -> np.ndarray:
