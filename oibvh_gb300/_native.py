@@ -88,6 +88,7 @@ class Tuning(ctypes.Structure):
         ("hit_capacity", ctypes.c_uint32),
         ("walk_front", ctypes.c_uint32),
         ("refit_group_log2", ctypes.c_uint32),
+        ("descend_ratio", ctypes.c_uint32),
     ]
 
 

@@ -524,10 +524,11 @@ __device__ __forceinline__ Expansion expand_test(const DetectArgs& a, WarpCands&
         if (na > 1) m |= overlap(A1, B0) ? 4u : 0u;
         if (na > 1 && nb > 1) m |= overlap(A1, B1) ? 8u : 0u;
         if (!leaves) {
-            dm |= descend_side(A0, a_leaf, B0, b_leaf);
-            if (nb > 1) dm |= descend_side(A0, a_leaf, B1, b_leaf) << 2;
-            if (na > 1) dm |= descend_side(A1, a_leaf, B0, b_leaf) << 4;
-            if (na > 1 && nb > 1) dm |= descend_side(A1, a_leaf, B1, b_leaf) << 6;
+            const float r = a.descend_ratio;
+            dm |= descend_side(A0, a_leaf, B0, b_leaf, r);
+            if (nb > 1) dm |= descend_side(A0, a_leaf, B1, b_leaf, r) << 2;
+            if (na > 1) dm |= descend_side(A1, a_leaf, B0, b_leaf, r) << 4;
+            if (na > 1 && nb > 1) dm |= descend_side(A1, a_leaf, B1, b_leaf, r) << 6;
         }
     }
     const uint32_t t = __reduce_add_sync(0xffffffffu, na * nb);
@@ -650,7 +651,7 @@ __global__ void __launch_bounds__(kDetectThreads) k_init_front(DetectArgs a, uin
             const Box ba = node_box(TA, ia, pv.entry_a), bb = node_box(TB, ib, pv.entry_b);
             ov = overlap(ba, bb);
             leafpair = ov && pv.entry_a == TA.L && pv.entry_b == TB.L;
-            node = bvtt_pack(lo, ia, ib, descend_side(ba, pv.entry_a == TA.L, bb, pv.entry_b == TB.L));
+            node = bvtt_pack(lo, ia, ib, descend_side(ba, pv.entry_a == TA.L, bb, pv.entry_b == TB.L, a.descend_ratio));
             cval = bvtt_pack(lo, x, y);
         }
         push_candidate<kFused>(a, wc, leafpair, cval, lane);

@@ -287,28 +287,25 @@ __device__ __forceinline__ TreeRef load_tree_ref(const TreeView& T)
 }
 
 // How to expand an overlapping node pair next: both sides while their boxes
-// are of similar size (squared diagonals within kDescendRatio), else only the
+// are of similar size (squared diagonals within `ratio`), else only the
 // larger box's side; a leaf never descends. The pair set does not depend on
 // it. Descending only the larger of two very different boxes keeps the pairs'
 // boxes matched (trees of different depths, meshes of different scales) and
 // tests fewer pairs; descending both keeps the number of expansion steps of
-// equal trees at one per level.
-#ifndef OIBVH_DESCEND_RATIO
-#define OIBVH_DESCEND_RATIO 16.0f
-#endif
-constexpr float kDescendRatio = OIBVH_DESCEND_RATIO;
+// equal trees at one per level. The ratio is a tuning parameter (default 16).
+constexpr float kDescendRatio = 16.0f;
 __device__ __forceinline__ float box_size2(const Box& b)
 {
     const float x = b.xx - b.nx, y = b.xy - b.ny, z = b.xz - b.nz;
     return x * x + y * y + z * z;
 }
-__device__ __forceinline__ uint32_t descend_side(const Box& a, bool a_leaf, const Box& b, bool b_leaf)
+__device__ __forceinline__ uint32_t descend_side(const Box& a, bool a_leaf, const Box& b, bool b_leaf, float ratio)
 {
     if (a_leaf) return kDescendB;
     if (b_leaf) return kDescendA;
     const float sa = box_size2(a), sb = box_size2(b);
-    if (sa > kDescendRatio * sb) return kDescendA;
-    if (sb > kDescendRatio * sa) return kDescendB;
+    if (sa > ratio * sb) return kDescendA;
+    if (sb > ratio * sa) return kDescendB;
     return kDescendBoth;
 }
 

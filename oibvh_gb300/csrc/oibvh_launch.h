@@ -114,6 +114,7 @@ struct DetectArgs {
     uint32_t handoff;      // front width at which k_top hands over to the walkers (<= 8192)
     uint32_t precision;    // 0: float triangle test (reference arithmetic); 1: FP64-filtered
     uint32_t walk_cap;     // per-warp front entries of the walkers (multiple of 32, <= 512; 0: 128)
+    float descend_ratio = kDescendRatio;  // both sides descend while the boxes' squared diagonals are within it
 };
 cudaError_t launch_init_front(const DetectArgs& a, uint32_t total0, cudaStream_t s);
 cudaError_t launch_top(const DetectArgs& a, cudaStream_t s);

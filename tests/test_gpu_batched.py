@@ -128,6 +128,7 @@ def test_autotune_keeps_the_pair_set(gpu):
     before = sc.int_tri_pairs()
     chosen = sc.autotune(0, 2)
     assert chosen["handoff"] in (512, 2048, 8192) and chosen["walk_front"] in (64, 128, 256, 512)
+    assert chosen["descend_ratio"] in (4, 16, 64, 1 << 30)
     sc.detectCollision(DeviceType.GPU0, 0, 1)
     assert np.array_equal(sc.int_tri_pairs(), before)
     want, _ = _oracle(w.positions(0), [m.tri for m in w.rest], w.pairs)
@@ -152,6 +153,28 @@ def test_walker_queue_capacity_keeps_the_pair_set(gpu):
         assert sc.candidate_count() == wc
     with pytest.raises(OibvhError):
         sc.set_tuning(walk_front=48)
+
+
+def test_descend_ratios_keep_the_pair_set(gpu):
+    """However the traversal chooses the side to descend (both sides always,
+    the larger box only, or both while the boxes are within a ratio), the pair
+    set and the candidate count are the oracle's."""
+    from oibvh_gb300 import DeviceType, OibvhError
+
+    w = _workload(8, seed=19, subdivs=(1, 3, 5))
+    sc, trees = _scene_from(w, build_with_scene=False)
+    for t, x in zip(trees, w.positions(0)):
+        t.refit(x)
+    want, wc = _oracle(w.positions(0), [m.tri for m in w.rest], w.pairs)
+    for r in (1, 2, 16, 64, 1 << 30):
+        sc.set_tuning(descend_ratio=r)
+        assert sc.tuning()["descend_ratio"] == r
+        for entry in (0, 4):
+            sc.detectCollision(DeviceType.GPU0, entry, 1)
+            assert np.array_equal(sc.int_tri_pairs(), want), (r, entry)
+            assert sc.candidate_count() == wc
+    with pytest.raises(OibvhError):
+        sc.set_tuning(descend_ratio=(1 << 30) + 1)
 
 
 def test_refit_level_group_depths_agree(gpu):
