@@ -1112,6 +1112,21 @@ def run_ours_precision(args, rank, world, local):
             q_lat.append(1e3 * (time.perf_counter() - t0))
     plain_s = (time.perf_counter() - tp0) / 3
     plain_hits = sum(ps.getIntTriPairCount() for ps in plain)
+    # the float arithmetic (the reference's), one pair per call, on the sample
+    # of pairs the reference's GPU kernels are timed on (REF_GPU_SAMPLE)
+    q_lat32 = []
+    for p in _sample_pairs(w, REF_GPU_SAMPLE):
+        ps = plain[p]
+        ps.set_precision(_native.PRECISION_FP32)
+        for rep_ in range(4):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ps.refit(stream=sh)
+            ps.detectCollision(DeviceType(dev), ENTRY_LEVEL, EXPAND_LEVELS, stream=sh)
+            ps.getIntTriPairCount()
+            if rep_:
+                q_lat32.append(1e3 * (time.perf_counter() - t0))
+        ps.set_precision(_native.PRECISION_FP64_FILTERED)
 
     ms_f, ms_e2e = max_over_ranks([ms_f, ms_e2e], dist, f"cuda:{dev}")
     if dist is not None:
@@ -1146,6 +1161,10 @@ def run_ours_precision(args, rank, world, local):
                               "how": "each pair its own scene: refit both trees + detect, synchronous, FP64-filtered",
                               "hits": plain_hits},
         "batched_over_plain": round(value / (n_pairs / plain_s), 2),
+        "plain_single_pair_fp32": {"ms_per_query": {"p50": round(_pctl(q_lat32, 50), 4),
+                                                    "p99": round(_pctl(q_lat32, 99), 4)},
+                                   "how": f"float test, one pair per call (refit both + detect), "
+                                          f"{REF_GPU_SAMPLE} sampled pairs x 3"},
         "e2e": {"value": round(K * n_pairs * world / (ms_e2e / 1e3), 1), "unit": "queries/s",
                 "h2d_bytes_per_step": int(mats_pinned.numel() * 4), "d2h_bytes_per_step": int(d2h / max(1, K)),
                 "latency_ms": {"p50": round(_pctl(lat_e2e, 50), 4), "p99": round(_pctl(lat_e2e, 99), 4)}},
@@ -1540,6 +1559,7 @@ def subconfigs_ours(args, local):
         "workload": pr["config"]["workload"], "queries_per_s": pr["value"], "frame_ms": pr["ms_per_step"],
         "frames": pr["steps"], "frame_latency_ms": pr["frame_latency_ms"],
         "plain_single_pair": pr["plain_single_pair"], "batched_over_plain": pr["batched_over_plain"],
+        "plain_single_pair_fp32": pr["plain_single_pair_fp32"],
         "fp64_oracle_mismatches": pr.get("fp64_oracle", {}).get("fp64_oracle_mismatches"),
         "fp64_oracle": pr.get("fp64_oracle"),
         "fp32_vs_fp64_disagreements": int(sum(f["fp32_vs_fp64_disagreements_per_pair"])),
@@ -1564,12 +1584,76 @@ def subconfigs_ours(args, local):
 
 
 def subconfigs_reference(args):
-    """The reference CPU path on the same sub-configs, on every host core."""
+    """The reference CPU path on the same sub-configs, on every host core, and
+    the reference's own GPU kernels where its construction can run safely."""
     sub = _sub_args(args, steps=3, warmup=1)
     sv = run_reference_serving(sub, 0, 1)
     pr = run_reference_precision(sub, 0, 1)
     pick = ("value", "unit", "cpu_baseline", "config", "ms_per_step")
-    return {"served": {k: sv[k] for k in pick}, "precision": {k: pr[k] for k in pick}}
+    return {"served": {k: sv[k] for k in pick}, "precision": {k: pr[k] for k in pick},
+            "reference_gpu": reference_gpu_sheets()}
+
+
+REF_GPU_SAMPLE = 16  # sheet pairs of config 4 timed through the reference's GPU kernels
+
+
+def reference_gpu_sheets():
+    """The reference's own GPU kernels (src/cuda/oibvh.cu, src/cuda/collide.cu,
+    compiled unmodified for sm_103a, driven by oracle/ref_gpu_harness.cu's
+    restatement of OibvhTree::refit and Scene::detectCollisionOnGPU, entry 4,
+    expand 3) per query on a sample of config 4's sheet pairs: refit both
+    trees, then detect, as the reference's frame does (positions and faces go
+    to the device and the trees back to the host on every refit). The other
+    configs' icosphere meshes have triangle counts 20 x 4^s, never powers of
+    two, so the construction kernels' schedules have partial blocks (threads
+    that return before __syncthreads); the harness refuses them."""
+    try:
+        import torch
+
+        from oracle.oracle import RefGPU
+        from oibvh_gb300 import workloads as W
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"reference GPU kernels not importable: {e}"}
+    if not RefGPU.available() or not torch.cuda.is_available():
+        return {"unavailable": "reference GPU kernels not built here (oracle/build_ref.sh) or no GPU"}
+    w = W.sheets(64, 256)
+    sample = _sample_pairs(w, REF_GPU_SAMPLE)
+    wall, kern, cands, hits, refused = [], [], 0, 0, 0
+    for p in sample:
+        a, b = w.pairs[p]
+        ta, tb = RefGPU.Tree(w.meshes[a].xyz, w.meshes[a].tri), RefGPU.Tree(w.meshes[b].xyz, w.meshes[b].tri)
+        if ta.build()[0] != RefGPU.OK or tb.build()[0] != RefGPU.OK:
+            refused += 1
+            continue
+        for rep_ in range(4):  # one warm-up query, three timed
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sa, ma = ta.refit(w.meshes[a].xyz)
+            sb, mb = tb.refit(w.meshes[b].xyz)
+            n, _, nc, md = RefGPU.detect([ta, tb], 4, 3)
+            torch.cuda.synchronize()
+            el = 1e3 * (time.perf_counter() - t0)
+            if n < 0 or sa or sb:
+                refused += 1
+                break
+            if rep_:
+                wall.append(el)
+                kern.append(float(ma[1] + mb[1] + md[1] + md[2]))
+        cands += nc
+        hits += max(n, 0)
+    if not wall:
+        return {"unavailable": f"every sampled pair was refused by the harness's safety checks ({refused})"}
+    return {"what": "the reference's own GPU kernels, compiled unmodified for sm_103a, headless host sequence "
+                    "(refit both trees + detect, entry 4, expand 3)",
+            "config": f"precision sheets: {len(wall) // 3} of {len(w.pairs)} pairs, 131,072 triangles per sheet",
+            "ms_per_query": {"p50": round(_pctl(wall, 50), 3), "p99": round(_pctl(wall, 99), 3)},
+            "queries_per_s": round(1e3 / statistics.median(wall), 2),
+            "kernels_ms_per_query": round(statistics.median(kern), 3),
+            "candidates_per_query": cands // max(1, len(wall) // 3), "hits_per_query": hits // max(1, len(wall) // 3),
+            "refused_pairs": refused,
+            "not_run": "configs 1, 2, 3 and 5: icosphere triangle counts are never powers of two, so the reference's "
+                       "construction kernels would run partial blocks whose threads return before __syncthreads "
+                       "(src/cuda/oibvh.cu:87-88, :122); the harness refuses them before launching"}
 
 
 def main():
