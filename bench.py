@@ -45,13 +45,15 @@ METRIC = "collision queries/s"
 UNIT = "queries/s"
 ENTRY_LEVEL, EXPAND_LEVELS = 4, 3  # src/main.cpp:284
 # DRAM bytes (read + written) per triangle of one k_refit launch, measured with
-# ncu on 64 batched pairs (15,520,000 triangles: 372.6 MB read, 453.5 MB written)
-REFIT_DRAM_BYTES_PER_TRIANGLE = (372.647936e6 + 453.495552e6) / 15520000
-# DRAM bytes per vertex of one k_transform_multi launch (ncu, 64 batched pairs)
-TRANSFORM_DRAM_BYTES_PER_VERTEX = (124.3e6 + 77.5e6) / 7766272
-# DRAM bytes of the traversal kernels (k_init_front, k_top, k_walk) of one frame
-# per BVTT pair tested (ncu, 64 batched pairs); None until measured
-TRAVERSAL_DRAM_BYTES_PER_TESTED = None
+# ncu on 64 batched pairs (15,520,000 triangles: 372.7 MB read, 452.3 MB written)
+REFIT_DRAM_BYTES_PER_TRIANGLE = (372.71e6 + 452.25e6) / 15520000
+# DRAM bytes per vertex of one k_transform_multi launch (ncu, 64 batched pairs:
+# 124.3 MB read, 74.0 MB written for 7,760,256 vertices)
+TRANSFORM_DRAM_BYTES_PER_VERTEX = (124.32e6 + 73.98e6) / 7760256
+# DRAM bytes (read + written) of the traversal kernels (k_init_front, k_top and
+# the k_walk rounds) of one frame per BVTT node pair tested, measured with ncu
+# on 64 batched pairs (163.2 MB per frame, 15,595,232 pairs tested)
+TRAVERSAL_DRAM_BYTES_PER_TESTED = (161.72e6 + 0.89e6 + 0.30e6 + 0.30e6) / 15595232
 
 
 def parse():
