@@ -1035,6 +1035,252 @@ __global__ void __launch_bounds__(kDetectThreads, 2) k_narrow_prec(DetectArgs a)
     if (qn > 0) settle_fp64(a, qc, qm, qn, lane);
 }
 
+// ---------------------------------------------------------------------------
+// Precision narrow phase in three passes, grouping candidates by how much of
+// the filtered test they need, so that the lanes of a warp run the same code:
+//  1. k_prec_classify, one candidate per thread: the plain float SAT (the
+//     reference's arithmetic), which also names the first separating axis. A
+//     float-separated candidate needs only that axis bounded: a margin above
+//     its error bound separates in every arithmetic (no hit, float and FP64
+//     agree); otherwise it goes to the recheck list. Shared vertices are hits
+//     at once; a float hit goes to the float-hit list, whose members need all
+//     17 bounded axes (no axis can separate in every arithmetic there).
+//  2. k_prec_settle over the float-hit list then the recheck list, one per
+//     lane: pass 1 of the filtered test (all 17 axes bounded, straight-line
+//     for float hits: no lane leaves early), undecided ones settled in FP64 32
+//     at a time from a per-warp queue.
+// The pair set is the all-FP64 one by construction, as in k_narrow_prec.
+// ---------------------------------------------------------------------------
+
+// The first of the 17 axes (reference order) that separates the triangles
+// in float, 17 when none does (then they intersect in float).
+__device__ __forceinline__ uint32_t tri_first_separating_axis(const V3& P1, const V3& P2, const V3& P3, const V3& Q1,
+                                                              const V3& Q2, const V3& Q3)
+{
+    const V3 p1{0.0f, 0.0f, 0.0f};
+    const V3 p2 = vsub(P2, P1), p3 = vsub(P3, P1);
+    const V3 q1 = vsub(Q1, P1), q2 = vsub(Q2, P1), q3 = vsub(Q3, P1);
+    const V3 e1 = vsub(p2, p1), e2 = vsub(p3, p2), e3 = vsub(p1, p3);
+    const V3 f1 = vsub(q2, q1), f2 = vsub(q3, q2), f3 = vsub(q1, q3);
+    const V3 n1 = vcross(e1, e2);
+    if (!project6(n1, p1, p2, p3, q1, q2, q3)) return 0;
+    const V3 m1 = vcross(f1, f2);
+    if (!project6(m1, p1, p2, p3, q1, q2, q3)) return 1;
+    const V3 E[3] = {e1, e2, e3}, F[3] = {f1, f2, f3};
+#pragma unroll
+    for (uint32_t i = 0; i < 3; ++i)
+#pragma unroll
+        for (uint32_t j = 0; j < 3; ++j)
+            if (!project6(vcross(E[i], F[j]), p1, p2, p3, q1, q2, q3)) return 2 + 3 * i + j;
+#pragma unroll
+    for (uint32_t i = 0; i < 3; ++i)
+        if (!project6(vcross(E[i], n1), p1, p2, p3, q1, q2, q3)) return 11 + i;
+#pragma unroll
+    for (uint32_t j = 0; j < 3; ++j)
+        if (!project6(vcross(F[j], m1), p1, p2, p3, q1, q2, q3)) return 14 + j;
+    return 17;
+}
+
+// Axis k with error bounds (kPass1Separated: its margin separates in every
+// arithmetic; otherwise undecided). Relative extents outside [2^-20, 2^20]
+// are never decided here (the bounds could under- or overflow).
+__device__ __forceinline__ uint32_t bounded_axis_separates(uint32_t k, const V3& P1, const V3& P2, const V3& P3,
+                                                           const V3& Q1, const V3& Q2, const V3& Q3)
+{
+    const V3 p2v = vsub(P2, P1), p3v = vsub(P3, P1);
+    const V3 q1v = vsub(Q1, P1), q2v = vsub(Q2, P1), q3v = vsub(Q3, P1);
+    float A = fmaxf(fmaxf(fmaxf(fabsf(p2v.x), fabsf(p2v.y)), fmaxf(fabsf(p2v.z), fabsf(p3v.x))),
+                    fmaxf(fmaxf(fabsf(p3v.y), fabsf(p3v.z)), fmaxf(fabsf(q1v.x), fabsf(q1v.y))));
+    A = fmaxf(A, fmaxf(fmaxf(fabsf(q1v.z), fabsf(q2v.x)), fmaxf(fabsf(q2v.y), fabsf(q2v.z))));
+    A = fmaxf(A, fmaxf(fmaxf(fabsf(q3v.x), fabsf(q3v.y)), fabsf(q3v.z)));
+    if (!(A >= 0x1p-20f && A <= 0x1p20f)) return kPass1Undecided;
+    const EV3 zero{V3{0.0f, 0.0f, 0.0f}, V3{0.0f, 0.0f, 0.0f}};
+    const EV3 p2 = ev_rel(p2v), p3 = ev_rel(p3v), q1 = ev_rel(q1v), q2 = ev_rel(q2v), q3 = ev_rel(q3v);
+    LaneTri t;
+    t.p2 = p2v;
+    t.p3 = p3v;
+    t.q1 = q1v;
+    t.q2 = q2v;
+    t.q3 = q3v;
+    t.n1 = (k == 0 || (k >= 11 && k < 14)) ? ecross(esub(p2, zero), esub(p3, p2)) : zero;
+    t.m1 = (k == 1 || k >= 14) ? ecross(esub(q2, q1), esub(q3, q2)) : zero;
+    bool s32;
+    return project6_bounded(axis_of(k, t), zero, p2, p3, q1, q2, q3, s32) == 0u ? kPass1Separated : kPass1Undecided;
+}
+
+__global__ void __launch_bounds__(kDetectThreads) k_prec_classify(DetectArgs a)
+{
+    const uint32_t n = min(a.counts[kCountCandSlots], a.cand_cap);
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t* hit_list = a.prec_lists;
+    uint32_t* recheck = a.prec_lists + a.cand_cap;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        bool hit = false, to_hits = false, to_recheck = false;
+        uint4 rec = make_uint4(0, 0, 0, 0);
+        if (i < n) {
+            V3 P1, P2, P3, Q1, Q2, Q3;
+            load_tris(a, a.cand[i], P1, P2, P3, Q1, Q2, Q3, rec);
+            if (veq(P1, Q1) || veq(P1, Q2) || veq(P1, Q3) || veq(P2, Q1) || veq(P2, Q2) || veq(P2, Q3) ||
+                veq(P3, Q1) || veq(P3, Q2) || veq(P3, Q3)) {
+                hit = true;  // a shared vertex: never separated, in any arithmetic
+            } else {
+                const uint32_t k = tri_first_separating_axis(P1, P2, P3, Q1, Q2, Q3);
+                if (k == 17) to_hits = true;
+                else to_recheck = bounded_axis_separates(k, P1, P2, P3, Q1, Q2, Q3) != kPass1Separated;
+            }
+        }
+        append_hit(a, hit, rec, lane);
+        const uint32_t ph = warp_append(a.counts + kCountPrecHits, to_hits, lane);
+        if (to_hits) hit_list[ph] = i;
+        const uint32_t pr = warp_append(a.counts + kCountPrecRecheck, to_recheck, lane);
+        if (to_recheck) recheck[pr] = i;
+    }
+}
+
+__global__ void __launch_bounds__(kDetectThreads) k_prec_settle(DetectArgs a)
+{
+    const uint32_t n_hits = min(a.counts[kCountPrecHits], a.cand_cap);
+    const uint32_t n = n_hits + min(a.counts[kCountPrecRecheck], a.cand_cap);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+    uint2* fp64_list = (uint2*)(a.prec_lists + 2 * (size_t)a.cand_cap);
+    for (uint32_t base = warp * 32; base < n; base += n_warps * 32) {
+        const uint32_t j = base + lane;
+        bool hit = false, queue = false;
+        uint4 rec = make_uint4(0, 0, 0, 0);
+        uint32_t i = 0, mask = 0;
+        if (j < n) {
+            i = j < n_hits ? a.prec_lists[j] : a.prec_lists[a.cand_cap + (j - n_hits)];
+            V3 P1, P2, P3, Q1, Q2, Q3;
+            load_tris(a, a.cand[i], P1, P2, P3, Q1, Q2, Q3, rec);
+            bool hit32 = false;
+            const uint32_t r = tri_pass1(P1, P2, P3, Q1, Q2, Q3, mask, hit32);
+            if (r == kPass1Hit) hit = true;
+            else if (r == kPass1Undecided) {
+                queue = true;
+                mask |= hit32 ? 0x80000000u : 0u;
+            }
+        }
+        append_hit(a, hit, rec, lane);
+        const uint32_t q = warp_append(a.counts + kCountPrecFp64, queue, lane);
+        if (queue) fp64_list[q] = make_uint2(i, mask);
+    }
+}
+
+// FP64 axis evaluation with every lane on the same instructions whatever its
+// axis: the face normals n1 = e1 x e2 and m1 = f1 x f2 are formed once per
+// candidate (FP64Tri), and per axis the cross product's two factors are
+// picked by selects (integer work) before ONE FP64 cross product and the
+// projections, so lanes on different kinds of axes do not issue their FP64
+// instructions apart (each FP64 warp instruction takes the SM's FP64 pipe for
+// many cycles). The operations and their order are the FP64 formula's
+// (axis_overlaps_fp64); the projection of p1 = 0 is 0 in any order.
+struct FP64Tri {
+    D6 r;
+    D3 n1, m1;
+};
+__device__ __forceinline__ FP64Tri fp64_tri(const V3& P1, const V3& P2, const V3& P3, const V3& Q1, const V3& Q2,
+                                            const V3& Q3)
+{
+    FP64Tri t;
+    t.r = fp64_relative(P1, P2, P3, Q1, Q2, Q3);
+    const D3 p1{0.0, 0.0, 0.0};
+    t.n1 = dcross(dsub(t.r.p2, p1), dsub(t.r.p3, t.r.p2));
+    t.m1 = dcross(dsub(t.r.q2, t.r.q1), dsub(t.r.q3, t.r.q2));
+    return t;
+}
+__device__ __forceinline__ D3 dsel(bool c, const D3& a, const D3& b)
+{
+    return D3{c ? a.x : b.x, c ? a.y : b.y, c ? a.z : b.z};
+}
+__device__ __forceinline__ bool axis_overlaps_fp64_uniform(uint32_t k, const FP64Tri& t)
+{
+    const D3 z{0.0, 0.0, 0.0};
+    const D6& r = t.r;
+    // e_i = (p2 - p1, p3 - p2, p1 - p3), f_j = (q2 - q1, q3 - q2, q1 - q3)
+    const uint32_t i = k < 11 ? (k - 2) / 3 : k - 11;
+    const uint32_t j = k < 11 ? (k - 2) % 3 : k - 14;
+    const D3 E = dsub(dsel(i == 0, r.p2, dsel(i == 1, r.p3, z)), dsel(i == 0, z, dsel(i == 1, r.p2, r.p3)));
+    const D3 F = dsub(dsel(j == 0, r.q2, dsel(j == 1, r.q3, r.q1)), dsel(j == 0, r.q1, dsel(j == 1, r.q2, r.q3)));
+    const D3 X = dsel(k >= 14, F, E);
+    const D3 Y = dsel(k < 11, F, dsel(k < 14, t.n1, t.m1));
+    const D3 c = dcross(X, Y);
+    const D3 ax = dsel(k == 0, t.n1, dsel(k == 1, t.m1, c));
+    const double P2 = ddot(ax, r.p2), P3 = ddot(ax, r.p3);
+    const double Q1 = ddot(ax, r.q1), Q2 = ddot(ax, r.q2), Q3 = ddot(ax, r.q3);
+    const double P1 = 0.0;
+    const double mx1 = fmax(fmax(P1, P2), P3), mn1 = fmin(fmin(P1, P2), P3);
+    const double mx2 = fmax(fmax(Q1, Q2), Q3), mn2 = fmin(fmin(Q1, Q2), Q3);
+    return !(mn1 > mx2) && !(mn2 > mx1);
+}
+
+// The FP64 list in lockstep: every lane holds one undecided candidate and
+// evaluates ONE of its undecided axes (in order) per iteration, so the FP64
+// pipe sees full warps however many axes each candidate needs; a lane whose
+// candidate is decided (an axis separates: no hit; none left: hit) takes the
+// next one from the warp's range, 16 lanes at a time (a refill costs the
+// chain candidate -> faces -> vertices).
+__global__ void __launch_bounds__(kDetectThreads) k_prec_fp64(DetectArgs a)
+{
+    const uint32_t n = min(a.counts[kCountPrecFp64], a.cand_cap);
+    const uint2* list = (const uint2*)(a.prec_lists + 2 * (size_t)a.cand_cap);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t per = (n + n_warps - 1) / n_warps;
+    const uint32_t lo = min(n, warp * per), hi = min(n, lo + per);
+    uint32_t next = lo;  // warp-uniform
+    bool busy = false;
+    uint32_t mask = 0, evaluated = 0, dis = 0, cands = 0;
+    FP64Tri t{};
+    uint4 rec = make_uint4(0, 0, 0, 0);
+    for (;;) {
+        const uint32_t idle = __ballot_sync(0xffffffffu, !busy);
+        const bool refill = __popc(idle) >= 16 || idle == 0xffffffffu;
+        const uint32_t take = refill ? min((uint32_t)__popc(idle), hi - next) : 0u;
+        const uint32_t rank = __popc(idle & ((1u << lane) - 1u));
+        if (!busy && rank < take) {
+            const uint2 item = list[next + rank];
+            V3 P1, P2, P3, Q1, Q2, Q3;
+            load_tris(a, a.cand[item.x], P1, P2, P3, Q1, Q2, Q3, rec);
+            t = fp64_tri(P1, P2, P3, Q1, Q2, Q3);
+            mask = item.y;
+            busy = true;
+            ++cands;
+        }
+        next += take;
+        bool hit = false;
+        if (busy) {
+            const uint32_t k = __ffs(mask & 0x1ffffu) - 1;
+            mask &= mask - 1;  // the lowest set bit is the axis just taken
+            ++evaluated;
+            const bool overlaps = axis_overlaps_fp64_uniform(k, t);
+            if (!overlaps || (mask & 0x1ffffu) == 0) {
+                busy = false;
+                hit = overlaps;
+                dis += hit != ((mask >> 31) != 0u) ? 1u : 0u;
+            }
+        }
+        append_hit(a, hit, rec, lane);
+        if (!__any_sync(0xffffffffu, busy) && next >= hi) break;
+    }
+    const uint32_t axes = __reduce_add_sync(0xffffffffu, evaluated);
+    const uint32_t nc = __reduce_add_sync(0xffffffffu, cands);
+    const uint32_t nd = __reduce_add_sync(0xffffffffu, dis);
+    if (lane == 0) {
+        if (axes) atomicAdd(a.counts + kCountFp64Axes, axes);
+        if (nc) atomicAdd(a.counts + kCountFp64Cands, nc);
+        if (nd) atomicAdd(a.counts + kCountDisagree, nd);
+    }
+}
+
+#ifndef OIBVH_PREC_PASSES
+#define OIBVH_PREC_PASSES 1
+#endif
+
 // The traversal kernels' fused narrow phase is the float test only; precision
 // mode runs the broad phase alone and then k_narrow_prec.
 static inline bool fused_precision(const DetectArgs& a) { return a.precision && a.fuse_narrow; }
@@ -1129,6 +1375,13 @@ int walk_blocks_per_sm(uint32_t walk_cap, bool fused)
 
 cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s)
 {
+    if (a.precision && OIBVH_PREC_PASSES && a.prec_lists) {
+        note_launches(3);
+        k_prec_classify<<<a.grid, kDetectThreads, 0, s>>>(a);
+        k_prec_settle<<<a.grid, kDetectThreads, 0, s>>>(a);
+        k_prec_fp64<<<a.grid, kDetectThreads, 0, s>>>(a);
+        return cudaGetLastError();
+    }
     note_launches(1);
     if (a.precision) k_narrow_prec<<<a.grid, kDetectThreads, 0, s>>>(a);
     else k_narrow<<<a.grid, kDetectThreads, 0, s>>>(a);

@@ -171,6 +171,7 @@ struct oibvh_scene_s {
     DevBuf<uint64_t> front0, front1, cand;
     DevBuf<uint4> hits;
     DevBuf<uint32_t> counts;
+    DevBuf<uint32_t> prec_lists;  // precision narrow phase: float-hit, recheck and FP64 lists (4 x cand_cap)
     PinnedBuf<TreeView> h_views;
     PinnedBuf<PairView> h_pairs;
     PinnedBuf<uint32_t> h_counts;
@@ -495,8 +496,12 @@ int narrow_pass(oibvh_scene_s* s, uint32_t np, uint64_t hits_before, cudaStream_
         CUDA_TRY(cudaMemcpyAsync(s->counts.p, s->h_counts.p, 2 * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
         CUDA_TRY(cudaMemcpyAsync(s->counts.p + kCountFp64Axes, s->h_counts.p + kCountFp64Axes,
                                  (kCountWork0 - kCountFp64Axes) * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+        const void* lists_before = s->prec_lists.p;
+        if (s->precision) OK_TRY(s->prec_lists.ensure(4 * (size_t)s->cand_cap, "cudaMalloc(precision lists)"));
+        if (s->prec_lists.p != lists_before) s->frame_stale = true;  // a captured frame used the old lists
         DetectArgs a{};
         a.precision = s->precision;
+        a.prec_lists = s->precision ? s->prec_lists.p : nullptr;
         a.trees = s->views.p;
         a.pairs = s->pairv.p;
         a.n_pairs = np;
@@ -1438,6 +1443,7 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
         // split narrow phase: the candidates of the whole frame are stored
         s->cand_cap = std::max(s->cand_cap, grow_cap(2 * s->cand_count, s->cand_cap));
         OK_TRY(s->cand.ensure(s->cand_cap, "cudaMalloc(candidates)"));
+        OK_TRY(s->prec_lists.ensure(4 * (size_t)s->cand_cap, "cudaMalloc(precision lists)"));
     }
     OK_TRY(s->h_frame_counts.ensure(kCountTotal, "cudaMallocHost(frame counts)"));
     PassPlan plan;
@@ -1471,6 +1477,7 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
     a.fuse_narrow = s->precision ? 0u : 1u;
     a.cand = s->precision ? s->cand.p : nullptr;
     a.cand_cap = s->precision ? s->cand_cap : 0u;
+    a.prec_lists = s->precision ? s->prec_lists.p : nullptr;
     a.grid = walk_grid(s, !s->precision);
     a.handoff = s->tune_handoff;
     a.walk_cap = s->tune_walk_cap;

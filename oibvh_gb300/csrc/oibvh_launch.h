@@ -109,6 +109,8 @@ struct DetectArgs {
     uint4* hits;
     uint32_t hit_cap;
     uint32_t* counts;      // see kCount* below
+    uint32_t* prec_lists;  // precision mode, 4 x cand_cap words: float-hit list, recheck list (candidate
+                           // indices), then the FP64 list ((candidate index, axis mask) pairs)
     uint32_t fuse_narrow;  // 1: test candidates in the traversal; 0: store them
     int grid;              // CTAs of the grid-stride / persistent kernels
     uint32_t handoff;      // front width at which k_top hands over to the walkers (<= 8192)
@@ -127,11 +129,14 @@ cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s);
 // counts[]: hits, flags, candidates found, candidate slots used (broad-only),
 // BVTT pairs tested, (precision mode) axes evaluated in FP64, candidates with
 // at least one such axis, candidates whose float and FP64 answers differ,
+// the sizes of the float-hit, recheck and FP64 lists of the precision narrow phase,
 // then the work-list size of each traversal round (list
 // 0: the overlapping start pairs; list 1: the front k_top hands over; list
 // r+1: what walk round r spilled).
 constexpr uint32_t kMaxRounds = 16;
 constexpr uint32_t kCountHits = 0, kCountFlags = 1, kCountCands = 2, kCountCandSlots = 3, kCountTested = 4,
-                   kCountFp64Axes = 5, kCountFp64Cands = 6, kCountDisagree = 7, kCountWork0 = 8, kCountTotal = kCountWork0 + kMaxRounds + 1;
+                   kCountFp64Axes = 5, kCountFp64Cands = 6, kCountDisagree = 7, kCountPrecHits = 8,
+                   kCountPrecRecheck = 9, kCountPrecFp64 = 10, kCountWork0 = 11,
+                   kCountTotal = kCountWork0 + kMaxRounds + 1;
 
 } // namespace oibvh
