@@ -1192,6 +1192,13 @@ __device__ __forceinline__ FP64Tri fp64_tri(const V3& P1, const V3& P2, const V3
     t.m1 = dcross(dsub(t.r.q2, t.r.q1), dsub(t.r.q3, t.r.q2));
     return t;
 }
+// A finite double as an unsigned key with the same order (-0 and +0 equal).
+__device__ __forceinline__ uint64_t ordered_key(double d)
+{
+    uint64_t b = (uint64_t)__double_as_longlong(d);
+    if (b == 0x8000000000000000ull) b = 0;
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
 __device__ __forceinline__ D3 dsel(bool c, const D3& a, const D3& b)
 {
     return D3{c ? a.x : b.x, c ? a.y : b.y, c ? a.z : b.z};
@@ -1209,13 +1216,19 @@ __device__ __forceinline__ bool axis_overlaps_fp64_uniform(uint32_t k, const FP6
     const D3 Y = dsel(k < 11, F, dsel(k < 14, t.n1, t.m1));
     const D3 c = dcross(X, Y);
     const D3 ax = dsel(k == 0, t.n1, dsel(k == 1, t.m1, c));
-    const double P2 = ddot(ax, r.p2), P3 = ddot(ax, r.p3);
-    const double Q1 = ddot(ax, r.q1), Q2 = ddot(ax, r.q2), Q3 = ddot(ax, r.q3);
-    const double P1 = 0.0;
-    const double mx1 = fmax(fmax(P1, P2), P3), mn1 = fmin(fmin(P1, P2), P3);
-    const double mx2 = fmax(fmax(Q1, Q2), Q3), mn2 = fmin(fmin(Q1, Q2), Q3);
+    // the comparisons on integer keys: the projections are finite, and after
+    // -0 is made +0 the key order is the double order
+    const uint64_t P1 = ordered_key(0.0), P2 = ordered_key(ddot(ax, r.p2)), P3 = ordered_key(ddot(ax, r.p3));
+    const uint64_t Q1 = ordered_key(ddot(ax, r.q1)), Q2 = ordered_key(ddot(ax, r.q2)), Q3 = ordered_key(ddot(ax, r.q3));
+    const uint64_t mx1 = max(max(P1, P2), P3), mn1 = min(min(P1, P2), P3);
+    const uint64_t mx2 = max(max(Q1, Q2), Q3), mn2 = min(min(Q1, Q2), Q3);
     return !(mn1 > mx2) && !(mn2 > mx1);
 }
+
+#ifndef OIBVH_FP64_REFILL
+#define OIBVH_FP64_REFILL 16
+#endif
+constexpr uint32_t kFp64Refill = OIBVH_FP64_REFILL;  // idle lanes that trigger a refill
 
 // The FP64 list in lockstep: every lane holds one undecided candidate and
 // evaluates ONE of its undecided axes (in order) per iteration, so the FP64
@@ -1239,7 +1252,7 @@ __global__ void __launch_bounds__(kDetectThreads) k_prec_fp64(DetectArgs a)
     uint4 rec = make_uint4(0, 0, 0, 0);
     for (;;) {
         const uint32_t idle = __ballot_sync(0xffffffffu, !busy);
-        const bool refill = __popc(idle) >= 16 || idle == 0xffffffffu;
+        const bool refill = __popc(idle) >= kFp64Refill || idle == 0xffffffffu;
         const uint32_t take = refill ? min((uint32_t)__popc(idle), hi - next) : 0u;
         const uint32_t rank = __popc(idle & ((1u << lane) - 1u));
         if (!busy && rank < take) {
