@@ -315,6 +315,8 @@ typedef struct oibvh_detect_stats {
     uint64_t fp64_axes;      /* precision mode: axis tests evaluated again in FP64 */
     uint64_t fp64_candidates;     /* precision mode: candidates with at least one such axis */
     uint64_t fp32_disagreements;  /* precision mode: candidates where float and FP64 answers differ */
+    uint64_t bounded_candidates;  /* precision mode: candidates the plain float test and its margin bound
+                                     left open, which took the bounded float pass */
 } oibvh_detect_stats;
 int oibvh_scene_get_stats(oibvh_scene_t s, oibvh_detect_stats* out);
 

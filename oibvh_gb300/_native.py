@@ -46,6 +46,7 @@ class DetectStats(ctypes.Structure):
         ("fp64_axes", ctypes.c_uint64),
         ("fp64_candidates", ctypes.c_uint64),
         ("fp32_disagreements", ctypes.c_uint64),
+        ("bounded_candidates", ctypes.c_uint64),
     ]
 
 

@@ -1052,32 +1052,66 @@ __global__ void __launch_bounds__(kDetectThreads, 2) k_narrow_prec(DetectArgs a)
 // The pair set is the all-FP64 one by construction, as in k_narrow_prec.
 // ---------------------------------------------------------------------------
 
+// project6 of the float test, which also clears `robust` unless both of the
+// axis' margins are below -B (used only when no axis separates).
+__device__ __forceinline__ bool project6_robust(const V3& ax, const V3& p1, const V3& p2, const V3& p3, const V3& q1,
+                                                const V3& q2, const V3& q3, float B, bool& robust)
+{
+    const float P1 = vdot(ax, p1), P2 = vdot(ax, p2), P3 = vdot(ax, p3);
+    const float Q1 = vdot(ax, q1), Q2 = vdot(ax, q2), Q3 = vdot(ax, q3);
+    const float mx1 = fmaxf(fmaxf(P1, P2), P3), mn1 = fminf(fminf(P1, P2), P3);
+    const float mx2 = fmaxf(fmaxf(Q1, Q2), Q3), mn2 = fminf(fminf(Q1, Q2), Q3);
+    if (mn1 > mx2) return false;
+    if (mn2 > mx1) return false;
+    robust = robust && __fsub_rn(mn1, mx2) < -B && __fsub_rn(mn2, mx1) < -B;
+    return true;
+}
+
 // The first of the 17 axes (reference order) that separates the triangles
-// in float, 17 when none does (then they intersect in float).
+// in float, 17 when none does (then they intersect in float). When none
+// does, `robust` tells whether every axis overlaps by more than a bound on
+// the float and FP64 errors: then the triangles intersect in FP64 as well.
+//
+// The bound follows from the largest relative coordinate A (|p_i|, |q_j| <=
+// A; relative extents in [2^-20, 2^20], else never robust) by propagating
+// the rounding of each operation (u = 2^-24): edges |e| <= 2A (error 4uA),
+// edge x edge and the normals |c| <= 8A^2 (48uA^2), edge x normal 32A^3
+// (320uA^3); a projection onto a degree-2 axis errs by at most 232uA^3, a
+// margin by 512uA^3 = 2^-15 A^3; onto a degree-3 axis 1312uA^4, a margin by
+// 2816uA^4 < 2^-12 A^4. FP64 errs by 2^-29 of that. B = twice (2^-14 A^3)
+// and four times (2^-10 A^4) these, covering second-order terms, underflow
+// (2^-149 per product, far below 2^-90) and the rounding of B itself.
 __device__ __forceinline__ uint32_t tri_first_separating_axis(const V3& P1, const V3& P2, const V3& P3, const V3& Q1,
-                                                              const V3& Q2, const V3& Q3)
+                                                              const V3& Q2, const V3& Q3, bool& robust)
 {
     const V3 p1{0.0f, 0.0f, 0.0f};
     const V3 p2 = vsub(P2, P1), p3 = vsub(P3, P1);
     const V3 q1 = vsub(Q1, P1), q2 = vsub(Q2, P1), q3 = vsub(Q3, P1);
+    float A = fmaxf(fmaxf(fmaxf(fabsf(p2.x), fabsf(p2.y)), fmaxf(fabsf(p2.z), fabsf(p3.x))),
+                    fmaxf(fmaxf(fabsf(p3.y), fabsf(p3.z)), fmaxf(fabsf(q1.x), fabsf(q1.y))));
+    A = fmaxf(A, fmaxf(fmaxf(fabsf(q1.z), fabsf(q2.x)), fmaxf(fabsf(q2.y), fabsf(q2.z))));
+    A = fmaxf(A, fmaxf(fmaxf(fabsf(q3.x), fabsf(q3.y)), fabsf(q3.z)));
+    robust = A >= 0x1p-20f && A <= 0x1p20f;
+    const float A3 = A * A * A;
+    const float B3 = 0x1p-14f * A3, B4 = 0x1p-10f * A3 * A;
     const V3 e1 = vsub(p2, p1), e2 = vsub(p3, p2), e3 = vsub(p1, p3);
     const V3 f1 = vsub(q2, q1), f2 = vsub(q3, q2), f3 = vsub(q1, q3);
     const V3 n1 = vcross(e1, e2);
-    if (!project6(n1, p1, p2, p3, q1, q2, q3)) return 0;
+    if (!project6_robust(n1, p1, p2, p3, q1, q2, q3, B3, robust)) return 0;
     const V3 m1 = vcross(f1, f2);
-    if (!project6(m1, p1, p2, p3, q1, q2, q3)) return 1;
+    if (!project6_robust(m1, p1, p2, p3, q1, q2, q3, B3, robust)) return 1;
     const V3 E[3] = {e1, e2, e3}, F[3] = {f1, f2, f3};
 #pragma unroll
     for (uint32_t i = 0; i < 3; ++i)
 #pragma unroll
         for (uint32_t j = 0; j < 3; ++j)
-            if (!project6(vcross(E[i], F[j]), p1, p2, p3, q1, q2, q3)) return 2 + 3 * i + j;
+            if (!project6_robust(vcross(E[i], F[j]), p1, p2, p3, q1, q2, q3, B3, robust)) return 2 + 3 * i + j;
 #pragma unroll
     for (uint32_t i = 0; i < 3; ++i)
-        if (!project6(vcross(E[i], n1), p1, p2, p3, q1, q2, q3)) return 11 + i;
+        if (!project6_robust(vcross(E[i], n1), p1, p2, p3, q1, q2, q3, B4, robust)) return 11 + i;
 #pragma unroll
     for (uint32_t j = 0; j < 3; ++j)
-        if (!project6(vcross(F[j], m1), p1, p2, p3, q1, q2, q3)) return 14 + j;
+        if (!project6_robust(vcross(F[j], m1), p1, p2, p3, q1, q2, q3, B4, robust)) return 14 + j;
     return 17;
 }
 
@@ -1126,9 +1160,14 @@ __global__ void __launch_bounds__(kDetectThreads) k_prec_classify(DetectArgs a)
                 veq(P3, Q1) || veq(P3, Q2) || veq(P3, Q3)) {
                 hit = true;  // a shared vertex: never separated, in any arithmetic
             } else {
-                const uint32_t k = tri_first_separating_axis(P1, P2, P3, Q1, Q2, Q3);
-                if (k == 17) to_hits = true;
-                else to_recheck = bounded_axis_separates(k, P1, P2, P3, Q1, Q2, Q3) != kPass1Separated;
+                bool robust;
+                const uint32_t k = tri_first_separating_axis(P1, P2, P3, Q1, Q2, Q3, robust);
+                if (k == 17) {
+                    if (robust) hit = true;  // every axis overlaps beyond the error bounds
+                    else to_hits = true;
+                } else {
+                    to_recheck = bounded_axis_separates(k, P1, P2, P3, Q1, Q2, Q3) != kPass1Separated;
+                }
             }
         }
         append_hit(a, hit, rec, lane);
@@ -1187,8 +1226,7 @@ __device__ __forceinline__ FP64Tri fp64_tri(const V3& P1, const V3& P2, const V3
 {
     FP64Tri t;
     t.r = fp64_relative(P1, P2, P3, Q1, Q2, Q3);
-    const D3 p1{0.0, 0.0, 0.0};
-    t.n1 = dcross(dsub(t.r.p2, p1), dsub(t.r.p3, t.r.p2));
+    t.n1 = dcross(t.r.p2, dsub(t.r.p3, t.r.p2));  // e1 = p2 - p1 = p2 exactly (p1 = +0)
     t.m1 = dcross(dsub(t.r.q2, t.r.q1), dsub(t.r.q3, t.r.q2));
     return t;
 }
@@ -1203,18 +1241,23 @@ __device__ __forceinline__ D3 dsel(bool c, const D3& a, const D3& b)
 {
     return D3{c ? a.x : b.x, c ? a.y : b.y, c ? a.z : b.z};
 }
-__device__ __forceinline__ bool axis_overlaps_fp64_uniform(uint32_t k, const FP64Tri& t)
+// `edges`: some lane of the warp is on an edge axis (k >= 2); when none is,
+// the warp skips the edge cross product (the plane axes are n1 and m1).
+__device__ __forceinline__ bool axis_overlaps_fp64_uniform(uint32_t k, const FP64Tri& t, bool edges)
 {
     const D3 z{0.0, 0.0, 0.0};
     const D6& r = t.r;
-    // e_i = (p2 - p1, p3 - p2, p1 - p3), f_j = (q2 - q1, q3 - q2, q1 - q3)
-    const uint32_t i = k < 11 ? (k - 2) / 3 : k - 11;
-    const uint32_t j = k < 11 ? (k - 2) % 3 : k - 14;
-    const D3 E = dsub(dsel(i == 0, r.p2, dsel(i == 1, r.p3, z)), dsel(i == 0, z, dsel(i == 1, r.p2, r.p3)));
-    const D3 F = dsub(dsel(j == 0, r.q2, dsel(j == 1, r.q3, r.q1)), dsel(j == 0, r.q1, dsel(j == 1, r.q2, r.q3)));
-    const D3 X = dsel(k >= 14, F, E);
-    const D3 Y = dsel(k < 11, F, dsel(k < 14, t.n1, t.m1));
-    const D3 c = dcross(X, Y);
+    D3 c = z;
+    if (edges) {
+        // e_i = (p2 - p1, p3 - p2, p1 - p3), f_j = (q2 - q1, q3 - q2, q1 - q3)
+        const uint32_t i = k < 11 ? (k - 2) / 3 : k - 11;
+        const uint32_t j = k < 11 ? (k - 2) % 3 : k - 14;
+        const D3 E = dsub(dsel(i == 0, r.p2, dsel(i == 1, r.p3, z)), dsel(i == 0, z, dsel(i == 1, r.p2, r.p3)));
+        const D3 F = dsub(dsel(j == 0, r.q2, dsel(j == 1, r.q3, r.q1)), dsel(j == 0, r.q1, dsel(j == 1, r.q2, r.q3)));
+        const D3 X = dsel(k >= 14, F, E);
+        const D3 Y = dsel(k < 11, F, dsel(k < 14, t.n1, t.m1));
+        c = dcross(X, Y);
+    }
     const D3 ax = dsel(k == 0, t.n1, dsel(k == 1, t.m1, c));
     // the comparisons on integer keys: the projections are finite, and after
     // -0 is made +0 the key order is the double order
@@ -1229,6 +1272,49 @@ __device__ __forceinline__ bool axis_overlaps_fp64_uniform(uint32_t k, const FP6
 #define OIBVH_FP64_REFILL 16
 #endif
 constexpr uint32_t kFp64Refill = OIBVH_FP64_REFILL;  // idle lanes that trigger a refill
+
+// FP64 setups (fp64_tri and the hit record) of the FP64 list's first
+// fp64_tri_cap entries, one entry per lane: formed here with every lane of a
+// warp busy, where k_prec_fp64 would form them in its refills with only the
+// refilling lanes. Structure of arrays: row r of entry i at r * cap + i.
+__device__ __forceinline__ void fp64_tri_store(double* base, uint32_t cap, uint32_t i, const FP64Tri& t, const uint4& rec)
+{
+    const double v[21] = {t.r.p2.x, t.r.p2.y, t.r.p2.z, t.r.p3.x, t.r.p3.y, t.r.p3.z, t.r.q1.x,
+                          t.r.q1.y, t.r.q1.z, t.r.q2.x, t.r.q2.y, t.r.q2.z, t.r.q3.x, t.r.q3.y,
+                          t.r.q3.z, t.n1.x, t.n1.y, t.n1.z, t.m1.x, t.m1.y, t.m1.z};
+#pragma unroll
+    for (uint32_t r = 0; r < 21; ++r) base[(size_t)r * cap + i] = v[r];
+    uint64_t* w = (uint64_t*)base;
+    w[(size_t)21 * cap + i] = ((uint64_t)rec.y << 32) | rec.x;
+    w[(size_t)22 * cap + i] = ((uint64_t)rec.w << 32) | rec.z;
+}
+__device__ __forceinline__ void fp64_tri_load(const double* base, uint32_t cap, uint32_t i, FP64Tri& t, uint4& rec)
+{
+    double v[21];
+#pragma unroll
+    for (uint32_t r = 0; r < 21; ++r) v[r] = __ldcg(base + (size_t)r * cap + i);
+    t.r.p2 = D3{v[0], v[1], v[2]};
+    t.r.p3 = D3{v[3], v[4], v[5]};
+    t.r.q1 = D3{v[6], v[7], v[8]};
+    t.r.q2 = D3{v[9], v[10], v[11]};
+    t.r.q3 = D3{v[12], v[13], v[14]};
+    t.n1 = D3{v[15], v[16], v[17]};
+    t.m1 = D3{v[18], v[19], v[20]};
+    const uint64_t* w = (const uint64_t*)base;
+    const uint64_t r0 = __ldcg(w + (size_t)21 * cap + i), r1 = __ldcg(w + (size_t)22 * cap + i);
+    rec = make_uint4((uint32_t)r0, (uint32_t)(r0 >> 32), (uint32_t)r1, (uint32_t)(r1 >> 32));
+}
+__global__ void __launch_bounds__(kDetectThreads) k_prec_fp64_setup(DetectArgs a)
+{
+    const uint32_t n = min(min(a.counts[kCountPrecFp64], a.cand_cap), a.fp64_tri_cap);
+    const uint2* list = (const uint2*)(a.prec_lists + 2 * (size_t)a.cand_cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        V3 P1, P2, P3, Q1, Q2, Q3;
+        uint4 rec;
+        load_tris(a, a.cand[list[i].x], P1, P2, P3, Q1, Q2, Q3, rec);
+        fp64_tri_store(a.fp64_tri, a.fp64_tri_cap, i, fp64_tri(P1, P2, P3, Q1, Q2, Q3), rec);
+    }
+}
 
 // The FP64 list in lockstep: every lane holds one undecided candidate and
 // evaluates ONE of its undecided axes (in order) per iteration, so the FP64
@@ -1256,21 +1342,27 @@ __global__ void __launch_bounds__(kDetectThreads) k_prec_fp64(DetectArgs a)
         const uint32_t take = refill ? min((uint32_t)__popc(idle), hi - next) : 0u;
         const uint32_t rank = __popc(idle & ((1u << lane) - 1u));
         if (!busy && rank < take) {
-            const uint2 item = list[next + rank];
-            V3 P1, P2, P3, Q1, Q2, Q3;
-            load_tris(a, a.cand[item.x], P1, P2, P3, Q1, Q2, Q3, rec);
-            t = fp64_tri(P1, P2, P3, Q1, Q2, Q3);
+            const uint32_t i = next + rank;
+            const uint2 item = list[i];
+            if (i < a.fp64_tri_cap) {  // formed by k_prec_fp64_setup
+                fp64_tri_load(a.fp64_tri, a.fp64_tri_cap, i, t, rec);
+            } else {
+                V3 P1, P2, P3, Q1, Q2, Q3;
+                load_tris(a, a.cand[item.x], P1, P2, P3, Q1, Q2, Q3, rec);
+                t = fp64_tri(P1, P2, P3, Q1, Q2, Q3);
+            }
             mask = item.y;
             busy = true;
             ++cands;
         }
         next += take;
         bool hit = false;
+        const uint32_t k = busy ? __ffs(mask & 0x1ffffu) - 1 : 0u;
+        const bool edges = __any_sync(0xffffffffu, busy && k >= 2);
         if (busy) {
-            const uint32_t k = __ffs(mask & 0x1ffffu) - 1;
             mask &= mask - 1;  // the lowest set bit is the axis just taken
             ++evaluated;
-            const bool overlaps = axis_overlaps_fp64_uniform(k, t);
+            const bool overlaps = axis_overlaps_fp64_uniform(k, t, edges);
             if (!overlaps || (mask & 0x1ffffu) == 0) {
                 busy = false;
                 hit = overlaps;
@@ -1389,9 +1481,10 @@ int walk_blocks_per_sm(uint32_t walk_cap, bool fused)
 cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s)
 {
     if (a.precision && OIBVH_PREC_PASSES && a.prec_lists) {
-        note_launches(3);
+        note_launches(a.fp64_tri_cap ? 4 : 3);
         k_prec_classify<<<a.grid, kDetectThreads, 0, s>>>(a);
         k_prec_settle<<<a.grid, kDetectThreads, 0, s>>>(a);
+        if (a.fp64_tri_cap) k_prec_fp64_setup<<<a.grid, kDetectThreads, 0, s>>>(a);
         k_prec_fp64<<<a.grid, kDetectThreads, 0, s>>>(a);
         return cudaGetLastError();
     }

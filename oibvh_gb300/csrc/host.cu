@@ -172,6 +172,8 @@ struct oibvh_scene_s {
     DevBuf<uint4> hits;
     DevBuf<uint32_t> counts;
     DevBuf<uint32_t> prec_lists;  // precision narrow phase: float-hit, recheck and FP64 lists (4 x cand_cap)
+    DevBuf<double> fp64_tri;      // precision narrow phase: FP64 setups (kFp64TriRows x fp64_tri_cap)
+    uint32_t fp64_tri_cap = 0;
     PinnedBuf<TreeView> h_views;
     PinnedBuf<PairView> h_pairs;
     PinnedBuf<uint32_t> h_counts;
@@ -483,6 +485,20 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
     return OIBVH_OK;
 }
 
+// Room for the FP64 setups of the next passes: twice the FP64 list this pass
+// had (the first pass forms every setup where it is used). A captured frame
+// that used the old buffer is captured again.
+int size_fp64_setups(oibvh_scene_s* s, uint32_t fp64_list)
+{
+    const uint64_t want = std::min<uint64_t>(2ull * fp64_list, s->cand_cap);
+    if (want <= s->fp64_tri_cap) return OIBVH_OK;
+    const uint32_t cap = grow_cap((uint32_t)want, s->fp64_tri_cap);
+    OK_TRY(s->fp64_tri.ensure((size_t)kFp64TriRows * cap, "cudaMalloc(FP64 setups)"));
+    s->fp64_tri_cap = cap;
+    s->frame_stale = true;
+    return OIBVH_OK;
+}
+
 // Narrow phase over the stored candidates of the last broad pass (pairv holds
 // that pass's pair table); hits are appended after the first `hits_before`.
 int narrow_pass(oibvh_scene_s* s, uint32_t np, uint64_t hits_before, cudaStream_t st)
@@ -512,6 +528,10 @@ int narrow_pass(oibvh_scene_s* s, uint32_t np, uint64_t hits_before, cudaStream_
         a.counts = s->counts.p;
         a.grid = sm_count(s->device) * 8;
         a.fuse_narrow = 1;
+        if (s->precision) {
+            a.fp64_tri = s->fp64_tri.p;
+            a.fp64_tri_cap = s->fp64_tri_cap;
+        }
         CUDA_TRY(launch_narrow(a, st));
         CUDA_TRY(cudaMemcpyAsync(s->h_counts.p, s->counts.p, kCountTotal * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                                  st));
@@ -528,6 +548,8 @@ int narrow_pass(oibvh_scene_s* s, uint32_t np, uint64_t hits_before, cudaStream_
         s->stats.fp64_axes += c[kCountFp64Axes];
         s->stats.fp64_candidates += c[kCountFp64Cands];
         s->stats.fp32_disagreements += c[kCountDisagree];
+        s->stats.bounded_candidates += (uint64_t)c[kCountPrecHits] + c[kCountPrecRecheck];
+        if (s->precision) OK_TRY(size_fp64_setups(s, c[kCountPrecFp64]));
         return OIBVH_OK;
     }
 }
@@ -536,7 +558,7 @@ int narrow_impl(oibvh_scene_s* s, cudaStream_t st)
 {
     if (!s->cands_valid) return fail(OIBVH_ERR_STATE, "narrow phase needs a broad phase first");
     DeviceGuard g(s->device);
-    s->stats.fp64_axes = s->stats.fp64_candidates = s->stats.fp32_disagreements = 0;
+    s->stats.fp64_axes = s->stats.fp64_candidates = s->stats.fp32_disagreements = s->stats.bounded_candidates = 0;
     return narrow_pass(s, (uint32_t)s->last_pairs.size(), 0, st);
 }
 
@@ -1478,6 +1500,8 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
     a.cand = s->precision ? s->cand.p : nullptr;
     a.cand_cap = s->precision ? s->cand_cap : 0u;
     a.prec_lists = s->precision ? s->prec_lists.p : nullptr;
+    a.fp64_tri = s->precision ? s->fp64_tri.p : nullptr;
+    a.fp64_tri_cap = s->precision ? s->fp64_tri_cap : 0u;
     a.grid = walk_grid(s, !s->precision);
     a.handoff = s->tune_handoff;
     a.walk_cap = s->tune_walk_cap;
@@ -1571,6 +1595,7 @@ API int oibvh_scene_finish_frame(oibvh_scene_t s, void* stream)
     s->stats.fp64_axes = c[kCountFp64Axes];
     s->stats.fp64_candidates = c[kCountFp64Cands];
     s->stats.fp32_disagreements = c[kCountDisagree];
+    s->stats.bounded_candidates = (uint64_t)c[kCountPrecHits] + c[kCountPrecRecheck];
     uint64_t peak = 0;
     for (uint32_t k = 0; k <= s->frame_rounds + 1; ++k) peak = std::max<uint64_t>(peak, c[kCountWork0 + k]);
     s->stats.front_peak = peak;

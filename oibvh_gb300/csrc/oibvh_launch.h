@@ -111,6 +111,9 @@ struct DetectArgs {
     uint32_t* counts;      // see kCount* below
     uint32_t* prec_lists;  // precision mode, 4 x cand_cap words: float-hit list, recheck list (candidate
                            // indices), then the FP64 list ((candidate index, axis mask) pairs)
+    double* fp64_tri;      // precision mode: the FP64 list's setups, kFp64TriRows rows of fp64_tri_cap
+                           // (structure of arrays; nullptr: each is formed where it is used)
+    uint32_t fp64_tri_cap;
     uint32_t fuse_narrow;  // 1: test candidates in the traversal; 0: store them
     int grid;              // CTAs of the grid-stride / persistent kernels
     uint32_t handoff;      // front width at which k_top hands over to the walkers (<= 8192)
@@ -125,6 +128,9 @@ cudaError_t launch_walk(const DetectArgs& a, uint32_t round, cudaStream_t s);
 // default), for the fused (narrow phase inside) or the broad-only walker
 int walk_blocks_per_sm(uint32_t walk_cap = 0, bool fused = true);
 cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s);
+// Rows of a precision-mode FP64 setup: the relative vertices p2, p3, q1, q2,
+// q3 and the normals n1, m1 (x, y, z each), then the hit record (2 words).
+constexpr uint32_t kFp64TriRows = 23;
 
 // counts[]: hits, flags, candidates found, candidate slots used (broad-only),
 // BVTT pairs tested, (precision mode) axes evaluated in FP64, candidates with
