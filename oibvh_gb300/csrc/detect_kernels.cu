@@ -19,8 +19,9 @@
 // Narrow phase: overlapping leaf pairs are buffered per warp in shared memory
 // and, 32 at a time, tested inside the traversal (the kernels' <true>
 // instantiation, the float test) or stored for a separate kernel (<false>,
-// fewer registers): k_narrow (float test, split API) or k_narrow_prec
-// (precision mode: the FP64-filtered test).
+// fewer registers): k_narrow (float test, split API) or, in precision mode,
+// the FP64-filtered test's passes (k_prec_classify, k_prec_settle,
+// k_prec_fp64_setup, k_prec_fp64).
 //
 // The float triangle test reproduces the reference's CPU arithmetic
 // (src/utils/utils.cpp:71-169, glm scalar dot/cross): every product, sum and
@@ -143,18 +144,6 @@ __device__ __forceinline__ double ddot(const D3& a, const D3& b)
 {
     return __dadd_rn(__dadd_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)), __dmul_rn(a.z, b.z));
 }
-__device__ __forceinline__ bool project6_d(const D3& ax, const D3& p1, const D3& p2, const D3& p3, const D3& q1,
-                                           const D3& q2, const D3& q3)
-{
-    const double P1 = ddot(ax, p1), P2 = ddot(ax, p2), P3 = ddot(ax, p3);
-    const double Q1 = ddot(ax, q1), Q2 = ddot(ax, q2), Q3 = ddot(ax, q3);
-    const double mx1 = fmax(fmax(P1, P2), P3), mn1 = fmin(fmin(P1, P2), P3);
-    const double mx2 = fmax(fmax(Q1, Q2), Q3), mn2 = fmin(fmin(Q1, Q2), Q3);
-    if (mn1 > mx2) return false;
-    if (mn2 > mx1) return false;
-    return true;
-}
-
 // Relative vertices of the FP64 formula: p_i = P_i - P1, q_j = Q_j - P1.
 struct D6 {
     D3 p2, p3, q1, q2, q3;
@@ -164,39 +153,6 @@ __device__ __forceinline__ D6 fp64_relative(const V3& P1, const V3& P2, const V3
 {
     const D3 dP1 = to_d(P1);
     return D6{dsub(to_d(P2), dP1), dsub(to_d(P3), dP1), dsub(to_d(Q1), dP1), dsub(to_d(Q2), dP1), dsub(to_d(Q3), dP1)};
-}
-
-// Axis k of the 17 (0: n1, 1: m1, 2 + 3i + j: e_i x f_j, 11 + i: e_i x n1,
-// 14 + j: f_j x m1) in FP64: true when it does NOT separate the triangles.
-// Edges as the FP64 formula forms them: e1 = p2 - p1, e2 = p3 - p2,
-// e3 = p1 - p3, f1 = q2 - q1, f2 = q3 - q2, f3 = q1 - q3 (p1 = 0).
-__device__ __forceinline__ bool axis_overlaps_fp64(uint32_t k, const D6& r)
-{
-    const D3 p1{0.0, 0.0, 0.0};
-    // only the edges this axis needs, each formed as the FP64 formula forms it
-    auto e = [&](uint32_t i) { return i == 0 ? dsub(r.p2, p1) : (i == 1 ? dsub(r.p3, r.p2) : dsub(p1, r.p3)); };
-    auto f = [&](uint32_t j) { return j == 0 ? dsub(r.q2, r.q1) : (j == 1 ? dsub(r.q3, r.q2) : dsub(r.q1, r.q3)); };
-    D3 ax;
-    if (k == 0) ax = dcross(e(0), e(1));
-    else if (k == 1) ax = dcross(f(0), f(1));
-    else if (k < 11) ax = dcross(e((k - 2) / 3), f((k - 2) % 3));
-    else if (k < 14) ax = dcross(e(k - 11), dcross(e(0), e(1)));
-    else ax = dcross(f(k - 14), dcross(f(0), f(1)));
-    return project6_d(ax, p1, r.p2, r.p3, r.q1, r.q2, r.q3);
-}
-
-// FP64 tests of the axes in `mask`, in order, until one separates.
-__device__ __noinline__ bool fp64_axes_separate(uint32_t mask, V3 P1, V3 P2, V3 P3, V3 Q1, V3 Q2, V3 Q3,
-                                                uint32_t& evaluated)
-{
-    const D6 r = fp64_relative(P1, P2, P3, Q1, Q2, Q3);
-    while (mask) {
-        const uint32_t k = __ffs(mask) - 1;
-        mask &= mask - 1;
-        ++evaluated;
-        if (!axis_overlaps_fp64(k, r)) return true;
-    }
-    return false;
 }
 
 // A float vector with a componentwise bound on its error.
@@ -826,12 +782,8 @@ __global__ void __launch_bounds__(kDetectThreads) k_narrow(DetectArgs a)
     }
 }
 
-// Narrow phase of precision mode over stored candidates. Pass 1 (float with
-// error bounds) takes one candidate per lane; candidates it leaves undecided
-// are queued per warp in shared memory and settled in FP64 32 at a time, so
-// the FP64 work runs in full warps instead of in the few lanes that need it.
-constexpr uint32_t kFp64Queue = 64;  // <= 31 left over + 32 added per round
-
+// Precision mode's narrow phase over stored candidates: one candidate's
+// triangles, and a hit appended with one atomic per warp.
 __device__ __forceinline__ void load_tris(const DetectArgs& a, uint64_t c, V3& P1, V3& P2, V3& P3, V3& Q1, V3& Q2,
                                           V3& Q3, uint4& rec)
 {
@@ -858,37 +810,8 @@ __device__ __forceinline__ void append_hit(const DetectArgs& a, bool hit, const 
     }
 }
 
-// FP64 stage of `count` queued candidates (one per lane).
-__device__ __forceinline__ void settle_fp64(const DetectArgs& a, const uint64_t* qc, const uint32_t* qm,
-                                            uint32_t count, uint32_t lane)
-{
-    bool hit = false, disagree = false;
-    uint32_t evaluated = 0;
-    uint4 rec = make_uint4(0, 0, 0, 0);
-    if (lane < count) {
-        V3 P1, P2, P3, Q1, Q2, Q3;
-        load_tris(a, qc[lane], P1, P2, P3, Q1, Q2, Q3, rec);
-        const uint32_t m = qm[lane];
-        hit = !fp64_axes_separate(m & 0x1ffffu, P1, P2, P3, Q1, Q2, Q3, evaluated);
-        disagree = hit != ((m >> 31) != 0u);
-    }
-    append_hit(a, hit, rec, lane);
-    const uint32_t axes = __reduce_add_sync(0xffffffffu, evaluated);
-    const uint32_t cands = __popc(__ballot_sync(0xffffffffu, lane < count));
-    const uint32_t dis = __popc(__ballot_sync(0xffffffffu, disagree));
-    if (lane == 0) {
-        if (axes) atomicAdd(a.counts + kCountFp64Axes, axes);
-        if (cands) atomicAdd(a.counts + kCountFp64Cands, cands);
-        if (dis) atomicAdd(a.counts + kCountDisagree, dis);
-    }
-}
-
-// Pass 1 in lockstep: every lane holds one candidate and evaluates ONE axis
-// of it per iteration with the same instructions (the axis is chosen by
-// selects, not branches); a lane whose candidate is decided takes the next
-// one from the warp's range. Axis order: the two face normals, the six
-// in-plane axes, then the nine edge-edge axes (coplanar neighbours separate
-// early on the in-plane ones).
+// One candidate's relative vertices and face normals (with error bounds),
+// from which axis_of forms any of the 17 axes with selects only.
 struct LaneTri {
     V3 p2, p3, q1, q2, q3;  // relative vertices (p1 = 0); their bound is u|x|
     EV3 n1, m1;             // face normals with error bounds
@@ -922,134 +845,26 @@ __device__ __forceinline__ EV3 axis_of(uint32_t k, const LaneTri& t)
     return esel(k == 0, t.n1, esel(k == 1, t.m1, ecross(X, Y)));
 }
 
-constexpr int kRefillBatch = 16;
-__constant__ uint8_t c_axis_order[17] = {0, 1, 11, 12, 13, 14, 15, 16, 2, 3, 4, 5, 6, 7, 8, 9, 10};
-
-__global__ void __launch_bounds__(kDetectThreads, 2) k_narrow_prec(DetectArgs a)
-{
-    __shared__ uint64_t s_qc[kDetectThreads / 32][kFp64Queue];
-    __shared__ uint32_t s_qm[kDetectThreads / 32][kFp64Queue];
-    const uint32_t n = min(a.counts[kCountCandSlots], a.cand_cap);
-    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
-    // this warp's contiguous range of candidates
-    const uint32_t per = (n + n_warps - 1) / n_warps;
-    const uint32_t lo = min(n, warp * per), hi = min(n, lo + per);
-    uint64_t* qc = s_qc[wib];
-    uint32_t* qm = s_qm[wib];
-    uint32_t qn = 0;    // FP64 queue fill (warp-uniform)
-    uint32_t next = lo; // next candidate of the range (warp-uniform)
-
-    bool busy = false;  // this lane holds a candidate in pass 1
-    uint64_t c = 0;
-    LaneTri t;
-    uint32_t step = 0, undecided = 0;
-    bool sep32 = false;
-    for (;;) {
-        // ---- refill idle lanes, decide what needs no axis at all ----
-        bool hit = false, queue = false;
-        uint4 rec = make_uint4(0, 0, 0, 0);
-        uint32_t mask = 0;
-        // a refill costs the warp three dependent loads (candidate, faces,
-        // vertices): refill only once kRefillBatch lanes are idle (or none is busy)
-        const uint32_t idle = __ballot_sync(0xffffffffu, !busy);
-        const bool refill = __popc(idle) >= kRefillBatch || idle == 0xffffffffu;
-        const uint32_t take = refill ? min((uint32_t)__popc(idle), hi - next) : 0u;
-        const uint32_t rank = __popc(idle & ((1u << lane) - 1u));
-        if (!busy && rank < take) {
-            c = a.cand[next + rank];
-            V3 P1, P2, P3, Q1, Q2, Q3;
-            load_tris(a, c, P1, P2, P3, Q1, Q2, Q3, rec);
-            const V3 p2v = vsub(P2, P1), p3v = vsub(P3, P1);
-            const V3 q1v = vsub(Q1, P1), q2v = vsub(Q2, P1), q3v = vsub(Q3, P1);
-            float A = fmaxf(fmaxf(fmaxf(fabsf(p2v.x), fabsf(p2v.y)), fmaxf(fabsf(p2v.z), fabsf(p3v.x))),
-                            fmaxf(fmaxf(fabsf(p3v.y), fabsf(p3v.z)), fmaxf(fabsf(q1v.x), fabsf(q1v.y))));
-            A = fmaxf(A, fmaxf(fmaxf(fabsf(q1v.z), fabsf(q2v.x)), fmaxf(fabsf(q2v.y), fabsf(q2v.z))));
-            A = fmaxf(A, fmaxf(fmaxf(fabsf(q3v.x), fabsf(q3v.y)), fabsf(q3v.z)));
-            if (!(A >= 0x1p-20f && A <= 0x1p20f)) {
-                // the bounds could under- or overflow: every axis in FP64
-                queue = true;
-                mask = ((1u << 17) - 1u) | (tri_intersect_exact(P1, P2, P3, Q1, Q2, Q3) ? 0x80000000u : 0u);
-            } else if (veq(P1, Q1) || veq(P1, Q2) || veq(P1, Q3) || veq(P2, Q1) || veq(P2, Q2) || veq(P2, Q3) ||
-                       veq(P3, Q1) || veq(P3, Q2) || veq(P3, Q3)) {
-                hit = true;  // a shared vertex: never separated
-            } else {
-                const EV3 zero{V3{0.0f, 0.0f, 0.0f}, V3{0.0f, 0.0f, 0.0f}};
-                t.p2 = p2v;
-                t.p3 = p3v;
-                t.q1 = q1v;
-                t.q2 = q2v;
-                t.q3 = q3v;
-                t.n1 = ecross(esub(ev_rel(p2v), zero), esub(ev_rel(p3v), ev_rel(p2v)));
-                t.m1 = ecross(esub(ev_rel(q2v), ev_rel(q1v)), esub(ev_rel(q3v), ev_rel(q2v)));
-                busy = true;
-                step = 0;
-                undecided = 0;
-                sep32 = false;
-            }
-        }
-        next += take;
-        // ---- one axis per busy lane ----
-        if (busy) {
-            const uint32_t k = c_axis_order[step];
-            const EV3 zero{V3{0.0f, 0.0f, 0.0f}, V3{0.0f, 0.0f, 0.0f}};
-            bool s32;
-            const uint32_t r = project6_bounded(axis_of(k, t), zero, ev_rel(t.p2), ev_rel(t.p3), ev_rel(t.q1),
-                                                ev_rel(t.q2), ev_rel(t.q3), s32);
-            if (r == 0u) {
-                busy = false;  // separates in every arithmetic: no hit
-            } else {
-                sep32 |= s32;
-                if (r == 2u) undecided |= 1u << k;
-                if (++step == 17) {
-                    busy = false;
-                    if (undecided == 0) {
-                        hit = true;
-                        const PairView& pv = a.pairs[bvtt_pair(c)];
-                        rec = make_uint4(pv.a, pv.b, __ldg(pv.ta.face + bvtt_a(c)).w, __ldg(pv.tb.face + bvtt_b(c)).w);
-                    } else {
-                        queue = true;
-                        mask = undecided | (sep32 ? 0u : 0x80000000u);
-                    }
-                }
-            }
-        }
-        // ---- results: hits out, undecided candidates to the FP64 queue ----
-        append_hit(a, hit, rec, lane);
-        const uint32_t qmask = __ballot_sync(0xffffffffu, queue);
-        if (queue) {
-            const uint32_t slot = qn + __popc(qmask & ((1u << lane) - 1u));
-            qc[slot] = c;
-            qm[slot] = mask;
-        }
-        qn += __popc(qmask);
-        __syncwarp();
-        if (qn >= 32) {
-            settle_fp64(a, qc + qn - 32, qm + qn - 32, 32, lane);
-            qn -= 32;
-            __syncwarp();
-        }
-        if (!__any_sync(0xffffffffu, busy) && next >= hi) break;
-    }
-    if (qn > 0) settle_fp64(a, qc, qm, qn, lane);
-}
-
 // ---------------------------------------------------------------------------
-// Precision narrow phase in three passes, grouping candidates by how much of
-// the filtered test they need, so that the lanes of a warp run the same code:
+// Precision narrow phase in passes, grouping candidates by how much of the
+// filtered test they need, so that the lanes of a warp run the same code:
 //  1. k_prec_classify, one candidate per thread: the plain float SAT (the
 //     reference's arithmetic), which also names the first separating axis. A
 //     float-separated candidate needs only that axis bounded: a margin above
 //     its error bound separates in every arithmetic (no hit, float and FP64
 //     agree); otherwise it goes to the recheck list. Shared vertices are hits
-//     at once; a float hit goes to the float-hit list, whose members need all
-//     17 bounded axes (no axis can separate in every arithmetic there).
+//     at once, and so is a float hit whose every axis overlaps beyond a
+//     static bound on the float and FP64 errors; other float hits go to the
+//     float-hit list, whose members need all 17 bounded axes.
 //  2. k_prec_settle over the float-hit list then the recheck list, one per
 //     lane: pass 1 of the filtered test (all 17 axes bounded, straight-line
-//     for float hits: no lane leaves early), undecided ones settled in FP64 32
-//     at a time from a per-warp queue.
-// The pair set is the all-FP64 one by construction, as in k_narrow_prec.
+//     for float hits: no lane leaves early); what it leaves undecided goes to
+//     the FP64 list with the mask of its undecided axes.
+//  3. k_prec_fp64_setup forms each FP64 list entry's FP64 vertices and
+//     normals with every lane busy; k_prec_fp64 then evaluates the undecided
+//     axes in FP64, one axis per lane per iteration, lanes refilled from the
+//     list as their candidates are decided.
+// The pair set is the all-FP64 one by construction.
 // ---------------------------------------------------------------------------
 
 // project6 of the float test, which also clears `robust` unless both of the
@@ -1382,12 +1197,8 @@ __global__ void __launch_bounds__(kDetectThreads) k_prec_fp64(DetectArgs a)
     }
 }
 
-#ifndef OIBVH_PREC_PASSES
-#define OIBVH_PREC_PASSES 1
-#endif
-
 // The traversal kernels' fused narrow phase is the float test only; precision
-// mode runs the broad phase alone and then k_narrow_prec.
+// mode runs the broad phase alone and then its narrow-phase passes.
 static inline bool fused_precision(const DetectArgs& a) { return a.precision && a.fuse_narrow; }
 
 cudaError_t launch_init_front(const DetectArgs& a, uint32_t total0, cudaStream_t s)
@@ -1480,7 +1291,8 @@ int walk_blocks_per_sm(uint32_t walk_cap, bool fused)
 
 cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s)
 {
-    if (a.precision && OIBVH_PREC_PASSES && a.prec_lists) {
+    if (a.precision) {
+        if (a.prec_lists == nullptr || (a.fp64_tri_cap && a.fp64_tri == nullptr)) return cudaErrorInvalidValue;
         note_launches(a.fp64_tri_cap ? 4 : 3);
         k_prec_classify<<<a.grid, kDetectThreads, 0, s>>>(a);
         k_prec_settle<<<a.grid, kDetectThreads, 0, s>>>(a);
@@ -1489,8 +1301,7 @@ cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s)
         return cudaGetLastError();
     }
     note_launches(1);
-    if (a.precision) k_narrow_prec<<<a.grid, kDetectThreads, 0, s>>>(a);
-    else k_narrow<<<a.grid, kDetectThreads, 0, s>>>(a);
+    k_narrow<<<a.grid, kDetectThreads, 0, s>>>(a);
     return cudaGetLastError();
 }
 
