@@ -240,13 +240,17 @@ typedef struct oibvh_tuning {
     uint32_t descend_ratio;       /* a node pair's two sides descend together while their boxes' squared
                                      diagonals are within this factor, else only the larger (1..2^30, 16;
                                      2^30: always together; 0 = keep) */
+    uint32_t claim_min;           /* walkers claim work-list items dynamically (up to 32 at a time) when a
+                                     list holds at least this many items per warp, else each takes a
+                                     static interleaved share (1..2^20, 1; 0 = keep) */
 } oibvh_tuning;
 int oibvh_scene_set_tuning(oibvh_scene_t s, const oibvh_tuning* t);
 int oibvh_scene_get_tuning(oibvh_scene_t s, oibvh_tuning* t);
 /* Project-written autotuner: times `reps` scene refits per refit level-group
  * depth, then `reps` detects of the scene's current state per setting, by
  * coordinate descent (start size x handoff, then the walkers' per-warp queue
- * capacity, then the descend ratio, then walker CTAs per SM), keeps the fastest, and sizes the queues
+ * capacity, then the descend ratio, then the claim threshold, then walker
+ * CTAs per SM), keeps the fastest, and sizes the queues
  * from the observed peaks with 2x headroom. Blocking; *chosen may be NULL. */
 int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t reps, oibvh_tuning* chosen);
 

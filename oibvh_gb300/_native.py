@@ -90,6 +90,7 @@ class Tuning(ctypes.Structure):
         ("walk_front", ctypes.c_uint32),
         ("refit_group_log2", ctypes.c_uint32),
         ("descend_ratio", ctypes.c_uint32),
+        ("claim_min", ctypes.c_uint32),
     ]
 
 

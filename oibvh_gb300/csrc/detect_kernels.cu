@@ -9,7 +9,7 @@
 // The broad phase is three kernels: k_init_front tests the cross product of
 // the node pairs at a start level and lists the overlapping ones; k_top (one
 // CTA) walks the narrow top levels until the front is wide; in k_walk every
-// warp takes an interleaved share of that front and walks it to the leaves
+// warp claims 32 items of that front at a time and walks them to the leaves
 // through a private FIFO ring in shared memory (its capacity a tuning
 // parameter); what outgrows it spills to the next round's list, so no grid-wide
 // synchronisation is needed. The host enqueues the rounds and reads the
@@ -690,17 +690,20 @@ __global__ void __launch_bounds__(kTopThreads) k_top(DetectArgs a)
     if (wc.n > 0) flush_candidates<kFused>(a, wc.buf, wc.n, lane);
 }
 
-// The wide bottom of the traversal, round `round` (>= 1): every warp takes
-// the work-list items w, w+W, w+2W, ... (W = warps in the grid; the
-// interleave spreads each region of the intersection over many warps) and
-// walks them to the leaves through a private FIFO ring of node pairs in
-// shared memory: each step pops up to 32 pairs (one per lane), expands them
-// and appends the overlapping children at the tail, with no barrier between
-// tree levels, so lanes stay busy as long as a warp's worth of pairs is
-// queued (a level-by-level front leaves the last chunk of every level part
-// empty). The ring is topped up from the warp's share of the list whenever
-// it holds fewer than 32 pairs. Warps never wait for each other; children
-// that do not fit in the ring spill to the next round's list.
+// The wide bottom of the traversal, round `round` (>= 1): every warp claims
+// up to 32 consecutive work-list items at a time (one atomic on the round's
+// claim counter; a list with fewer than claim_min items per warp, a tuning
+// parameter, is dealt out statically instead, one interleaved share per
+// warp) and walks them to the leaves through a private FIFO ring of node
+// pairs in shared memory: each step pops up to 32 pairs (one per lane),
+// expands them and appends the overlapping children at the tail, with no
+// barrier between tree levels, so lanes stay busy as long as a warp's worth
+// of pairs is queued (a level-by-level front leaves the last chunk of every
+// level part empty). The ring is topped up with the next claim whenever it
+// holds fewer than 32 pairs, so warps whose items expand less take more of
+// the list. Warps never wait for each other; children that do not fit in the
+// ring spill to the next round's list (consecutively per warp, so a claim of
+// consecutive items keeps one subtree's spill together).
 // kDense: compiled for 4 CTAs per SM (64 registers; the fused form spills a
 // few bytes), used when the grid asks for 4; otherwise the register budget of
 // 3 CTAs per SM (no spills).
@@ -715,13 +718,20 @@ __global__ void __launch_bounds__(kDetectThreads, kDense ? 4 : 3) k_walk(DetectA
     uint64_t* __restrict__ spill = (round & 1) ? a.work[0] : a.work[1];
     uint32_t* spill_cnt = a.counts + kCountWork0 + round + 1;
     const uint32_t n_src = min(*(volatile uint32_t*)(a.counts + kCountWork0 + round), a.work_cap);
-    const uint32_t W = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t* claim = a.counts + kCountClaim0 + round;
     const uint32_t R = walk_ring(a.walk_cap);  // ring entries (>= 64)
     uint64_t* ring = s_front + (size_t)wib * R;
-    // items of this warp's share: w + j * W for j < n_mine
-    const uint32_t n_mine = n_src > w ? (n_src - w + W - 1) / W : 0u;
+    // A list of at least claim_min items per warp is claimed `chunk`
+    // consecutive items at a time (its items per warp, 1..32); a shorter one
+    // is dealt out statically, items w, w + W, w + 2W, ... to warp w (W warps),
+    // so that every warp gets work.
+    const uint32_t W = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const bool claiming = n_src >= max(1u, a.claim_min) * W;
+    const uint32_t chunk = min(32u, max(1u, n_src / W));
+    const uint32_t n_mine = claiming ? 0u : (n_src > w ? (n_src - w + W - 1) / W : 0u);
     uint32_t next_item = 0;
+    bool drained = !claiming;     // warp-uniform: no unclaimed item left (claiming lists)
     uint32_t head = 0, live = 0;  // warp-uniform: ring[head .. head + live) mod R is queued
     uint32_t tested = 0;
     auto slot = [&](uint32_t off) {  // ring index of the entry `off` after head (off < R)
@@ -729,7 +739,19 @@ __global__ void __launch_bounds__(kDetectThreads, kDense ? 4 : 3) k_walk(DetectA
         return i >= R ? i - R : i;
     };
     for (;;) {
-        if (live < 32 && next_item < n_mine) {
+        if (live < 32 && !drained) {
+            // the next `chunk` items of the list, claimed with one atomic per
+            // warp: warps whose items expand less come back sooner and take
+            // more, and neighbouring items (often one subtree's spill) stay together
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(claim, chunk);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            const uint32_t take = base < n_src ? min(chunk, n_src - base) : 0u;  // live + take <= 63 < R
+            drained = base + chunk >= n_src;
+            if (lane < take) ring[slot(live + lane)] = __ldcg(src + base + lane);
+            live += take;
+            __syncwarp();
+        } else if (live < 32 && next_item < n_mine) {
             const uint32_t take = min(32u, n_mine - next_item);  // live + take <= 63 < R
             if (lane < take) ring[slot(live + lane)] = __ldcg(src + w + (size_t)(next_item + lane) * W);
             next_item += take;

@@ -205,6 +205,7 @@ struct oibvh_scene_s {
     uint32_t tune_walk_cap = 128;   // per-warp front entries of the walkers
     uint32_t tune_refit_log = 10;   // refit level-group depth (levels per CTA: 9, 10 or 11)
     uint32_t tune_descend = 16;     // both sides descend while the boxes' squared diagonals are within it
+    uint32_t tune_claim = 1;        // walkers claim list items dynamically from this many per warp
 
     // captured frame (CUDA graph): [transform] + refit + detect
     cudaGraphExec_t frame_exec = nullptr;
@@ -431,6 +432,7 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
             a.walk_cap = s->tune_walk_cap;
             a.precision = s->precision;
             a.descend_ratio = (float)s->tune_descend;
+            a.claim_min = s->tune_claim;
             CUDA_TRY(launch_init_front(a, (uint32_t)plan.front0, st));
             CUDA_TRY(launch_top(a, st));
             uint32_t rounds = 1;  // list 1 is the first walk round's input
@@ -1212,6 +1214,8 @@ API int oibvh_scene_set_tuning(oibvh_scene_t s, const oibvh_tuning* t)
     if (t->refit_group_log2) s->tune_refit_log = t->refit_group_log2;
     if (t->descend_ratio > (1u << 30)) return fail(OIBVH_ERR_ARG, "descend_ratio: 1..2^30 (0 keeps the value)");
     if (t->descend_ratio) s->tune_descend = t->descend_ratio;
+    if (t->claim_min > (1u << 20)) return fail(OIBVH_ERR_ARG, "claim_min: 1..2^20 (0 keeps the value)");
+    if (t->claim_min) s->tune_claim = t->claim_min;
     s->tune_start_log2 = t->start_pairs_log2;
     s->tune_handoff = t->handoff;
     s->tune_walk_per_sm = t->walk_blocks_per_sm;
@@ -1230,6 +1234,7 @@ API int oibvh_scene_get_tuning(oibvh_scene_t s, oibvh_tuning* t)
     t->walk_front = s->tune_walk_cap;
     t->refit_group_log2 = s->tune_refit_log;
     t->descend_ratio = s->tune_descend;
+    t->claim_min = s->tune_claim;
     t->front_capacity = s->front_cap;
     t->hit_capacity = s->hit_cap;
     return OIBVH_OK;
@@ -1290,10 +1295,11 @@ API int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t rep
     }
     float best = 1e30f;
     uint32_t b_start = s->tune_start_log2, b_handoff = s->tune_handoff, b_cap = 128, b_per = 0;
-    uint32_t b_desc = 16;
+    uint32_t b_desc = 16, b_claim = 1;
     s->tune_walk_cap = 128;
     s->tune_walk_per_sm = 0;
     s->tune_descend = 16;
+    s->tune_claim = 1;
     for (uint32_t sl : {12u, 14u, 16u, 18u, 20u})
         for (uint32_t h : {512u, 2048u, 8192u}) {
             s->tune_start_log2 = sl;
@@ -1320,6 +1326,14 @@ API int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t rep
         if (ms < best) best = ms, b_desc = r;
     }
     s->tune_descend = b_desc;
+    for (uint32_t c : {4u, 32u}) {
+        if (st != OIBVH_OK) break;
+        s->tune_claim = c;
+        float ms;
+        if (!time_setting(ms)) break;
+        if (ms < best) best = ms, b_claim = c;
+    }
+    s->tune_claim = b_claim;
     const int fit = walk_blocks_per_sm(b_cap);
     for (int per = 1; per < fit && st == OIBVH_OK; ++per) {
         s->tune_walk_per_sm = (uint32_t)per;
@@ -1341,8 +1355,9 @@ API int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t rep
             s->tune_walk_cap = 128;
             s->tune_walk_per_sm = 0;
             s->tune_descend = 16;
+            s->tune_claim = 1;
             if (time_setting(ms_default) && ms_default < ms_chosen) {
-                b_start = 16, b_handoff = 2048, b_cap = 128, b_per = 0, b_desc = 16;
+                b_start = 16, b_handoff = 2048, b_cap = 128, b_per = 0, b_desc = 16, b_claim = 1;
             }
         }
         reps = reps0;
@@ -1351,6 +1366,7 @@ API int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t rep
         s->tune_walk_cap = b_cap;
         s->tune_walk_per_sm = b_per;
         s->tune_descend = b_desc;
+        s->tune_claim = b_claim;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1362,6 +1378,7 @@ API int oibvh_scene_autotune(oibvh_scene_t s, uint32_t entry_level, uint32_t rep
     bt.walk_front = b_cap;
     bt.refit_group_log2 = b_group;
     bt.descend_ratio = b_desc;
+    bt.claim_min = b_claim;
     // capacities: the largest work list and hit count seen, doubled
     st = detect_impl(s, s->device, entry_level, 1, full_detect_mode(s), 0);
     if (st != OIBVH_OK) return st;
@@ -1507,6 +1524,7 @@ int capture_frame_impl(oibvh_scene_s* s, cudaStream_t st)
     a.walk_cap = s->tune_walk_cap;
     a.precision = s->precision;
     a.descend_ratio = (float)s->tune_descend;
+    a.claim_min = s->tune_claim;
 
     s->frame_args = a;
     s->frame_front0 = (uint32_t)plan.front0;

@@ -120,6 +120,7 @@ struct DetectArgs {
     uint32_t precision;    // 0: float triangle test (reference arithmetic); 1: FP64-filtered
     uint32_t walk_cap;     // per-warp front entries of the walkers (multiple of 32, <= 512; 0: 128)
     float descend_ratio = kDescendRatio;  // both sides descend while the boxes' squared diagonals are within it
+    uint32_t claim_min = 1;  // walkers claim list items dynamically from this many items per warp
 };
 cudaError_t launch_init_front(const DetectArgs& a, uint32_t total0, cudaStream_t s);
 cudaError_t launch_top(const DetectArgs& a, cudaStream_t s);
@@ -138,11 +139,13 @@ constexpr uint32_t kFp64TriRows = 23;
 // the sizes of the float-hit, recheck and FP64 lists of the precision narrow phase,
 // then the work-list size of each traversal round (list
 // 0: the overlapping start pairs; list 1: the front k_top hands over; list
-// r+1: what walk round r spilled).
+// r+1: what walk round r spilled), then how many items of each list the
+// walkers have claimed.
 constexpr uint32_t kMaxRounds = 16;
 constexpr uint32_t kCountHits = 0, kCountFlags = 1, kCountCands = 2, kCountCandSlots = 3, kCountTested = 4,
                    kCountFp64Axes = 5, kCountFp64Cands = 6, kCountDisagree = 7, kCountPrecHits = 8,
                    kCountPrecRecheck = 9, kCountPrecFp64 = 10, kCountWork0 = 11,
-                   kCountTotal = kCountWork0 + kMaxRounds + 1;
+                   kCountClaim0 = kCountWork0 + kMaxRounds + 1,  // items of list r claimed so far
+                   kCountTotal = kCountClaim0 + kMaxRounds + 1;
 
 } // namespace oibvh

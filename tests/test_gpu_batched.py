@@ -177,6 +177,34 @@ def test_descend_ratios_keep_the_pair_set(gpu):
         sc.set_tuning(descend_ratio=(1 << 30) + 1)
 
 
+def test_claim_thresholds_keep_the_pair_set(gpu):
+    """Walkers that claim work-list items dynamically (from 1 item per warp on)
+    or take static interleaved shares (a threshold above any list) find the
+    oracle's pair set and candidate count, in direct detects and in frames."""
+    import torch
+
+    from oibvh_gb300 import DeviceType, OibvhError
+
+    w = _workload(12, seed=23, subdivs=(2, 4, 5))
+    sc, trees = _scene_from(w)
+    rest = torch.from_numpy(w.packed_rest_xyzw()).cuda()
+    mats = torch.from_numpy(w.matrices(2)).cuda()
+    want, wc = _oracle(w.positions(2), [m.tri for m in w.rest], w.pairs)
+    for c in (1, 4, 32, 1 << 20):
+        for start in (12, 20):
+            sc.set_tuning(claim_min=c, start_pairs_log2=start, handoff=512)
+            assert sc.tuning()["claim_min"] == c
+            sc.capture_frame(4, 3, True, rest.data_ptr(), mats.data_ptr())
+            sc.launch_frame()
+            sc.finish_frame()
+            assert np.array_equal(sc.int_tri_pairs(), want), (c, start)
+            assert sc.candidate_count() == wc
+            sc.detectCollision(DeviceType.GPU0, 0, 1)
+            assert np.array_equal(sc.int_tri_pairs(), want), (c, start)
+    with pytest.raises(OibvhError):
+        sc.set_tuning(claim_min=(1 << 20) + 1)
+
+
 def test_refit_level_group_depths_agree(gpu):
     """The scene refit with level groups of 9, 10 and 11 levels per CTA (two
     climbing stages for the deep tree) writes the oracle's boxes bit for bit."""
