@@ -52,8 +52,8 @@ REFIT_DRAM_BYTES_PER_TRIANGLE = (372.71e6 + 452.25e6) / 15520000
 TRANSFORM_DRAM_BYTES_PER_VERTEX = (124.32e6 + 73.98e6) / 7760256
 # DRAM bytes (read + written) of the traversal kernels (k_init_front, k_top and
 # the k_walk rounds) of one frame per BVTT node pair tested, measured with ncu
-# on 64 batched pairs (163.2 MB per frame, 15,595,232 pairs tested)
-TRAVERSAL_DRAM_BYTES_PER_TESTED = (161.72e6 + 0.89e6 + 0.30e6 + 0.30e6) / 15595232
+# on 64 batched pairs (206.9 MB per frame, 15,594,052 pairs tested)
+TRAVERSAL_DRAM_BYTES_PER_TESTED = (204.71e6 + 1.54e6 + 0.30e6 + 0.30e6) / 15594052
 
 
 def parse():
