@@ -1105,10 +1105,13 @@ __device__ __forceinline__ bool axis_overlaps_fp64_uniform(uint32_t k, const FP6
     return !(mn1 > mx2) && !(mn2 > mx1);
 }
 
+// Idle lanes that trigger a refill: with the setups formed ahead a refill is
+// loads only, so the lanes are refilled early (4 measured best of 4 / 8 / 12
+// / 16 on the sheets; 16 was best while the refills formed the setups).
 #ifndef OIBVH_FP64_REFILL
-#define OIBVH_FP64_REFILL 16
+#define OIBVH_FP64_REFILL 4
 #endif
-constexpr uint32_t kFp64Refill = OIBVH_FP64_REFILL;  // idle lanes that trigger a refill
+constexpr uint32_t kFp64Refill = OIBVH_FP64_REFILL;
 
 // FP64 setups (fp64_tri and the hit record) of the FP64 list's first
 // fp64_tri_cap entries, one entry per lane: formed here with every lane of a
@@ -1157,8 +1160,9 @@ __global__ void __launch_bounds__(kDetectThreads) k_prec_fp64_setup(DetectArgs a
 // evaluates ONE of its undecided axes (in order) per iteration, so the FP64
 // pipe sees full warps however many axes each candidate needs; a lane whose
 // candidate is decided (an axis separates: no hit; none left: hit) takes the
-// next one from the warp's range, 16 lanes at a time (a refill costs the
-// chain candidate -> faces -> vertices).
+// next one from the warp's range, once kFp64Refill lanes are idle (a refill
+// costs the setup's loads, or, past the setup buffer, the chain candidate ->
+// faces -> vertices and the setup's FP64 work).
 __global__ void __launch_bounds__(kDetectThreads) k_prec_fp64(DetectArgs a)
 {
     const uint32_t n = min(a.counts[kCountPrecFp64], a.cand_cap);
