@@ -1113,6 +1113,231 @@ __device__ __forceinline__ bool axis_overlaps_fp64_uniform(uint32_t k, const FP6
 #endif
 constexpr uint32_t kFp64Refill = OIBVH_FP64_REFILL;
 
+// ---------------------------------------------------------------------------
+// Double-float pass: the FP64 list's undecided axes evaluated with pairs of
+// floats on the FP32 pipe (the FP64 pipe of this part runs at 1/64 of its
+// rate), with a bound W on |double-float value - exact| + |FP64 value -
+// exact| for every quantity. The FP64 value of each projection then lies
+// within W of the double-float one, so the FP64 comparisons of an axis are
+// known whenever the intervals [v - W, v + W] of the two triangles' sets do
+// not straddle: the axis separates in FP64, or overlaps in FP64, exactly as
+// the FP64 pass would find. What stays undecided (nearly or exactly coplanar
+// triangles, whose FP64 projections are rounding noise) goes on to FP64.
+//
+// Arithmetic (Joldes, Muller, Popescu, "Tight and rigorous error bounds for
+// basic building blocks of double-word arithmetic", ACM TOMS 2017): exact
+// TwoSum and Fast2Sum, the FMA-based exact product, AccurateDWPlusDW
+// (relative error <= 3u^2/(1-4u)) and DWTimesDW3 (<= 4u^2), u = 2^-24. The
+// relative coordinates are exact (TwoSum of two floats); the FP64 formula
+// rounds them once (2^-53). Each operation then adds at most U|c| to W with
+// U = 2^-44 (> 5u^2 + 2^-53, double-float and FP64 rounding together), and
+// a product the propagated |a| W_b + |b| W_a + W_a W_b; 2^-140 per step covers
+// underflowing low parts. The decision doubles W.
+// ---------------------------------------------------------------------------
+struct DF {
+    float h, l;
+};
+struct DFB {  // a double-float value and its bound
+    DF v;
+    float w;
+};
+constexpr float kDfU = 0x1p-44f, kDfEta = 0x1p-140f;
+__device__ __forceinline__ DF two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float ap = __fsub_rn(s, b), bp = __fsub_rn(s, ap);
+    return DF{s, __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp))};
+}
+__device__ __forceinline__ DF fast_two_sum(float a, float b)  // |a| >= |b| (or a's exponent at least b's)
+{
+    const float s = __fadd_rn(a, b);
+    return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF df_add(const DF& x, const DF& y)  // AccurateDWPlusDW
+{
+    const DF s = two_sum(x.h, y.h), t = two_sum(x.l, y.l);
+    const DF v = fast_two_sum(s.h, __fadd_rn(s.l, t.h));
+    return fast_two_sum(v.h, __fadd_rn(t.l, v.l));
+}
+__device__ __forceinline__ DF df_neg(const DF& x) { return DF{-x.h, -x.l}; }
+__device__ __forceinline__ DF df_mul(const DF& x, const DF& y)  // DWTimesDW3
+{
+    const float ch = __fmul_rn(x.h, y.h), cl1 = __fmaf_rn(x.h, y.h, -ch);
+    const float tl1 = __fmaf_rn(x.h, y.l, __fmul_rn(x.l, y.l));
+    const float cl2 = __fmaf_rn(x.l, y.h, tl1);
+    return fast_two_sum(ch, __fadd_rn(cl1, cl2));
+}
+__device__ __forceinline__ float df_abs(const DF& x) { return __fadd_ru(fabsf(x.h), fabsf(x.l)); }
+// The propagated part is scaled by 1 + 2^-20, which covers the FP64
+// rounding of the propagated error itself (2^-53 of it, second order).
+constexpr float kDfGrow = 1.0f + 0x1p-20f;
+__device__ __forceinline__ float dfb_w_sum(const DFB& a, const DFB& b, const DF& c)
+{
+    return __fadd_ru(__fmaf_ru(kDfU, df_abs(c), __fmul_ru(kDfGrow, __fadd_ru(a.w, b.w))), kDfEta);
+}
+__device__ __forceinline__ DFB dfb_sub(const DFB& a, const DFB& b)
+{
+    const DF c = df_add(a.v, df_neg(b.v));
+    return DFB{c, dfb_w_sum(a, b, c)};
+}
+__device__ __forceinline__ DFB dfb_add(const DFB& a, const DFB& b)
+{
+    const DF c = df_add(a.v, b.v);
+    return DFB{c, dfb_w_sum(a, b, c)};
+}
+// |ab - exact| + |FP64 ab - exact| <= |a| W_b + |b| W_a + 2 W_a W_b, plus the
+// two roundings of the product
+__device__ __forceinline__ DFB dfb_mul(const DFB& a, const DFB& b)
+{
+    const DF c = df_mul(a.v, b.v);
+    float w = __fmaf_ru(df_abs(a.v), b.w, __fmul_ru(df_abs(b.v), a.w));
+    w = __fmaf_ru(__fmul_ru(2.0f, a.w), b.w, w);
+    w = __fadd_ru(__fmaf_ru(kDfU, df_abs(c), __fmul_ru(kDfGrow, w)), kDfEta);
+    return DFB{c, w};
+}
+struct DFB3 {
+    DFB x, y, z;
+};
+__device__ __forceinline__ DFB3 dfb3_sub(const DFB3& a, const DFB3& b)
+{
+    return DFB3{dfb_sub(a.x, b.x), dfb_sub(a.y, b.y), dfb_sub(a.z, b.z)};
+}
+// the FP64 formula's cross product: (x.y*y.z - y.y*x.z, x.z*y.x - y.z*x.x, x.x*y.y - y.x*x.y)
+__device__ __forceinline__ DFB3 dfb3_cross(const DFB3& x, const DFB3& y)
+{
+    return DFB3{dfb_sub(dfb_mul(x.y, y.z), dfb_mul(y.y, x.z)), dfb_sub(dfb_mul(x.z, y.x), dfb_mul(y.z, x.x)),
+                dfb_sub(dfb_mul(x.x, y.y), dfb_mul(y.x, x.y))};
+}
+// (a.x*b.x + a.y*b.y) + a.z*b.z
+__device__ __forceinline__ DFB dfb3_dot(const DFB3& a, const DFB3& b)
+{
+    return dfb_add(dfb_add(dfb_mul(a.x, b.x), dfb_mul(a.y, b.y)), dfb_mul(a.z, b.z));
+}
+// A relative coordinate P - P1: exact as a double-float; FP64 rounds it once.
+__device__ __forceinline__ DFB dfb_rel(float a, float b)
+{
+    const DF d = two_sum(a, -b);
+    return DFB{d, __fmul_ru(0x1p-53f, df_abs(d))};
+}
+__device__ __forceinline__ DFB3 dfb3_rel(const V3& p, const V3& o)
+{
+    return DFB3{dfb_rel(p.x, o.x), dfb_rel(p.y, o.y), dfb_rel(p.z, o.z)};
+}
+struct DFTri {
+    DFB3 p2, p3, q1, q2, q3, n1, m1;
+};
+// Axis k (0: n1, 1: m1, 2 + 3i + j: e_i x f_j, 11 + i: e_i x n1, 14 + j: f_j x
+// m1) with the edges formed as the FP64 formula forms them (e1 = p2 - 0 = p2,
+// e3 = 0 - p3 = -p3 exactly, the others one subtraction).
+__device__ __forceinline__ DFB3 dfb_axis(uint32_t k, const DFTri& t)
+{
+    if (k == 0) return t.n1;
+    if (k == 1) return t.m1;
+    auto e = [&](uint32_t i) {
+        if (i == 0) return t.p2;
+        if (i == 1) return dfb3_sub(t.p3, t.p2);
+        return DFB3{DFB{df_neg(t.p3.x.v), t.p3.x.w}, DFB{df_neg(t.p3.y.v), t.p3.y.w}, DFB{df_neg(t.p3.z.v), t.p3.z.w}};
+    };
+    auto f = [&](uint32_t j) {
+        if (j == 0) return dfb3_sub(t.q2, t.q1);
+        if (j == 1) return dfb3_sub(t.q3, t.q2);
+        return dfb3_sub(t.q1, t.q3);
+    };
+    if (k < 11) return dfb3_cross(e((k - 2) / 3), f((k - 2) % 3));
+    if (k < 14) return dfb3_cross(e(k - 11), t.n1);
+    return dfb3_cross(f(k - 14), t.m1);
+}
+// Axis k of FP64 known from double-floats: 0 = separates, 1 = overlaps, 2 = undecided.
+__device__ __forceinline__ uint32_t dfb_axis_fp64(uint32_t k, const DFTri& t)
+{
+    const DFB3 ax = dfb_axis(k, t);
+    const DFB P[3] = {DFB{DF{0.0f, 0.0f}, 0.0f}, dfb3_dot(ax, t.p2), dfb3_dot(ax, t.p3)};
+    const DFB Q[3] = {dfb3_dot(ax, t.q1), dfb3_dot(ax, t.q2), dfb3_dot(ax, t.q3)};
+    // intervals that hold the FP64 values: value as hi + lo (the sum's rounding
+    // is inside the doubled bound)
+    float pl = 3.4e38f, ph = -3.4e38f, ql = 3.4e38f, qh = -3.4e38f;  // min of lows, max of highs, ...
+    float plh = -3.4e38f, phl = 3.4e38f, qlh = -3.4e38f, qhl = 3.4e38f;  // max of lows, min of highs
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float v = __fadd_rn(P[i].v.h, P[i].v.l), w = __fmul_ru(2.0f, __fadd_ru(P[i].w, __fmul_ru(0x1p-23f, fabsf(v))));
+        const float lo = __fsub_rd(v, w), hi = __fadd_ru(v, w);
+        pl = fminf(pl, lo); ph = fmaxf(ph, hi); plh = fmaxf(plh, lo); phl = fminf(phl, hi);
+        const float u = __fadd_rn(Q[i].v.h, Q[i].v.l), x = __fmul_ru(2.0f, __fadd_ru(Q[i].w, __fmul_ru(0x1p-23f, fabsf(u))));
+        const float ulo = __fsub_rd(u, x), uhi = __fadd_ru(u, x);
+        ql = fminf(ql, ulo); qh = fmaxf(qh, uhi); qlh = fmaxf(qlh, ulo); qhl = fminf(qhl, uhi);
+    }
+    // FP64 mn1 lies in [pl, phl], mx1 in [plh, ph], mn2 in [ql, qhl], mx2 in [qlh, qh]
+    if (pl > qh || ql > ph) return 0u;             // mn1 > mx2 or mn2 > mx1 for sure
+    if (phl < qlh && qhl < plh) return 1u;         // mn1 < mx2 and mn2 < mx1 for sure
+    return 2u;
+}
+
+// The FP64 list through the double-float pass, one candidate per lane: its
+// undecided axes in order until one separates for sure; the axes still open
+// (and the float answer) go to the list the FP64 passes take.
+__global__ void __launch_bounds__(kDetectThreads) k_prec_df(DetectArgs a)
+{
+    const uint32_t n = min(a.counts[kCountPrecFp64], a.cand_cap);
+    const uint2* list = (const uint2*)(a.prec_lists + 2 * (size_t)a.cand_cap);
+    uint2* left = (uint2*)a.prec_lists;  // the float-hit and recheck lists' room, free after the bounded pass
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t dis = 0;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t j = base + threadIdx.x;
+        bool hit = false, keep = false;
+        uint4 rec = make_uint4(0, 0, 0, 0);
+        uint2 item = make_uint2(0, 0);
+        if (j < n) {
+            item = list[j];
+            V3 P1, P2, P3, Q1, Q2, Q3;
+            load_tris(a, a.cand[item.x], P1, P2, P3, Q1, Q2, Q3, rec);
+            uint32_t mask = item.y & 0x1ffffu, open = 0;
+            bool separated = false;
+            const float A = fmaxf(fmaxf(fmaxf(fabsf(__fsub_rn(P2.x, P1.x)), fabsf(__fsub_rn(P2.y, P1.y))),
+                                        fmaxf(fabsf(__fsub_rn(P2.z, P1.z)), fabsf(__fsub_rn(P3.x, P1.x)))),
+                                  fmaxf(fmaxf(fabsf(__fsub_rn(P3.y, P1.y)), fabsf(__fsub_rn(P3.z, P1.z))),
+                                        fmaxf(fabsf(__fsub_rn(Q1.x, P1.x)), fabsf(__fsub_rn(Q1.y, P1.y)))));
+            const float A2 = fmaxf(fmaxf(fmaxf(fabsf(__fsub_rn(Q1.z, P1.z)), fabsf(__fsub_rn(Q2.x, P1.x))),
+                                         fmaxf(fabsf(__fsub_rn(Q2.y, P1.y)), fabsf(__fsub_rn(Q2.z, P1.z)))),
+                                   fmaxf(fmaxf(fabsf(__fsub_rn(Q3.x, P1.x)), fabsf(__fsub_rn(Q3.y, P1.y))),
+                                         fabsf(__fsub_rn(Q3.z, P1.z))));
+            const float Am = fmaxf(A, A2);
+            if (!(Am >= 0x1p-20f && Am <= 0x1p20f)) {
+                open = mask;  // the bounds could under- or overflow: all to FP64
+            } else {
+                DFTri t;
+                t.p2 = dfb3_rel(P2, P1);
+                t.p3 = dfb3_rel(P3, P1);
+                t.q1 = dfb3_rel(Q1, P1);
+                t.q2 = dfb3_rel(Q2, P1);
+                t.q3 = dfb3_rel(Q3, P1);
+                t.n1 = dfb3_cross(t.p2, dfb3_sub(t.p3, t.p2));
+                t.m1 = dfb3_cross(dfb3_sub(t.q2, t.q1), dfb3_sub(t.q3, t.q2));
+                while (mask) {
+                    const uint32_t k = __ffs(mask) - 1;
+                    mask &= mask - 1;
+                    const uint32_t r = dfb_axis_fp64(k, t);
+                    if (r == 0u) {
+                        separated = true;
+                        break;
+                    }
+                    if (r == 2u) open |= 1u << k;
+                }
+            }
+            if (!separated && open == 0u) hit = true;  // every axis overlaps in FP64
+            keep = !separated && open != 0u;
+            if (!keep) dis += (hit != ((item.y >> 31) != 0u)) ? 1u : 0u;
+            item.y = open | (item.y & 0x80000000u);
+        }
+        append_hit(a, hit, rec, lane);
+        const uint32_t q = warp_append(a.counts + kCountPrecLeft, keep, lane);
+        if (keep) left[q] = item;
+    }
+    const uint32_t nd = __reduce_add_sync(0xffffffffu, dis);
+    if (lane == 0 && nd) atomicAdd(a.counts + kCountDisagree, nd);
+}
+
 // FP64 setups (fp64_tri and the hit record) of the FP64 list's first
 // fp64_tri_cap entries, one entry per lane: formed here with every lane of a
 // warp busy, where k_prec_fp64 would form them in its refills with only the
@@ -1146,8 +1371,8 @@ __device__ __forceinline__ void fp64_tri_load(const double* base, uint32_t cap, 
 }
 __global__ void __launch_bounds__(kDetectThreads) k_prec_fp64_setup(DetectArgs a)
 {
-    const uint32_t n = min(min(a.counts[kCountPrecFp64], a.cand_cap), a.fp64_tri_cap);
-    const uint2* list = (const uint2*)(a.prec_lists + 2 * (size_t)a.cand_cap);
+    const uint32_t n = min(min(a.counts[kCountPrecLeft], a.cand_cap), a.fp64_tri_cap);
+    const uint2* list = (const uint2*)a.prec_lists;  // what the double-float pass left open
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         V3 P1, P2, P3, Q1, Q2, Q3;
         uint4 rec;
@@ -1165,8 +1390,8 @@ __global__ void __launch_bounds__(kDetectThreads) k_prec_fp64_setup(DetectArgs a
 // faces -> vertices and the setup's FP64 work).
 __global__ void __launch_bounds__(kDetectThreads) k_prec_fp64(DetectArgs a)
 {
-    const uint32_t n = min(a.counts[kCountPrecFp64], a.cand_cap);
-    const uint2* list = (const uint2*)(a.prec_lists + 2 * (size_t)a.cand_cap);
+    const uint32_t n = min(a.counts[kCountPrecLeft], a.cand_cap);
+    const uint2* list = (const uint2*)a.prec_lists;  // what the double-float pass left open
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
@@ -1319,9 +1544,10 @@ cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s)
 {
     if (a.precision) {
         if (a.prec_lists == nullptr || (a.fp64_tri_cap && a.fp64_tri == nullptr)) return cudaErrorInvalidValue;
-        note_launches(a.fp64_tri_cap ? 4 : 3);
+        note_launches(a.fp64_tri_cap ? 5 : 4);
         k_prec_classify<<<a.grid, kDetectThreads, 0, s>>>(a);
         k_prec_settle<<<a.grid, kDetectThreads, 0, s>>>(a);
+        k_prec_df<<<a.grid, kDetectThreads, 0, s>>>(a);
         if (a.fp64_tri_cap) k_prec_fp64_setup<<<a.grid, kDetectThreads, 0, s>>>(a);
         k_prec_fp64<<<a.grid, kDetectThreads, 0, s>>>(a);
         return cudaGetLastError();

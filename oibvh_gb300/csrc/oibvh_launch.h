@@ -136,7 +136,8 @@ constexpr uint32_t kFp64TriRows = 23;
 // counts[]: hits, flags, candidates found, candidate slots used (broad-only),
 // BVTT pairs tested, (precision mode) axes evaluated in FP64, candidates with
 // at least one such axis, candidates whose float and FP64 answers differ,
-// the sizes of the float-hit, recheck and FP64 lists of the precision narrow phase,
+// the sizes of the float-hit, recheck and FP64 lists of the precision narrow phase
+// and of the list its double-float pass leaves to FP64,
 // then the work-list size of each traversal round (list
 // 0: the overlapping start pairs; list 1: the front k_top hands over; list
 // r+1: what walk round r spilled), then how many items of each list the
@@ -144,7 +145,7 @@ constexpr uint32_t kFp64TriRows = 23;
 constexpr uint32_t kMaxRounds = 16;
 constexpr uint32_t kCountHits = 0, kCountFlags = 1, kCountCands = 2, kCountCandSlots = 3, kCountTested = 4,
                    kCountFp64Axes = 5, kCountFp64Cands = 6, kCountDisagree = 7, kCountPrecHits = 8,
-                   kCountPrecRecheck = 9, kCountPrecFp64 = 10, kCountWork0 = 11,
+                   kCountPrecRecheck = 9, kCountPrecFp64 = 10, kCountPrecLeft = 11, kCountWork0 = 12,
                    kCountClaim0 = kCountWork0 + kMaxRounds + 1,  // items of list r claimed so far
                    kCountTotal = kCountClaim0 + kMaxRounds + 1;
 

@@ -72,9 +72,9 @@ def test_near_degenerate_pairs(gpu, seed):
     assert np.array_equal(got64, want64), f"{_sym(got64, want64)} mismatches against the FP64 oracle"
     assert st64["candidates"] == cands
     assert st64["fp32_disagreements"] == _sym(want32, want64)
-    assert 0 < st64["fp64_candidates"] <= cands
-    # the FP64 pass takes only what the bounded pass left undecided
-    assert st64["fp64_candidates"] <= st64["bounded_candidates"] <= cands
+    # the FP64 pass takes only what the bounded and double-float passes left undecided
+    assert 0 <= st64["fp64_candidates"] <= st64["bounded_candidates"] <= cands
+    assert st64["bounded_candidates"] > 0
     assert st32["fp64_axes"] == 0 and st32["bounded_candidates"] == 0
 
 
@@ -136,7 +136,37 @@ def test_sheets_full_size_zero_mismatches(gpu):
         parts = list(ex.map(one, w.pairs))
     want64 = sort_pairs(np.concatenate(parts, 0))
     assert np.array_equal(got64, want64), f"{_sym(got64, want64)} mismatches against the FP64 oracle"
-    assert st["fp64_candidates"] > 0
+    # the double-float pass decides these (sheets within 1e-7 of each other) without FP64
+    assert st["bounded_candidates"] >= st["fp64_candidates"]
+
+
+def _coplanar_soup(seed, n_tri=600):
+    """Two soups of triangles in the plane z = 0.5 (exactly representable):
+    their normal axes project both sets to exactly the same value, so neither
+    the float bounds nor the double-float pass can decide them; FP64 does."""
+    from oibvh_gb300.meshes import Mesh
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(2):
+        c = rng.uniform(0.0, 1.0, (n_tri, 1, 2))
+        v = c + rng.uniform(-0.03, 0.03, (n_tri, 3, 2))
+        xyz = np.concatenate([v.reshape(-1, 2), np.full((3 * n_tri, 1), 0.5)], 1).astype(np.float32)
+        out.append(Mesh(xyz, np.arange(3 * n_tri, dtype=np.uint32).reshape(-1, 3)))
+    return out
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_coplanar_soups_take_the_fp64_pass(gpu, seed):
+    from oibvh_gb300 import _native as N
+
+    meshes = _coplanar_soup(seed)
+    _, want64, cands = _oracle_sets(meshes, None)
+    sc, _ = _scene(meshes, None)
+    got64, st = _run(sc, N.PRECISION_FP64_FILTERED)
+    assert np.array_equal(got64, want64), f"{_sym(got64, want64)} mismatches against the FP64 oracle"
+    assert st["candidates"] == cands
+    assert st["fp64_candidates"] > 0 and st["fp64_axes"] > 0  # the FP64 pass ran
 
 
 def test_precision_argument_checks(gpu):
