@@ -487,9 +487,10 @@ int detect_impl(oibvh_scene_s* s, int device_type, uint32_t entry, uint32_t expa
     return OIBVH_OK;
 }
 
-// Room for the FP64 setups of the next passes: twice the FP64 list this pass
-// had (the first pass forms every setup where it is used). A captured frame
-// that used the old buffer is captured again.
+// Room for the FP64 setups of the next passes: twice the list the
+// double-float pass left to FP64 this time (the first pass forms every setup
+// where it is used). A captured frame that used the old buffer is captured
+// again.
 int size_fp64_setups(oibvh_scene_s* s, uint32_t fp64_list)
 {
     const uint64_t want = std::min<uint64_t>(2ull * fp64_list, s->cand_cap);
@@ -551,7 +552,7 @@ int narrow_pass(oibvh_scene_s* s, uint32_t np, uint64_t hits_before, cudaStream_
         s->stats.fp64_candidates += c[kCountFp64Cands];
         s->stats.fp32_disagreements += c[kCountDisagree];
         s->stats.bounded_candidates += (uint64_t)c[kCountPrecHits] + c[kCountPrecRecheck];
-        if (s->precision) OK_TRY(size_fp64_setups(s, c[kCountPrecFp64]));
+        if (s->precision) OK_TRY(size_fp64_setups(s, c[kCountPrecLeft]));
         return OIBVH_OK;
     }
 }
