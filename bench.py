@@ -28,6 +28,7 @@ cores, one independent frame per thread.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -1324,6 +1325,17 @@ def run_ours_serving(args, rank, world, local):
         sampler.start()
 
     def run_stream(rate, n, seed):
+        # the load generator is Python: a cyclic-GC pass over the process's
+        # objects (tens of ms once the other workloads have run) would stall
+        # submission and count as queueing, so it stays off while a stream runs
+        gc.collect()
+        gc.disable()
+        try:
+            return _run_stream(rate, n, seed)
+        finally:
+            gc.enable()
+
+    def _run_stream(rate, n, seed):
         ab, mats = w.queries(n, seed=seed)
         rng = np.random.Generator(np.random.PCG64(seed + 7))
         arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
@@ -1345,6 +1357,8 @@ def run_ours_serving(args, rank, world, local):
             tickets[k] = tk.value
             lag[k] = now - target
         lat = np.empty(n)
+        queue = np.empty(n)
+        service = np.empty(n)
         sizes = np.empty(n)
         pairs = 0
         r = _native.QueryResult()
@@ -1352,6 +1366,8 @@ def run_ours_serving(args, rank, world, local):
         for k in range(n):
             _native.check(L.oibvh_server_wait(srv._h, int(tickets[k]), 600000, C.byref(r)), "oibvh_server_wait")
             lat[k] = 1e3 * lag[k] + (r.queue_us + r.service_us) / 1e3
+            queue[k] = r.queue_us / 1e3
+            service[k] = r.service_us / 1e3
             sizes[k] = r.batch_size
             pairs += r.n_pairs
             t_last = max(t_last, arrivals[k] + lag[k] + (r.queue_us + r.service_us) / 1e6)
@@ -1360,6 +1376,11 @@ def run_ours_serving(args, rank, world, local):
                 "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 4),
                                "p99": round(float(np.percentile(lat, 99)), 4),
                                "max": round(float(lat.max()), 4)},
+                "submit_lag_ms": {"p99": round(1e3 * float(np.percentile(lag, 99)), 4),
+                                  "max": round(1e3 * float(lag.max()), 4)},
+                "queue_ms": {"p99": round(float(np.percentile(queue, 99)), 4), "max": round(float(queue.max()), 4)},
+                "service_ms": {"p99": round(float(np.percentile(service, 99)), 4),
+                               "max": round(float(service.max()), 4)},
                 "mean_batch": round(float(sizes.mean()), 2), "pairs": int(pairs)}
 
     # warm-up stream (lane buffers grow to their working sizes)
@@ -1546,9 +1567,13 @@ def subconfigs_ours(args, local):
         "sweep": [{"offered_per_s": r["offered_per_s"], "queries": r["queries"],
                    "throughput_per_s": r["throughput_per_s"], "p50_ms": r["latency_ms"]["p50"],
                    "p99_ms": r["latency_ms"]["p99"], "max_ms": r["latency_ms"]["max"],
+                   "submit_lag_max_ms": r["submit_lag_ms"]["max"], "queue_p99_ms": r["queue_ms"]["p99"],
+                   "service_p99_ms": r["service_ms"]["p99"],
                    "mean_batch": r["mean_batch"]} for r in sv["sweep"]],
+        "server_redos": sv["server_stats"]["redos"], "max_batch_seen": sv["server_stats"]["max_batch_seen"],
         "plain_one_at_a_time": sv["plain_one_at_a_time"], "served_over_plain": sv["served_over_plain"],
-        "latency_how": "per query: (submit - scheduled Poisson arrival) + queue + service, host clock",
+        "latency_how": ("per query: (submit - scheduled Poisson arrival) + queue + service, host clock; "
+                        "the Python load generator runs with its cyclic GC off during a stream"),
         "gpu_launches": sv["gpu_launches"], "clocks": sv["clocks"],
     }
     if "cpu_baseline" in sv:

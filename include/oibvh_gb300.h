@@ -340,7 +340,10 @@ int oibvh_scene_destroy(oibvh_scene_t s);
  * internal node), allocated up front; n_lanes CUDA streams each carry one
  * batch at a time (at most max_batch queries). add_mesh registers built
  * trees (their current positions are the rest positions; the trees must
- * outlive the server); start launches the loop thread. submit is
+ * outlive the server); start allocates every lane's staging tables (for
+ * max_batch queries), BVTT work lists and hit queue with its pinned host
+ * copy, then launches the loop thread, so that the loop allocates only when
+ * a batch is redone with larger queues. submit is
  * thread-safe and returns at once; a query waits until its slot fits in the
  * arena (FIFO) and a lane is idle, then runs with every query admitted at
  * that moment. wait blocks until the query is done (OIBVH_ERR_TIMEOUT after

@@ -1226,31 +1226,39 @@ __device__ __forceinline__ DFB3 dfb3_rel(const V3& p, const V3& o)
 struct DFTri {
     DFB3 p2, p3, q1, q2, q3, n1, m1;
 };
-// Axis k (0: n1, 1: m1, 2 + 3i + j: e_i x f_j, 11 + i: e_i x n1, 14 + j: f_j x
-// m1) with the edges formed as the FP64 formula forms them (e1 = p2 - 0 = p2,
-// e3 = 0 - p3 = -p3 exactly, the others one subtraction).
-__device__ __forceinline__ DFB3 dfb_axis(uint32_t k, const DFTri& t)
+__device__ __forceinline__ DFB3 dfb3_sel(bool c, const DFB3& a, const DFB3& b)
 {
-    if (k == 0) return t.n1;
-    if (k == 1) return t.m1;
-    auto e = [&](uint32_t i) {
-        if (i == 0) return t.p2;
-        if (i == 1) return dfb3_sub(t.p3, t.p2);
-        return DFB3{DFB{df_neg(t.p3.x.v), t.p3.x.w}, DFB{df_neg(t.p3.y.v), t.p3.y.w}, DFB{df_neg(t.p3.z.v), t.p3.z.w}};
+    auto s = [c](const DFB& x, const DFB& y) {
+        return DFB{DF{c ? x.v.h : y.v.h, c ? x.v.l : y.v.l}, c ? x.w : y.w};
     };
-    auto f = [&](uint32_t j) {
-        if (j == 0) return dfb3_sub(t.q2, t.q1);
-        if (j == 1) return dfb3_sub(t.q3, t.q2);
-        return dfb3_sub(t.q1, t.q3);
-    };
-    if (k < 11) return dfb3_cross(e((k - 2) / 3), f((k - 2) % 3));
-    if (k < 14) return dfb3_cross(e(k - 11), t.n1);
-    return dfb3_cross(f(k - 14), t.m1);
+    return DFB3{s(a.x, b.x), s(a.y, b.y), s(a.z, b.z)};
+}
+// Axis k (0: n1, 1: m1, 2 + 3i + j: e_i x f_j, 11 + i: e_i x n1, 14 + j: f_j x
+// m1), e_i = (p2 - 0, p3 - p2, 0 - p3), f_j = (q2 - q1, q3 - q2, q1 - q3) as
+// the FP64 formula forms them (p2 - 0 and 0 - p3 are exact; their bounds
+// grow by one rounding's share, which only widens the intervals). The two
+// factors of the cross product are picked by selects, so the lanes of a warp
+// run one cross product whatever their axes; `edges` (warp-uniform) is false
+// when no lane of the warp is on a cross-product axis.
+__device__ __forceinline__ DFB3 dfb_axis(uint32_t k, const DFTri& t, bool edges)
+{
+    if (!edges) return dfb3_sel(k == 0, t.n1, t.m1);
+    const DFB z{DF{0.0f, 0.0f}, 0.0f};
+    const DFB3 Z{z, z, z};
+    const uint32_t i = k < 11 ? (k - 2) / 3 : k - 11;  // edge of A (axes 2..13)
+    const uint32_t j = k < 11 ? (k - 2) % 3 : k - 14;  // edge of B (axes 2..10, 14..16)
+    const DFB3 E = dfb3_sub(dfb3_sel(i == 0, t.p2, dfb3_sel(i == 1, t.p3, Z)),
+                            dfb3_sel(i == 0, Z, dfb3_sel(i == 1, t.p2, t.p3)));
+    const DFB3 F = dfb3_sub(dfb3_sel(j == 0, t.q2, dfb3_sel(j == 1, t.q3, t.q1)),
+                            dfb3_sel(j == 0, t.q1, dfb3_sel(j == 1, t.q2, t.q3)));
+    const bool ef = k >= 2 && k < 11, en = k >= 11 && k < 14;
+    const DFB3 c = dfb3_cross(dfb3_sel(ef || en, E, F), dfb3_sel(ef, F, dfb3_sel(en, t.n1, t.m1)));
+    return dfb3_sel(k == 0, t.n1, dfb3_sel(k == 1, t.m1, c));
 }
 // Axis k of FP64 known from double-floats: 0 = separates, 1 = overlaps, 2 = undecided.
-__device__ __forceinline__ uint32_t dfb_axis_fp64(uint32_t k, const DFTri& t)
+__device__ __forceinline__ uint32_t dfb_axis_fp64(uint32_t k, const DFTri& t, bool edges)
 {
-    const DFB3 ax = dfb_axis(k, t);
+    const DFB3 ax = dfb_axis(k, t, edges);
     const DFB P[3] = {DFB{DF{0.0f, 0.0f}, 0.0f}, dfb3_dot(ax, t.p2), dfb3_dot(ax, t.p3)};
     const DFB Q[3] = {dfb3_dot(ax, t.q1), dfb3_dot(ax, t.q2), dfb3_dot(ax, t.q3)};
     // intervals that hold the FP64 values: value as hi + lo (the sum's rounding
@@ -1272,67 +1280,113 @@ __device__ __forceinline__ uint32_t dfb_axis_fp64(uint32_t k, const DFTri& t)
     return 2u;
 }
 
-// The FP64 list through the double-float pass, one candidate per lane: its
-// undecided axes in order until one separates for sure; the axes still open
-// (and the float answer) go to the list the FP64 passes take.
+// Idle lanes that trigger a refill of the double-float pass (a refill forms
+// the new candidates' double-float vertices and normals with only the idle
+// lanes active, so refilling early costs setups, late costs idle steps).
+#ifndef OIBVH_DF_REFILL
+#define OIBVH_DF_REFILL 12
+#endif
+constexpr uint32_t kDfRefill = OIBVH_DF_REFILL;
+
+// The FP64 list through the double-float pass: each lane holds a candidate
+// and evaluates one of its undecided axes per step, all lanes of a warp on
+// the same instructions (dfb_axis picks the axis with selects), until an
+// axis separates for sure or the mask is done; the axes still open (and the
+// float answer) go to the list the FP64 passes take. A lane whose candidate
+// is decided is refilled from the warp's share of the list once enough lanes
+// are idle: the masks differ in length (most candidates end at their first
+// axis, coplanar ones run all of theirs), so a lane per candidate for the
+// whole walk would idle most lanes. The warp's share is chunks of 32
+// consecutive entries, grid-strided.
 __global__ void __launch_bounds__(kDetectThreads) k_prec_df(DetectArgs a)
 {
     const uint32_t n = min(a.counts[kCountPrecFp64], a.cand_cap);
     const uint2* list = (const uint2*)(a.prec_lists + 2 * (size_t)a.cand_cap);
     uint2* left = (uint2*)a.prec_lists;  // the float-hit and recheck lists' room, free after the bounded pass
     const uint32_t lane = threadIdx.x & 31;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    uint32_t dis = 0;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-        const uint32_t j = base + threadIdx.x;
-        bool hit = false, keep = false;
-        uint4 rec = make_uint4(0, 0, 0, 0);
-        uint2 item = make_uint2(0, 0);
-        if (j < n) {
-            item = list[j];
-            V3 P1, P2, P3, Q1, Q2, Q3;
-            load_tris(a, a.cand[item.x], P1, P2, P3, Q1, Q2, Q3, rec);
-            uint32_t mask = item.y & 0x1ffffu, open = 0;
-            bool separated = false;
-            const float A = fmaxf(fmaxf(fmaxf(fabsf(__fsub_rn(P2.x, P1.x)), fabsf(__fsub_rn(P2.y, P1.y))),
-                                        fmaxf(fabsf(__fsub_rn(P2.z, P1.z)), fabsf(__fsub_rn(P3.x, P1.x)))),
-                                  fmaxf(fmaxf(fabsf(__fsub_rn(P3.y, P1.y)), fabsf(__fsub_rn(P3.z, P1.z))),
-                                        fmaxf(fabsf(__fsub_rn(Q1.x, P1.x)), fabsf(__fsub_rn(Q1.y, P1.y)))));
-            const float A2 = fmaxf(fmaxf(fmaxf(fabsf(__fsub_rn(Q1.z, P1.z)), fabsf(__fsub_rn(Q2.x, P1.x))),
-                                         fmaxf(fabsf(__fsub_rn(Q2.y, P1.y)), fabsf(__fsub_rn(Q2.z, P1.z)))),
-                                   fmaxf(fmaxf(fabsf(__fsub_rn(Q3.x, P1.x)), fabsf(__fsub_rn(Q3.y, P1.y))),
-                                         fabsf(__fsub_rn(Q3.z, P1.z))));
-            const float Am = fmaxf(A, A2);
-            if (!(Am >= 0x1p-20f && Am <= 0x1p20f)) {
-                open = mask;  // the bounds could under- or overflow: all to FP64
-            } else {
-                DFTri t;
-                t.p2 = dfb3_rel(P2, P1);
-                t.p3 = dfb3_rel(P3, P1);
-                t.q1 = dfb3_rel(Q1, P1);
-                t.q2 = dfb3_rel(Q2, P1);
-                t.q3 = dfb3_rel(Q3, P1);
-                t.n1 = dfb3_cross(t.p2, dfb3_sub(t.p3, t.p2));
-                t.m1 = dfb3_cross(dfb3_sub(t.q2, t.q1), dfb3_sub(t.q3, t.q2));
-                while (mask) {
-                    const uint32_t k = __ffs(mask) - 1;
-                    mask &= mask - 1;
-                    const uint32_t r = dfb_axis_fp64(k, t);
-                    if (r == 0u) {
-                        separated = true;
-                        break;
+    const uint32_t W = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    // the t-th entry of this warp's share (increasing in t)
+    auto entry = [&](uint32_t t) { return (w + (t >> 5) * W) * 32u + (t & 31u); };
+    uint32_t t_next = 0, dis = 0;
+    bool more = entry(0) < n;
+    bool live = false;
+    uint2 item = make_uint2(0, 0);
+    uint4 rec = make_uint4(0, 0, 0, 0);
+    uint32_t mask = 0, open = 0;
+    bool separated = false;
+    DFTri t;
+    const DFB z{DF{0.0f, 0.0f}, 0.0f};
+    t.p2 = t.p3 = t.q1 = t.q2 = t.q3 = t.n1 = t.m1 = DFB3{z, z, z};
+    for (;;) {
+        const uint32_t idle = __ballot_sync(0xffffffffu, !live);
+        if (more && (__popc(idle) >= kDfRefill || idle == 0xffffffffu)) {
+            if (!live) {
+                const uint32_t j = entry(t_next + __popc(idle & ((1u << lane) - 1u)));
+                if (j < n) {
+                    item = list[j];
+                    V3 P1, P2, P3, Q1, Q2, Q3;
+                    load_tris(a, a.cand[item.x], P1, P2, P3, Q1, Q2, Q3, rec);
+                    live = true;
+                    mask = item.y & 0x1ffffu;
+                    open = 0;
+                    separated = false;
+                    const float A =
+                        fmaxf(fmaxf(fmaxf(fabsf(__fsub_rn(P2.x, P1.x)), fabsf(__fsub_rn(P2.y, P1.y))),
+                                    fmaxf(fabsf(__fsub_rn(P2.z, P1.z)), fabsf(__fsub_rn(P3.x, P1.x)))),
+                              fmaxf(fmaxf(fabsf(__fsub_rn(P3.y, P1.y)), fabsf(__fsub_rn(P3.z, P1.z))),
+                                    fmaxf(fabsf(__fsub_rn(Q1.x, P1.x)), fabsf(__fsub_rn(Q1.y, P1.y)))));
+                    const float A2 =
+                        fmaxf(fmaxf(fmaxf(fabsf(__fsub_rn(Q1.z, P1.z)), fabsf(__fsub_rn(Q2.x, P1.x))),
+                                    fmaxf(fabsf(__fsub_rn(Q2.y, P1.y)), fabsf(__fsub_rn(Q2.z, P1.z)))),
+                              fmaxf(fmaxf(fabsf(__fsub_rn(Q3.x, P1.x)), fabsf(__fsub_rn(Q3.y, P1.y))),
+                                    fabsf(__fsub_rn(Q3.z, P1.z))));
+                    const float Am = fmaxf(A, A2);
+                    if (!(Am >= 0x1p-20f && Am <= 0x1p20f)) {
+                        open = mask;  // the bounds could under- or overflow: all to FP64
+                        mask = 0;
+                    } else {
+                        t.p2 = dfb3_rel(P2, P1);
+                        t.p3 = dfb3_rel(P3, P1);
+                        t.q1 = dfb3_rel(Q1, P1);
+                        t.q2 = dfb3_rel(Q2, P1);
+                        t.q3 = dfb3_rel(Q3, P1);
+                        t.n1 = dfb3_cross(t.p2, dfb3_sub(t.p3, t.p2));
+                        t.m1 = dfb3_cross(dfb3_sub(t.q2, t.q1), dfb3_sub(t.q3, t.q2));
                     }
-                    if (r == 2u) open |= 1u << k;
                 }
             }
-            if (!separated && open == 0u) hit = true;  // every axis overlaps in FP64
-            keep = !separated && open != 0u;
-            if (!keep) dis += (hit != ((item.y >> 31) != 0u)) ? 1u : 0u;
-            item.y = open | (item.y & 0x80000000u);
+            t_next += __popc(idle);
+            more = entry(t_next) < n;
         }
+        if (!__any_sync(0xffffffffu, live)) {
+            if (!more) break;
+            continue;
+        }
+        const bool busy = live && mask != 0u;
+        if (__any_sync(0xffffffffu, busy)) {
+            const uint32_t k = busy ? __ffs(mask) - 1 : 0u;
+            const bool edges = __any_sync(0xffffffffu, busy && k >= 2);
+            const uint32_t r = dfb_axis_fp64(k, t, edges);
+            if (busy) {
+                mask &= mask - 1;
+                if (r == 0u) {
+                    separated = true;
+                    mask = 0;
+                } else if (r == 2u) {
+                    open |= 1u << k;
+                }
+            }
+        }
+        // decided lanes: the hit, or the entry with its open axes for FP64
+        const bool done = live && mask == 0u;
+        const bool hit = done && !separated && open == 0u;  // every axis overlaps in FP64
+        const bool keep = done && !separated && open != 0u;
+        if (done && !keep) dis += (hit != ((item.y >> 31) != 0u)) ? 1u : 0u;
         append_hit(a, hit, rec, lane);
         const uint32_t q = warp_append(a.counts + kCountPrecLeft, keep, lane);
-        if (keep) left[q] = item;
+        if (keep) left[q] = make_uint2(item.x, open | (item.y & 0x80000000u));
+        if (done) live = false;
     }
     const uint32_t nd = __reduce_add_sync(0xffffffffu, dis);
     if (lane == 0 && nd) atomicAdd(a.counts + kCountDisagree, nd);

@@ -189,6 +189,7 @@ struct oibvh_server_s {
 
     ~oibvh_server_s();
     void loop();
+    int reserve_lanes();
     int launch(Lane& L, std::vector<Query*>& batch);
     int enqueue_detect(Lane& L);
     int advance(Lane& L);
@@ -209,6 +210,41 @@ oibvh_server_s::~oibvh_server_s()
     }
     cv_submit.notify_all();
     if (worker.joinable()) worker.join();
+}
+
+// Every lane's staging tables (for max_batch queries), work lists, hit
+// queue and its pinned copy, allocated before the loop starts: a lane's first
+// batch, or the first batch larger than any before it, would otherwise
+// allocate in the loop (pinned host memory and cudaFree stall every lane for
+// milliseconds). Only a redo with larger queues allocates afterwards.
+int oibvh_server_s::reserve_lanes()
+{
+    const uint32_t per = refit_counters_per_tree();
+    const size_t n = max_batch;
+    for (auto& Lp : lanes) {
+        Lane& L = *Lp;
+        OK_TRY(ensure_pow2(L.h_views, 2 * n, "cudaMallocHost(views)"));
+        OK_TRY(ensure_pow2(L.views, 2 * n, "cudaMalloc(views)"));
+        OK_TRY(ensure_pow2(L.h_pairs, n, "cudaMallocHost(pairs)"));
+        OK_TRY(ensure_pow2(L.pairv, n, "cudaMalloc(pairs)"));
+        OK_TRY(ensure_pow2(L.h_jobs, n, "cudaMallocHost(jobs)"));
+        OK_TRY(ensure_pow2(L.jobs, n, "cudaMalloc(jobs)"));
+        OK_TRY(ensure_pow2(L.h_rjobs, n, "cudaMallocHost(refit jobs)"));
+        OK_TRY(ensure_pow2(L.rjobs, n, "cudaMalloc(refit jobs)"));
+        OK_TRY(ensure_pow2(L.h_mats, 12 * n, "cudaMallocHost(matrices)"));
+        OK_TRY(ensure_pow2(L.mats, 12 * n, "cudaMalloc(matrices)"));
+        OK_TRY(ensure_pow2(L.rcount, (size_t)per * n, "cudaMalloc(refit counters)"));
+        OK_TRY(L.counts.ensure(kCountTotal, "cudaMalloc(counts)"));
+        OK_TRY(L.h_counts.ensure(kCountTotal, "cudaMallocHost(counts)"));
+        L.front_cap = init_front_cap;
+        L.hit_cap = init_hit_cap;
+        L.cap_gen = cap_gen;
+        OK_TRY(L.front0.ensure(L.front_cap, "cudaMalloc(work list)"));
+        OK_TRY(L.front1.ensure(L.front_cap, "cudaMalloc(work list)"));
+        OK_TRY(L.hits.ensure(L.hit_cap, "cudaMalloc(hits)"));
+        OK_TRY(ensure_pow2(L.h_hits, L.hit_cap, "cudaMallocHost(hits)"));
+    }
+    return OIBVH_OK;
 }
 
 // One batch: tables, transform, refit, then the detect.
@@ -599,6 +635,8 @@ API int oibvh_server_start(oibvh_server_t s)
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->running) return OIBVH_OK;
     if (s->pool.empty()) return fail(OIBVH_ERR_STATE, "the pool is empty");
+    DeviceGuard g(s->device);
+    OK_TRY(s->reserve_lanes());
     s->running = true;
     s->worker = std::thread([s] { s->loop(); });
     return OIBVH_OK;
