@@ -1326,8 +1326,8 @@ def run_ours_serving(args, rank, world, local):
 
     def run_stream(rate, n, seed):
         # the load generator is Python: a cyclic-GC pass over the process's
-        # objects (tens of ms once the other workloads have run) would stall
-        # submission and count as queueing, so it stays off while a stream runs
+        # objects would stall submission and count as latency, so it stays
+        # off while a stream runs
         gc.collect()
         gc.disable()
         try:

@@ -882,10 +882,13 @@ __device__ __forceinline__ EV3 axis_of(uint32_t k, const LaneTri& t)
 //     lane: pass 1 of the filtered test (all 17 axes bounded, straight-line
 //     for float hits: no lane leaves early); what it leaves undecided goes to
 //     the FP64 list with the mask of its undecided axes.
-//  3. k_prec_fp64_setup forms each FP64 list entry's FP64 vertices and
-//     normals with every lane busy; k_prec_fp64 then evaluates the undecided
-//     axes in FP64, one axis per lane per iteration, lanes refilled from the
-//     list as their candidates are decided.
+//  3. k_prec_df evaluates those axes in double-float arithmetic with a bound
+//     on its own and FP64's errors, deciding each axis as FP64 would where
+//     the bound allows; the axes it leaves open go on.
+//  4. k_prec_fp64_setup forms each remaining entry's FP64 vertices and
+//     normals with every lane busy; k_prec_fp64 then evaluates the open axes
+//     in FP64, one axis per lane per iteration, lanes refilled from the list
+//     as their candidates are decided.
 // The pair set is the all-FP64 one by construction.
 // ---------------------------------------------------------------------------
 
