@@ -1429,9 +1429,9 @@ def run_ours_serving(args, rank, world, local):
         "served_over_plain": round(top["throughput_per_s"] / plain_qps, 2),
         "server_stats": st,
         "e2e": {"value": top["throughput_per_s"], "unit": "queries/s", "h2d_bytes_per_step": 48,
-                "d2h_bytes_per_step": round(16 * sweep_pairs / max(1, sweep_queries), 1),
+                "d2h_bytes_per_step": round(8 * sweep_pairs / max(1, sweep_queries) + 4, 1),
                 "note": "every served query is end to end: host submit -> host pairs; a step is one query "
-                        "(48 B of transform in, its hit records out)"},
+                        "(48 B of transform in; its pairs out, 8 B each, and a 4 B offset)"},
         "gpu_launches": int(sweep_launches),
         "gpu_launches_note": f"this library's kernels over the {sweep_queries} queries of the sweep",
         "clocks": clocks,

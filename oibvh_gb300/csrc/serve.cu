@@ -17,9 +17,11 @@
 //     and the counters copied back; so queries that arrive while earlier
 //     batches are on the GPU are admitted as lanes and memory free up, and
 //     batches on different lanes overlap on the device;
-//   * a batch completes in two stream-ordered steps (counters, then exactly
-//     the hit records) tracked by events; the loop never waits on the device
-//     while other work can be launched;
+//   * the batch's hits are grouped by query on the device; it completes in
+//     two stream-ordered steps (counters and per-query offsets, then exactly
+//     the grouped pairs, 8 B each) tracked by events, each query's pairs then
+//     one block copy on the host; the loop never waits on the device while
+//     other work can be launched;
 //   * a batch whose queues were too small (flags, or spill beyond the
 //     launched walk rounds) is redone on its lane with larger queues, so
 //     results are never truncated.
@@ -129,7 +131,10 @@ struct Lane {
     DevBuf<uint4> hits;
     DevBuf<uint32_t> counts;
     PinnedBuf<uint32_t> h_counts;
-    PinnedBuf<uint4> h_hits;
+    DevBuf<uint32_t> qcount, qcursor, qoff;  // per query of the batch: hit count, scatter cursor, offset
+    PinnedBuf<uint32_t> h_qoff;
+    DevBuf<uint2> out;     // the batch's (triA, triB) grouped by query
+    PinnedBuf<uint2> h_out;
     uint32_t front_cap = 0, hit_cap = 0;  // set from the server's capacities at the first batch
     uint32_t cap_gen = ~0u;  // queue capacities follow the server's settings of this generation
     uint32_t rounds = kServeWalkRoundsInit;
@@ -159,6 +164,80 @@ uint32_t grow(uint64_t need, uint32_t cur)
     uint64_t c = std::max<uint64_t>(need + need / 4 + 1024, (uint64_t)cur * 2);
     return (uint32_t)std::min<uint64_t>(c, 0x7fffffffull);
 }
+
+// A batch's hit records {view a = 2i, view b = 2i + 1, triA, triB} grouped
+// by query i on the device, so that the host takes each query's pairs as one
+// block (a copy) instead of sorting every record into its query: count per
+// query, exclusive scan, scatter of the (triA, triB) words. Lanes of a warp
+// on the same query combine their atomics (__match_any_sync). The order of
+// pairs within a query is not specified.
+constexpr uint32_t kNoQuery = 0xffffffffu;
+__global__ void k_bucket_count(const uint4* __restrict__ hits, const uint32_t* __restrict__ counts, uint32_t hit_cap,
+                               uint32_t* __restrict__ qcount)
+{
+    const uint32_t n = min(counts[kCountHits], hit_cap);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+        const uint32_t k = base + lane;
+        const uint32_t q = k < n ? __ldg(&hits[k].x) >> 1 : kNoQuery;
+        const uint32_t peers = __match_any_sync(0xffffffffu, q);
+        if (q != kNoQuery && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(qcount + q, (uint32_t)__popc(peers));
+    }
+}
+// One block: qoff[i] = sum of qcount[0..i), qoff[n] = the total; cursor = qoff.
+__global__ void __launch_bounds__(1024) k_bucket_scan(const uint32_t* __restrict__ qcount, uint32_t n,
+                                                      uint32_t* __restrict__ qoff, uint32_t* __restrict__ cursor)
+{
+    __shared__ uint32_t warp_sum[32];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
+    const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+    const uint32_t b = min(n, threadIdx.x * per), e = min(n, b + per);
+    uint32_t mine = 0;
+    for (uint32_t i = b; i < e; ++i) mine += qcount[i];
+    uint32_t x = mine;  // inclusive scan within the warp
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t v = lane < n_warps ? warp_sum[lane] : 0u;
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
+        }
+        warp_sum[lane] = v;  // inclusive over warps
+    }
+    __syncthreads();
+    uint32_t run = x - mine + (warp ? warp_sum[warp - 1] : 0u);
+    for (uint32_t i = b; i < e; ++i) {
+        qoff[i] = run;
+        cursor[i] = run;
+        run += qcount[i];
+    }
+    if (threadIdx.x == 0) qoff[n] = warp_sum[n_warps - 1];
+}
+__global__ void k_bucket_scatter(const uint4* __restrict__ hits, const uint32_t* __restrict__ counts, uint32_t hit_cap,
+                                 uint32_t* __restrict__ cursor, uint2* __restrict__ out)
+{
+    const uint32_t n = min(counts[kCountHits], hit_cap);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+        const uint32_t k = base + lane;
+        const uint4 h = k < n ? hits[k] : make_uint4(0, 0, 0, 0);
+        const uint32_t q = k < n ? h.x >> 1 : kNoQuery;
+        const uint32_t peers = __match_any_sync(0xffffffffu, q);
+        const uint32_t leader = __ffs(peers) - 1;
+        uint32_t pos = 0;
+        if (q != kNoQuery && lane == leader) pos = atomicAdd(cursor + q, (uint32_t)__popc(peers));
+        pos = __shfl_sync(0xffffffffu, pos, leader) + __popc(peers & ((1u << lane) - 1u));
+        if (q != kNoQuery) out[pos] = make_uint2(h.z, h.w);
+    }
+}
+constexpr uint32_t kBucketThreads = 256;
 
 }  // namespace
 
@@ -242,7 +321,12 @@ int oibvh_server_s::reserve_lanes()
         OK_TRY(L.front0.ensure(L.front_cap, "cudaMalloc(work list)"));
         OK_TRY(L.front1.ensure(L.front_cap, "cudaMalloc(work list)"));
         OK_TRY(L.hits.ensure(L.hit_cap, "cudaMalloc(hits)"));
-        OK_TRY(ensure_pow2(L.h_hits, L.hit_cap, "cudaMallocHost(hits)"));
+        OK_TRY(L.qcount.ensure(n + 1, "cudaMalloc(query counts)"));
+        OK_TRY(L.qcursor.ensure(n + 1, "cudaMalloc(query cursors)"));
+        OK_TRY(L.qoff.ensure(n + 1, "cudaMalloc(query offsets)"));
+        OK_TRY(L.h_qoff.ensure(n + 1, "cudaMallocHost(query offsets)"));
+        OK_TRY(L.out.ensure(L.hit_cap, "cudaMalloc(grouped pairs)"));
+        OK_TRY(ensure_pow2(L.h_out, L.hit_cap, "cudaMallocHost(grouped pairs)"));
     }
     return OIBVH_OK;
 }
@@ -265,6 +349,10 @@ int oibvh_server_s::launch(Lane& L, std::vector<Query*>& batch)
     OK_TRY(ensure_pow2(L.rcount, (size_t)per * n, "cudaMalloc(refit counters)"));
     OK_TRY(L.counts.ensure(kCountTotal, "cudaMalloc(counts)"));
     OK_TRY(L.h_counts.ensure(kCountTotal, "cudaMallocHost(counts)"));
+    OK_TRY(L.qcount.ensure((size_t)n + 1, "cudaMalloc(query counts)"));
+    OK_TRY(L.qcursor.ensure((size_t)n + 1, "cudaMalloc(query cursors)"));
+    OK_TRY(L.qoff.ensure((size_t)n + 1, "cudaMalloc(query offsets)"));
+    OK_TRY(L.h_qoff.ensure((size_t)n + 1, "cudaMallocHost(query offsets)"));
 
     // start level: the entry level, deepened so the batch's start cross
     // product holds about 2^start_log2 node pairs
@@ -366,7 +454,9 @@ int oibvh_server_s::enqueue_detect(Lane& L)
     OK_TRY(L.front0.ensure(L.front_cap, "cudaMalloc(work list)"));
     OK_TRY(L.front1.ensure(L.front_cap, "cudaMalloc(work list)"));
     OK_TRY(L.hits.ensure(L.hit_cap, "cudaMalloc(hits)"));
+    OK_TRY(L.out.ensure(L.hit_cap, "cudaMalloc(grouped pairs)"));
     CUDA_TRY(cudaMemsetAsync(L.counts.p, 0, kCountTotal * sizeof(uint32_t), st));
+    CUDA_TRY(cudaMemsetAsync(L.qcount.p, 0, L.n_pairs * sizeof(uint32_t), st));
     DetectArgs a{};
     a.trees = L.views.p;
     a.pairs = L.pairv.p;
@@ -384,7 +474,15 @@ int oibvh_server_s::enqueue_detect(Lane& L)
     CUDA_TRY(launch_init_front(a, (uint32_t)L.front0_count, st));
     CUDA_TRY(launch_top(a, st));
     for (uint32_t r = 1; r <= L.rounds; ++r) CUDA_TRY(launch_walk(a, r, st));
+    // the hits grouped by query (discarded if the batch is redone)
+    const uint32_t bgrid = (uint32_t)sm_count(device) * 2;
+    k_bucket_count<<<bgrid, kBucketThreads, 0, st>>>(L.hits.p, L.counts.p, L.hit_cap, L.qcount.p);
+    k_bucket_scan<<<1, 1024, 0, st>>>(L.qcount.p, L.n_pairs, L.qoff.p, L.qcursor.p);
+    k_bucket_scatter<<<bgrid, kBucketThreads, 0, st>>>(L.hits.p, L.counts.p, L.hit_cap, L.qcursor.p, L.out.p);
+    CUDA_TRY(cudaGetLastError());
+    note_launches(3);
     CUDA_TRY(cudaMemcpyAsync(L.h_counts.p, L.counts.p, kCountTotal * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(L.h_qoff.p, L.qoff.p, ((size_t)L.n_pairs + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaEventRecord(L.ev, st));
     L.phase = 1;
     return OIBVH_OK;
@@ -446,21 +544,17 @@ int oibvh_server_s::advance(Lane& L)
             stats.candidates += c[kCountCands];
             stats.hits += L.n_hits;
         }
-        OK_TRY(ensure_pow2(L.h_hits, std::max<uint64_t>(L.n_hits, L.hit_cap), "cudaMallocHost(hits)"));
+        OK_TRY(ensure_pow2(L.h_out, std::max<uint64_t>(L.n_hits, L.hit_cap), "cudaMallocHost(grouped pairs)"));
         if (L.n_hits)
-            CUDA_TRY(cudaMemcpyAsync(L.h_hits.p, L.hits.p, L.n_hits * sizeof(uint4), cudaMemcpyDeviceToHost, L.st));
+            CUDA_TRY(cudaMemcpyAsync(L.h_out.p, L.out.p, L.n_hits * sizeof(uint2), cudaMemcpyDeviceToHost, L.st));
         CUDA_TRY(cudaEventRecord(L.ev, L.st));
         L.phase = 2;
         return OIBVH_OK;
     }
-    // phase 2: hit records {view a = 2 i, view b = 2 i + 1, triA, triB} -> query i
-    for (Query* q : L.batch) q->pairs.clear();
-    for (uint64_t k = 0; k < L.n_hits; ++k) {
-        const uint4 h = L.h_hits.p[k];
-        Query* q = L.batch[h.x / 2];
-        q->pairs.push_back(h.z);
-        q->pairs.push_back(h.w);
-    }
+    // phase 2: query i's (triA, triB) words are h_out[qoff[i] .. qoff[i + 1])
+    const uint32_t* words = (const uint32_t*)L.h_out.p;
+    for (size_t i = 0; i < L.batch.size(); ++i)
+        L.batch[i]->pairs.assign(words + 2 * (size_t)L.h_qoff.p[i], words + 2 * (size_t)L.h_qoff.p[i + 1]);
     finish(L, OIBVH_OK, "");
     return OIBVH_OK;
 }

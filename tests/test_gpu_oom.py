@@ -2,8 +2,9 @@
 hook oibvh_debug_fail_alloc_after(n): the n-th allocation the library attempts
 from then on fails as cudaMalloc would (cudaErrorMemoryAllocation) without
 calling CUDA. Every allocation of tree creation and build, scene detect
-(including queue regrowth), frame capture and the server (creation and a
-batch's lane buffers) is made to fail in turn: the call reports
+(including queue regrowth), frame capture and the server (creation, the
+lane buffers allocated at start, a batch's reallocated queues) is made to
+fail in turn: the call reports
 OIBVH_ERR_OOM, and afterwards the same handles work and give the oracle's
 pair sets (or are destroyed cleanly). The reference ignores every CUDA error
 (include/cuda/utils.cuh:6-34) and has no such path."""
@@ -168,11 +169,32 @@ def test_server_creation_and_batch_report_oom_then_serve():
     h, _ = p.detect()
     want = sort_pairs(h)[:, 2:]
     assert want.shape[0] > 0
-    srv = Server(0, 64 << 20, 16, 1)
-    for t in trees:
-        srv.add_mesh(t)
+    def pool_server():
+        srv = Server(0, 64 << 20, 16, 1)
+        for t in trees:
+            srv.add_mesh(t)
+        return srv
+
+    # start allocates every lane's buffers: each of its allocations fails in
+    # turn, and a later start on the same server succeeds
+    srv = pool_server()
+    ks = _attempts(srv.start)
+    srv.close()
+    assert ks >= 10
+    for n in range(0, ks, 3):
+        srv = pool_server()
+        _expect_oom(n, srv.start)
+        srv.start()
+        t1 = srv.submit(0, 1, mat)
+        srv.wait(t1)
+        assert np.array_equal(srv.pairs(t1), want)
+        srv.release(t1)
+        srv.close()
+    # new queue capacities: the next batch reallocates its lane's queues, and
+    # that allocation fails
+    srv = pool_server()
     srv.start()
-    # the first batch sizes its lane's buffers: its first allocation fails
+    srv.set_queue_capacity(64, 64)
     N.lib().oibvh_debug_fail_alloc_after(0)
     t0 = srv.submit(0, 1, mat)
     with pytest.raises(N.OibvhError) as e:
@@ -180,9 +202,10 @@ def test_server_creation_and_batch_report_oom_then_serve():
     assert e.value.status == N.ERR_OOM
     N.lib().oibvh_debug_fail_alloc_after(-1)
     srv.release(t0)
-    for _ in range(2):  # the lane starts clean: later queries are served
+    for _ in range(2):  # the lane starts clean: later queries are served (queues regrown)
         t1 = srv.submit(0, 1, mat)
         srv.wait(t1)
         assert np.array_equal(srv.pairs(t1), want)
         srv.release(t1)
+    assert srv.stats()["redos"] >= 1
     srv.close()
