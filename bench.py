@@ -65,7 +65,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["batched", "precision", "serving", "deforming", "plain"], default="batched")
-    ap.add_argument("--rates", default="1000,3000,10000,30000,60000,100000", help="serving: offered query rates (1/s)")
+    ap.add_argument("--rates", default="1000,3000,10000,30000,60000,100000,150000", help="serving: offered query rates (1/s)")
     ap.add_argument("--pool", type=int, default=2000, help="serving: resident meshes")
     ap.add_argument("--budget-gb", type=float, default=16.0, help="serving: device memory budget for query slots")
     ap.add_argument("--pairs", type=int, default=512, help="mesh pairs of the batched workload")
@@ -1547,7 +1547,7 @@ def _free_device_memory():
         pass
 
 
-SERVED_RATES = "10000,30000,60000,100000"
+SERVED_RATES = "10000,30000,60000,100000,150000"
 
 
 def subconfigs_ours(args, local):
