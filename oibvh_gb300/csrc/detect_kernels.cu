@@ -1597,11 +1597,13 @@ int walk_blocks_per_sm(uint32_t walk_cap, bool fused)
     return n > 0 ? n : 1;
 }
 
+uint32_t narrow_kernels(const DetectArgs& a) { return a.precision ? (a.fp64_tri_cap ? 5u : 4u) : 1u; }
+
 cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s)
 {
     if (a.precision) {
         if (a.prec_lists == nullptr || (a.fp64_tri_cap && a.fp64_tri == nullptr)) return cudaErrorInvalidValue;
-        note_launches(a.fp64_tri_cap ? 5 : 4);
+        note_launches(narrow_kernels(a));
         k_prec_classify<<<a.grid, kDetectThreads, 0, s>>>(a);
         k_prec_settle<<<a.grid, kDetectThreads, 0, s>>>(a);
         k_prec_df<<<a.grid, kDetectThreads, 0, s>>>(a);

@@ -1441,7 +1441,7 @@ cudaError_t enqueue_frame(oibvh_scene_s* s, cudaStream_t st, cudaEvent_t* ev, ui
         n.fuse_narrow = 1;
         n.grid = sm_count(s->device) * 8;
         e = launch_narrow(n, st);
-        ++k;
+        k += narrow_kernels(n);
     }
     mark(5);
     if (e == cudaSuccess)

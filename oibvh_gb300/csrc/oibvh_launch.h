@@ -129,6 +129,7 @@ cudaError_t launch_walk(const DetectArgs& a, uint32_t round, cudaStream_t s);
 // default), for the fused (narrow phase inside) or the broad-only walker
 int walk_blocks_per_sm(uint32_t walk_cap = 0, bool fused = true);
 cudaError_t launch_narrow(const DetectArgs& a, cudaStream_t s);
+uint32_t narrow_kernels(const DetectArgs& a);  // kernels launch_narrow launches
 // Rows of a precision-mode FP64 setup: the relative vertices p2, p3, q1, q2,
 // q3 and the normals n1, m1 (x, y, z each), then the hit record (2 words).
 constexpr uint32_t kFp64TriRows = 23;
