@@ -424,7 +424,7 @@ int oibvh_server_destroy(oibvh_server_t s);
  *
  * The first call on a device resolves the scratch address (cudaGetSymbolAddress
  * with that device current) and caches it with the id of the device's
- * context: make that first call before any stream capture. A call in a new
+ * context: make that first call at start-up. A call in a new
  * context (after cudaDeviceReset) resolves it again. All calls share the one
  * scratch area and overwrite it (the counters are cleared at the start of
  * each call); calls whose GPU work overlaps (different host threads or

@@ -15,7 +15,7 @@
 // code cannot use the array's name as a device address, so the first call on
 // a device (with that device current) resolves the address with
 // cudaGetSymbolAddress and caches it together with the id of the device's
-// context; make that first call before any stream capture. A later call in a
+// context; make that first call at start-up. A later call in a
 // new context (after cudaDeviceReset) resolves it again. Every call shares
 // the one array: the counters are cleared at the start of each call, and
 // calls whose GPU work overlaps (several host threads, or several streams)
