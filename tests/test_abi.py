@@ -79,6 +79,7 @@ def test_extension_argument_errors_need_no_gpu():
     assert L.oibvh_server_submit(None, 0, 1, mat.ctypes.data_as(N._f32p), ctypes.byref(t)) == N.ERR_ARG
     assert L.oibvh_server_wait(None, 1, 10, None) == N.ERR_ARG
     assert L.oibvh_server_release(None, 1) == N.ERR_ARG
+    assert L.oibvh_server_start(None) == N.ERR_ARG
     assert L.oibvh_server_destroy(None) == N.OK
     # scene-level knobs on a null scene
     assert L.oibvh_scene_set_precision(None, 1) == N.ERR_ARG
