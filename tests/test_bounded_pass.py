@@ -11,8 +11,9 @@ every arithmetic when a margin (mn1 - mx2 or mn2 - mx1) exceeds tau = 2
 when both margins are below -tau. This replays that arithmetic in numpy
 float32 (correctly rounded, one rounding per operation; the device may fuse
 some of the bound's multiply-adds, which the factor 2 covers) and checks on
-random, nearly coplanar and rescaled triangle pairs that every axis the
-bounds decide is decided the same way by the FP64 formula.
+random, nearly and exactly coplanar triangle pairs, rescaled across the
+pass's range [2^-20, 2^20] and to its ends, that every axis the bounds decide
+is decided the same way by the FP64 formula.
 """
 import numpy as np
 
@@ -106,9 +107,10 @@ def _decisions(P1, P2, P3, Q1, Q2, Q3):
 def test_bounded_decisions_agree_with_fp64():
     rng = np.random.default_rng(1204)
     decided_sep = decided_overlap = 0
-    for trial in range(18):
+    for trial in range(24):
         n = 20000
-        scale = np.float32(2.0 ** rng.integers(-18, 18))
+        # the last six trials at the ends of the range (2^-20: bounds in the float subnormals)
+        scale = np.float32(2.0 ** (rng.integers(-18, 18) if trial < 18 else (-20.5, 18.5)[trial % 2]))
         P = (rng.standard_normal((n, 3, 3)) * scale).astype(np.float32)
         jitter = rng.standard_normal((n, 3, 3)) * float(scale) * 10.0 ** rng.uniform(-7, 0)
         Q = (P[:, rng.permutation(3)] + jitter).astype(np.float32)

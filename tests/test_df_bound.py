@@ -12,8 +12,9 @@ float32. The FP64 values follow the FP64 pass's formula (relative vertices,
 edges, cross products, dot products in the reference's operation order,
 src/utils/utils.cpp:97-169, one rounding per operation). Inputs: random
 triangle pairs, nearly coplanar ones and exactly coplanar ones, at relative
-extents across [2^-18, 2^18]; the check covers every axis of each pair, not
-only the axes a pass would visit.
+extents across [2^-18, 2^18], and at the ends of the pass's range [2^-20,
+2^20] with collinear triangles, shared vertices and shared edges; the check
+covers every axis of each pair, not only the axes a pass would visit.
 """
 from fractions import Fraction as Fr
 
@@ -238,3 +239,39 @@ def test_rounding_helper_matches_numpy():
         up, dn = _round(_exact(a) * _exact(b), "ru"), _round(_exact(a) * _exact(b), "rd")
         assert _exact(dn) <= _exact(a) * _exact(b) <= _exact(up)
         assert up == dn or np.nextafter(dn, _UP) == up
+
+
+def _edge_pairs(rng):
+    """Relative extents at the ends of the pass's range (2^-20: low parts and
+    bounds in the float subnormals) and inside it; collinear (zero-area)
+    triangles, a shared vertex, coplanar triangles sharing an edge."""
+    out = []
+    for t in range(48):
+        scale = (2.0 ** -20.5, 2.0 ** -20, 2.0 ** 18.5, 1.0, 2.0 ** -10, 2.0 ** 10)[t % 6]
+        P = rng.standard_normal((3, 3)) * scale
+        form = t % 4
+        if form == 0:  # A collinear
+            P[2] = P[0] + 0.5 * (P[1] - P[0])
+            Q = P[rng.permutation(3)] + rng.standard_normal((3, 3)) * scale * 1e-3
+        elif form == 1:  # a shared vertex
+            Q = P.copy()
+            Q[1:] += rng.standard_normal((2, 3)) * scale
+        elif form == 2:  # coplanar, sharing an edge
+            P[:, 2] = scale
+            Q = P.copy()
+            Q[2] = P[2] + rng.standard_normal(3) * scale
+            Q[2, 2] = scale
+        else:
+            Q = P[rng.permutation(3)] + rng.standard_normal((3, 3)) * scale * 1e-3
+        P32, Q32 = P.astype(np.float32), Q.astype(np.float32)
+        A = np.abs(np.concatenate([P32[1:] - P32[0], Q32 - P32[0]])).max()
+        if 2.0 ** -20 <= A <= 2.0 ** 20:  # the pass's range (others go to FP64 whole)
+            out.append((P32, Q32))
+    return out
+
+
+def test_double_float_intervals_at_the_range_ends_and_degenerate_triangles():
+    pairs = _edge_pairs(np.random.default_rng(99))
+    assert len(pairs) >= 40
+    for P, Q in pairs:
+        check_pair(P, Q)
