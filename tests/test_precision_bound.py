@@ -43,9 +43,10 @@ def _margins(P1, P2, P3, Q1, Q2, Q3):
 def test_robust_float_hits_are_fp64_hits():
     rng = np.random.default_rng(2026)
     robust_total = 0
-    for trial in range(24):
+    for trial in range(30):
         n = 20000
-        scale = np.float32(2.0 ** rng.integers(-18, 18))
+        # the last six trials at the ends of the rule's range [2^-20, 2^20]
+        scale = np.float32(2.0 ** (rng.integers(-18, 18) if trial < 24 else (-20.5, 18.5)[trial % 2]))
         P = (rng.standard_normal((n, 3, 3)) * scale).astype(np.float32)
         jitter = rng.standard_normal((n, 3, 3)) * float(scale) * 10.0 ** rng.uniform(-7, 0)
         Q = (P[:, rng.permutation(3)] + jitter).astype(np.float32)
